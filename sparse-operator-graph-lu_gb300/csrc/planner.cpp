@@ -1,0 +1,527 @@
+// Recursive 2x2 block LU via explicit inverses, planned in two levels, then
+// level-scheduled. Emits the same op DAG as the reference planner
+// (BlockPlanner.cpp:103-374, 865-1292, 1305-1577; solver.cpp:56-110):
+//
+//   [L11,U11] = LU(A11); Li = L11^-1; Ui = U11^-1
+//   U12 = Li*A12; L21 = A21*Ui; S = A22 - L21*U12; [L22,U22] = LU(S)
+//
+// Block matrices are quadtrees over a power-of-two grid of blocks; absent
+// children are zero blocks and generate no ops.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "plan.h"
+
+namespace sog {
+namespace {
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct QNode {
+    int32_t level, id;
+    int32_t ch[4];  // 0 = b11, 1 = b12, 2 = b21, 3 = b22; 0 = absent
+};
+
+// Op emitter over one block-id space (one planning level).
+struct Emitter {
+    std::vector<QNode> nodes;  // nodes[0] is the "absent" sentinel
+    std::vector<Op> ops;
+    int32_t storage = 1;  // next block id; id 0 = none
+    int32_t* seq;         // op sequence counter shared by both levels (operation.cpp:84-95)
+
+    explicit Emitter(int32_t* s) : seq(s) { nodes.push_back({-1, 0, {0, 0, 0, 0}}); }
+
+    int32_t node(int level) {
+        nodes.push_back({level, 0, {0, 0, 0, 0}});
+        return (int32_t)nodes.size() - 1;
+    }
+    QNode& at(int32_t i) { return nodes[i]; }
+    int32_t fresh_id() { return storage++; }
+    void emit(int32_t op, int32_t src, int32_t src2, int32_t res, int32_t res2, int32_t group) {
+        ops.push_back({op, src, src2, res, res2, 0, ++*seq, group});
+    }
+    int32_t child_or_new(int32_t c, int q) {
+        int32_t k = at(c).ch[q];
+        if (k == 0) {
+            k = node(at(c).level - 1);
+            at(c).ch[q] = k;
+        }
+        return k;
+    }
+
+    // c (+/-)= a * b  (BlockPlanner.cpp:1230-1283)
+    void mul(int32_t a, int32_t b, int32_t c, int32_t group, int32_t kind) {
+        if (a == 0 || b == 0) return;
+        if (at(a).level == 0) {
+            if (at(a).id > 0 && at(b).id > 0) {
+                if (at(c).id <= 0) at(c).id = fresh_id();
+                emit(kind, at(a).id, at(b).id, at(c).id, 0, group);
+            }
+            return;
+        }
+        for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++)
+                for (int k = 0; k < 2; k++) {
+                    int32_t ak = at(a).ch[i * 2 + k], bk = at(b).ch[k * 2 + j];
+                    if (ak != 0 && bk != 0) {
+                        int32_t ck = child_or_new(c, i * 2 + j);
+                        mul(ak, bk, ck, group, kind);
+                    }
+                }
+    }
+    // c = a - b, with copy / negate where one side is absent (BlockPlanner.cpp:1126-1201)
+    void sub(int32_t a, int32_t b, int32_t c, int32_t group) {
+        if (at(a).level == 0) {
+            if (at(a).id > 0 || at(b).id > 0) {
+                if (at(c).id <= 0) at(c).id = fresh_id();
+                emit(OP_SUB, at(b).id, at(a).id, at(c).id, 0, group);
+            }
+            return;
+        }
+        for (int i = 0; i < 4; i++) {
+            int32_t ai = at(a).ch[i], bi = at(b).ch[i];
+            if (ai == 0 && bi == 0) continue;
+            int32_t ci = child_or_new(c, i);
+            if (ai != 0 && bi != 0) sub(ai, bi, ci, group);
+            else if (ai != 0) copy(ai, ci, group);
+            else neg(bi, ci, group);
+        }
+    }
+    void copy(int32_t a, int32_t c, int32_t group) {
+        if (at(a).level == 0) {
+            if (at(a).id > 0) {
+                if (at(c).id <= 0) at(c).id = fresh_id();
+                emit(OP_SUB, 0, at(a).id, at(c).id, 0, group);
+            }
+            return;
+        }
+        for (int i = 0; i < 4; i++)
+            if (at(a).ch[i] != 0) {
+                int32_t ci = child_or_new(c, i);
+                copy(at(a).ch[i], ci, group);
+            }
+    }
+    void neg(int32_t b, int32_t c, int32_t group) {
+        if (at(b).level == 0) {
+            if (at(b).id > 0) {
+                if (at(c).id <= 0) at(c).id = fresh_id();
+                emit(OP_SUB, at(b).id, 0, at(c).id, 0, group);
+            }
+            return;
+        }
+        for (int i = 0; i < 4; i++)
+            if (at(b).ch[i] != 0) {
+                int32_t ci = child_or_new(c, i);
+                neg(at(b).ch[i], ci, group);
+            }
+    }
+    // y = l^-1 for block lower-triangular l; a3, when given, already holds the
+    // inverse of l's leading quadrant (BlockPlanner.cpp:1019-1054).
+    void inv_lower(int32_t l, int32_t y, int32_t a3, int32_t group) {
+        if (at(l).level == 0) {
+            if (at(l).id > 0) {
+                at(y).id = fresh_id();
+                emit(OP_LOWERINV, at(l).id, 0, at(y).id, 0, group);
+            }
+            return;
+        }
+        int32_t a = at(l).ch[0], c = at(l).ch[2], d = at(l).ch[3];
+        int lev = at(a).level;
+        int32_t d1 = node(lev);
+        inv_lower(d, d1, 0, group);
+        at(y).ch[3] = d1;
+        int32_t d1c = node(lev);
+        mul(d1, c, d1c, group, OP_MUL);
+        int32_t a1 = a3;
+        if (a1 == 0) {
+            a1 = node(lev);
+            inv_lower(a, a1, 0, group);
+        }
+        at(y).ch[0] = a1;
+        int32_t c21 = node(lev);
+        mul(d1c, a1, c21, group, OP_MULNEG);
+        at(y).ch[2] = c21;
+    }
+    // y = u^-1 for block upper-triangular u (BlockPlanner.cpp:1056-1092).
+    void inv_upper(int32_t u, int32_t y, int32_t a3, int32_t group) {
+        if (at(u).level == 0) {
+            if (at(u).id > 0) {
+                at(y).id = fresh_id();
+                emit(OP_UPPERINV, at(u).id, 0, at(y).id, 0, group);
+            }
+            return;
+        }
+        int32_t a = at(u).ch[0], b = at(u).ch[1], d = at(u).ch[3];
+        int lev = at(a).level;
+        int32_t a2 = a3;
+        if (a2 == 0) {
+            a2 = node(lev);
+            inv_upper(a, a2, 0, group);
+        }
+        at(y).ch[0] = a2;
+        int32_t a1b = node(lev);
+        mul(a2, b, a1b, group, OP_MUL);
+        int32_t d1 = node(lev);
+        inv_upper(d, d1, 0, group);
+        at(y).ch[3] = d1;
+        int32_t a1bd1 = node(lev);
+        mul(a1b, d1, a1bd1, group, OP_MULNEG);
+        at(y).ch[1] = a1bd1;
+    }
+    // [l, u] = LU(a); l3/u3, when given, receive the inverses of l's and u's
+    // leading quadrants for the caller to reuse (BlockPlanner.cpp:865-939).
+    void lu(int32_t a, int32_t l, int32_t u, int32_t l3, int32_t u3, int32_t group) {
+        if (at(a).level == 0) {
+            if (at(a).id > 0) {
+                if (at(l).id <= 0) at(l).id = fresh_id();
+                if (at(u).id <= 0) at(u).id = fresh_id();
+                emit(OP_LU, at(a).id, 0, at(l).id, at(u).id, group);
+            }
+            return;
+        }
+        int lev = at(a).level;
+        int32_t ha = at(a).ch[0];
+        int32_t l1 = node(lev - 1), u1 = node(lev - 1);
+        int32_t l2 = l3, u2 = u3;
+        if (l2 == 0) {
+            l2 = node(lev - 1);
+            u2 = node(lev - 1);
+        }
+        int32_t hl1 = 0, hu1 = 0;
+        if (lev > 1) {
+            hl1 = node(lev - 2);
+            hu1 = node(lev - 2);
+        }
+        lu(ha, l1, u1, hl1, hu1, group);
+        inv_lower(l1, l2, hl1, group);
+        inv_upper(u1, u2, hu1, group);
+        at(l).ch[0] = l1;
+        at(u).ch[0] = u1;
+        int32_t aua1b = node(lev - 1);
+        int32_t b = at(a).ch[1];
+        if (b != 0) {
+            mul(l2, b, aua1b, group, OP_MUL);
+            at(u).ch[1] = aua1b;
+        }
+        int32_t dsub = node(lev - 1);
+        int32_t d = at(a).ch[3], c = at(a).ch[2];
+        if (c != 0) {
+            int32_t ca1al = node(lev - 1);
+            mul(c, u2, ca1al, group, OP_MUL);
+            at(l).ch[2] = ca1al;
+            int32_t ca1b = node(lev - 1);
+            mul(ca1al, aua1b, ca1b, group, OP_MUL);
+            sub(d, ca1b, dsub, group);
+        } else {
+            dsub = d;
+        }
+        int32_t nl1 = node(lev - 1), nu1 = node(lev - 1);
+        int32_t dl1 = 0, du1 = 0;
+        if (lev > 1) {
+            dl1 = node(lev - 2);
+            du1 = node(lev - 2);
+        }
+        lu(dsub, nl1, nu1, dl1, du1, group);
+        at(l).ch[3] = nl1;
+        at(u).ch[3] = nu1;
+    }
+
+    // quadtree of input blocks over a grid of `rows` x `rows` blocks
+    int32_t root_for(int rows) { return node(__builtin_popcount((unsigned)(rows - 1))); }
+    // get-or-create the leaf at (bi, bj) (matrix.cpp:65-88); returns the leaf node
+    int32_t leaf_at(int32_t root, int bi, int bj) {
+        int32_t cur = root;
+        for (int step = at(root).level; step > 0; step--) {
+            int q = (((bi >> (step - 1)) & 1) << 1) | ((bj >> (step - 1)) & 1);
+            cur = child_or_new(cur, q);
+        }
+        return cur;
+    }
+    int32_t find_leaf(int32_t root, int bi, int bj) {
+        int32_t cur = root;
+        for (int step = at(root).level; step > 0 && cur != 0; step--) {
+            int q = (((bi >> (step - 1)) & 1) << 1) | ((bj >> (step - 1)) & 1);
+            cur = at(cur).ch[q];
+        }
+        return cur;
+    }
+    void collect(int32_t m, int bi, int bj, std::vector<Leaf>& out) {
+        if (m == 0) return;
+        if (at(m).level == 0) {
+            if (at(m).id > 0) out.push_back({bi, bj, at(m).id});
+            return;
+        }
+        int h = 1 << (at(m).level - 1);
+        for (int q = 0; q < 4; q++) collect(at(m).ch[q], bi + (q >> 1) * h, bj + (q & 1) * h, out);
+    }
+};
+
+struct OpOrder {
+    bool operator()(const Op& x, const Op& y) const {
+        if (x.stage != y.stage) return x.stage < y.stage;
+        if (x.group != y.group) return x.group < y.group;
+        if (x.res != y.res) return x.res < y.res;
+        if (x.src != y.src) return x.src < y.src;
+        return x.seq < y.seq;
+    }
+};
+
+// Liveness, dead-op elimination, stage assignment and ordering
+// (BlockPlanner.cpp:103-374). `inputs` / `outputs` are block ids.
+void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>& inputs,
+              const std::vector<int32_t>& outputs, bool always_prune) {
+    std::vector<int32_t> lastuse(storage, 0), stage(storage, 0);
+    stage[0] = 1;
+    for (int32_t id : inputs) { stage[id] = 1; lastuse[id] = 0; }
+    for (int32_t id : outputs) lastuse[id] = storage;
+    // backward liveness: a source is live if any op writing a live block reads it
+    for (int64_t i = (int64_t)ops.size() - 1; i >= 0; i--) {
+        const Op& o = ops[i];
+        int32_t mark = 0;
+        if (o.res > 0) { mark = o.res; if (o.res2 > 0 && o.res2 > mark) mark = o.res2; }
+        if (o.res > 0 && o.res2 > 0 && lastuse[o.res] == 0 && lastuse[o.res2] == 0) continue;
+        if (o.res > 0 && o.res2 == 0 && lastuse[o.res] == 0) continue;
+        if (mark > 0) {
+            if (o.src > 0 && lastuse[o.src] < mark) lastuse[o.src] = mark;
+            if (o.src2 > 0) {
+                if (o.src2 >= storage) continue;
+                if (lastuse[o.src2] < mark) lastuse[o.src2] = mark;
+            }
+        }
+    }
+    size_t waste = 0;
+    for (const Op& o : ops) {
+        if (lastuse[o.res] > 0) continue;
+        if (o.res2 > 0 && lastuse[o.res2] > 0) continue;
+        waste++;
+    }
+    if (always_prune || waste > ops.size() / 25) {
+        size_t w = 0;
+        for (size_t i = 0; i < ops.size(); i++) {
+            const Op& o = ops[i];
+            if (lastuse[o.res] > 0 || (o.res2 > 0 && lastuse[o.res2] > 0)) ops[w++] = o;
+        }
+        ops.resize(w);
+    }
+    // stage = 1 + max(stage of sources), at least 2 (BlockPlanner.cpp:225-266)
+    for (Op& o : ops) {
+        int32_t s = 0;
+        if (o.src > 0) {
+            s = std::max(stage[o.src] + 1, 2);
+            if (o.src2 > 0) s = std::max(s, stage[o.src2] + 1);
+        } else {
+            if (o.src2 > 0) s = std::max(s, stage[o.src2] + 1);
+            s = std::max(s, 2);
+        }
+        o.stage = s;
+        if (o.res > 0 && stage[o.res] < s) stage[o.res] = s;
+        if (o.res2 > 0 && stage[o.res2] < s) stage[o.res2] = s;
+    }
+    // every single-result writer of a block moves to that block's last write stage
+    for (int64_t i = (int64_t)ops.size() - 1; i >= 0; i--) {
+        Op& o = ops[i];
+        if (o.res2 > 0) continue;
+        if (o.res > 0 && stage[o.res] > o.stage) o.stage = stage[o.res];
+    }
+    std::sort(ops.begin(), ops.end(), OpOrder());
+    // stages of more than 8000 ops are split (BlockPlanner.cpp:335-354)
+    int32_t jump = 0, band = 0, cur = 0;
+    for (Op& o : ops) {
+        if (o.stage > cur) { cur = o.stage; band = 0; }
+        if (band > 8000) { jump++; band = 0; }
+        o.stage += jump;
+        band++;
+    }
+}
+
+}  // namespace
+
+void mirror_triplets(int n, int64_t nnz, bool symmetric, const int32_t* I, const int32_t* J, const double* V,
+                     std::vector<int32_t>& Io, std::vector<int32_t>& Jo, std::vector<double>& Vo) {
+    Io.clear(); Jo.clear(); Vo.clear();
+    Io.reserve(symmetric ? 2 * nnz : nnz);
+    Jo.reserve(Io.capacity());
+    Vo.reserve(Io.capacity());
+    for (int64_t k = 0; k < nnz; k++) {
+        if (I[k] < 0 || I[k] >= n || J[k] < 0 || J[k] >= n) throw std::runtime_error("triplet index out of range");
+        Io.push_back(I[k]); Jo.push_back(J[k]); Vo.push_back(V ? V[k] : 0.0);
+        if (symmetric && I[k] != J[k]) { Io.push_back(J[k]); Jo.push_back(I[k]); Vo.push_back(V ? V[k] : 0.0); }
+    }
+}
+
+Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int32_t* J0, const double* V0,
+                int threads) {
+    if (symmetric) throw std::runtime_error("symmetric (LL^T) input is not supported by this executor");
+    if (n <= 0) throw std::runtime_error("dimension must be positive");
+    Plan p;
+    double t0 = now_s();
+    std::vector<int32_t> I, J;
+    std::vector<double> V;
+    mirror_triplets(n, nnz, symmetric, I0, J0, V0, I, J, V);
+    p.cfg = make_config(n);
+    p.ord = gps_order(n, I, J, V, threads);
+    for (size_t k = 0; k < I.size(); k++) { I[k] = p.ord.old_to_new[I[k]]; J[k] = p.ord.old_to_new[J[k]]; }
+    p.t_order = now_s() - t0;
+    double t1 = now_s();
+
+    const int R = p.cfg.block_rows, R2 = p.cfg.block_rows_l2, bs2 = p.cfg.block_size_l2;
+    const int sh2 = __builtin_popcount((unsigned)(bs2 - 1));
+    const int n_ext = p.cfg.n_ext();
+    int32_t seq = 0;
+
+    // ---- coarse level (PlanL2, BlockPlanner.cpp:1470-1490): blocks in first-touch order
+    Emitter cz(&seq);
+    int32_t croot = cz.root_for(R2);
+    std::vector<int32_t> cinputs;
+    auto ctouch = [&](int bi, int bj) {
+        int32_t lf = cz.leaf_at(croot, bi, bj);
+        if (cz.at(lf).id == 0) { cz.at(lf).id = cz.fresh_id(); cinputs.push_back(cz.at(lf).id); }
+        return lf;
+    };
+    for (size_t k = 0; k < I.size(); k++) ctouch(I[k] >> sh2, J[k] >> sh2);
+    for (int i = n; i < n_ext; i++) ctouch(i / bs2, i / bs2);
+    int32_t cl = cz.root_for(R2), cu = cz.root_for(R2);
+    cz.lu(croot, cl, cu, 0, 0, 0);
+    p.coarse_ops_emitted = (int64_t)cz.ops.size();
+    std::vector<Leaf> cL, cU;
+    cz.collect(cl, 0, 0, cL);
+    cz.collect(cu, 0, 0, cU);
+    {
+        std::vector<int32_t> outs;
+        for (auto& lf : cL) outs.push_back(lf.id);
+        for (auto& lf : cU) outs.push_back(lf.id);
+        schedule(cz.ops, cz.storage, cinputs, outs, true);
+    }
+    p.coarse_ops = (int64_t)cz.ops.size();
+
+    // ---- fine level: input tiles in (block row, block col) order (BlockPlanner.cpp:1491-1539)
+    Emitter fz(&seq);
+    int32_t froot = fz.root_for(R);
+    {
+        std::vector<int64_t> keys(I.size());
+        for (size_t k = 0; k < I.size(); k++) keys[k] = (int64_t)(I[k] >> 6) * R + (J[k] >> 6);
+        std::vector<int64_t> uk(keys);
+        std::sort(uk.begin(), uk.end());
+        uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+        for (int64_t key : uk) {
+            int32_t lf = fz.leaf_at(froot, (int)(key / R), (int)(key % R));
+            fz.at(lf).id = fz.fresh_id();
+            p.input_bi.push_back((int32_t)(key / R));
+            p.input_bj.push_back((int32_t)(key % R));
+        }
+        for (int i = n; i < n_ext; i++) {
+            int bi = i >> 6;
+            int32_t lf = fz.leaf_at(froot, bi, bi);
+            if (fz.at(lf).id == 0) {
+                fz.at(lf).id = fz.fresh_id();
+                p.input_bi.push_back(bi);
+                p.input_bj.push_back(bi);
+            }
+            p.pad_tile.push_back(fz.at(lf).id - 1);
+            p.pad_off.push_back((int16_t)((i & 63) * 64 + (i & 63)));
+        }
+        p.n_input = fz.storage - 1;
+        // the unpivoted recursion needs every diagonal block present (the
+        // reference dereferences a missing one, BlockPlanner.cpp:881)
+        for (int bi = 0; bi < R; bi++)
+            if (fz.find_leaf(froot, bi, bi) == 0 || fz.at(fz.find_leaf(froot, bi, bi)).id == 0)
+                throw std::runtime_error("structurally zero diagonal block " + std::to_string(bi));
+        // value scatter: last occurrence of a duplicate wins
+        p.scatter_tile.resize(I.size());
+        p.scatter_off.resize(I.size());
+        std::vector<int32_t> order(I.size());
+        for (size_t k = 0; k < I.size(); k++) {
+            int32_t lf = fz.find_leaf(froot, I[k] >> 6, J[k] >> 6);
+            p.scatter_tile[k] = fz.at(lf).id - 1;
+            p.scatter_off[k] = (int16_t)((I[k] & 63) * 64 + (J[k] & 63));
+            order[k] = (int32_t)k;
+        }
+        std::vector<int64_t> slot(I.size());
+        for (size_t k = 0; k < I.size(); k++) slot[k] = (int64_t)p.scatter_tile[k] * 4096 + p.scatter_off[k];
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return slot[a] < slot[b]; });
+        for (size_t k = 0; k + 1 < order.size(); k++)
+            if (slot[order[k]] == slot[order[k + 1]]) p.scatter_tile[order[k]] = -1;
+    }
+    std::vector<int32_t> finputs;
+    for (int32_t id = 1; id <= p.n_input; id++) finputs.push_back(id);
+
+    // coarse input block -> fine subtree at the same position (matrixZoomSet, BlockPlanner.cpp:1305-1315)
+    const int scale = bs2 / 64;
+    const int levL2 = __builtin_popcount((unsigned)(scale - 1));
+    std::vector<int32_t> zoom(cz.storage, 0);
+    {
+        std::vector<Leaf> cin;
+        cz.collect(croot, 0, 0, cin);
+        for (auto& lf : cin) {
+            int32_t cur = froot;
+            int fl = fz.at(froot).level;
+            int bi = lf.bi * scale, bj = lf.bj * scale;
+            for (int step = fl; step > levL2 && cur != 0; step--) {
+                int q = (((bi >> (step - 1)) & 1) << 1) | ((bj >> (step - 1)) & 1);
+                cur = fz.at(cur).ch[q];
+            }
+            zoom[lf.id] = cur;
+        }
+    }
+    // expand every coarse op into fine ops (copyOperatorL2, BlockPlanner.cpp:1332-1460)
+    for (const Op& o : cz.ops) {
+        if (o.res > 0 && zoom[o.res] == 0) zoom[o.res] = fz.node(levL2);
+        if (o.res2 > 0 && zoom[o.res2] == 0) zoom[o.res2] = fz.node(levL2);
+        const int32_t g = o.seq;
+        switch (o.op) {
+            case OP_LOWERINV: fz.inv_lower(zoom[o.src], zoom[o.res], 0, g); break;
+            case OP_UPPERINV: fz.inv_upper(zoom[o.src], zoom[o.res], 0, g); break;
+            case OP_LU: fz.lu(zoom[o.src], zoom[o.res], zoom[o.res2], 0, 0, g); break;
+            case OP_MUL: fz.mul(zoom[o.src], zoom[o.src2], zoom[o.res], g, OP_MUL); break;
+            case OP_MULNEG: fz.mul(zoom[o.src], zoom[o.src2], zoom[o.res], g, OP_MULNEG); break;
+            case OP_SUB:
+                if (o.src > 0) {
+                    if (o.src2 > 0) fz.sub(zoom[o.src2], zoom[o.src], zoom[o.res], g);
+                    else fz.neg(zoom[o.src], zoom[o.res], g);
+                } else if (o.src2 > 0) {
+                    fz.copy(zoom[o.src2], zoom[o.res], g);
+                }
+                break;
+            default: throw std::runtime_error("unexpected coarse op");
+        }
+    }
+    p.fine_ops_emitted = (int64_t)fz.ops.size();
+    // fine L/U leaves: coarse output leaves zoomed to their fine subtrees (matrixZoomUpdate)
+    auto zoom_leaves = [&](const std::vector<Leaf>& cl_, std::vector<Leaf>& out) {
+        for (auto& lf : cl_) {
+            std::vector<Leaf> sub;
+            fz.collect(zoom[lf.id], 0, 0, sub);
+            for (auto& s : sub) out.push_back({lf.bi * scale + s.bi, lf.bj * scale + s.bj, s.id});
+        }
+        std::sort(out.begin(), out.end(), [](const Leaf& a, const Leaf& b) {
+            return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj;
+        });
+    };
+    zoom_leaves(cL, p.L);
+    zoom_leaves(cU, p.U);
+    {
+        std::vector<int32_t> outs;
+        for (auto& lf : p.L) outs.push_back(lf.id);
+        for (auto& lf : p.U) outs.push_back(lf.id);
+        schedule(fz.ops, fz.storage, finputs, outs, false);
+    }
+    p.ops = std::move(fz.ops);
+    p.storage_count = fz.storage;
+    p.stages = p.ops.empty() ? 0 : p.ops.back().stage;
+    p.t_plan = now_s() - t1;
+    return p;
+}
+
+void scatter_tiles(const Plan& p, const double* V, double* tiles) {
+    std::memset(tiles, 0, sizeof(double) * 4096 * (size_t)p.n_input);
+    for (size_t k = 0; k < p.scatter_tile.size(); k++)
+        if (p.scatter_tile[k] >= 0) tiles[(size_t)p.scatter_tile[k] * 4096 + p.scatter_off[k]] = V[k];
+    for (size_t k = 0; k < p.pad_tile.size(); k++) tiles[(size_t)p.pad_tile[k] * 4096 + p.pad_off[k]] = 1.0;
+}
+
+}  // namespace sog
