@@ -1,0 +1,180 @@
+/*
+ * soglu_gb300 — GB300 (sm_103a) executor for the factor-and-solve path of
+ * sparse-operator-graph-LU, behind a plain C ABI (no exceptions, no C++ or
+ * torch types; int status codes; opaque handles).
+ *
+ * The reference solver has no FFI; its executor boundary is internal:
+ *   planner  -> BlockPlanner::calculate()           (BlockPlanner.cpp:376)
+ *            -> BlockPlanner::solve(bl, bu, b, n)   (BlockPlanner.cpp:834)
+ * and its outer API is SOGLU::solveLU (solver.cpp:121, solver.h:24). Each
+ * entry point below names the reference interface it replaces.
+ *
+ * Threading: a context owns one CUDA stream on one device; calls on one
+ * context must come from one thread at a time. Systems are independent.
+ */
+#ifndef SOGLU_GB300_H
+#define SOGLU_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define SOG_OK 0
+#define SOG_EINVAL 1    /* malformed argument, matrix or DAG */
+#define SOG_ENOMEM 2    /* device block pool or device memory exhausted */
+#define SOG_EPIVOT 3    /* a diagonal-block pivot was clamped or grew past the limit */
+#define SOG_ENAN 4      /* NaN/Inf in the solution */
+#define SOG_ETIMEOUT 5  /* a bounded device-side wait expired; the context stays usable */
+#define SOG_ECUDA 6     /* CUDA runtime error (message in sog_last_error) */
+#define SOG_ENOCONV 7   /* iterative refinement did not reach the tolerance */
+#define SOG_ESTATE 8    /* call out of order (e.g. solve before factor) */
+#define SOG_ENODEV 9    /* no CUDA device, or the library was built without one */
+
+/* ---- precision and executor modes ---------------------------------------- */
+#define SOG_FP64 0      /* plain FP64 factor + solve (DMMA tile products) */
+#define SOG_MIXED 1     /* FP32 factors, 3xTF32 tile products, FP64 iterative refinement */
+
+#define SOG_EXEC_PERSISTENT 0 /* one persistent launch pulling ready tasks from a device queue */
+#define SOG_EXEC_LEVELS 1     /* one launch per dependency level (stage-synchronous, like calculate()) */
+
+/* One unit operation: the fields of the reference's struct operation
+ * (operation.h:37-48); op numbering follows enum blockOp (operation.h:20):
+ * 1 lu, 2 lowerInv, 3 upperInv, 4 sub, 8 mul, 9 mulneg. Block id 0 = none. */
+typedef struct {
+    int32_t op, src, src2, result, result2, stage;
+} sog_op;
+
+typedef struct sog_plan sog_plan;     /* host planner output: ordering + op DAG */
+typedef struct sog_ctx sog_ctx;       /* device, stream, block pool */
+typedef struct sog_system sog_system; /* one system's tiles/factors resident on the device */
+
+typedef struct {
+    int32_t n, n_ext, block_rows, block_rows_l2, block_size_l2;
+    int32_t storage_count; /* block ids are 1..storage_count-1 */
+    int32_t n_input;       /* input tiles carry ids 1..n_input */
+    int32_t stages;
+    int64_t nops, n_lleaf, n_uleaf, nnz;
+    int64_t op_count[13];  /* per enum blockOp */
+    int64_t coarse_ops, fine_ops_emitted;
+    double t_order, t_plan; /* seconds */
+} sog_plan_info;
+
+typedef struct {
+    int32_t precision;   /* SOG_FP64 or SOG_MIXED */
+    int32_t executor;    /* SOG_EXEC_PERSISTENT or SOG_EXEC_LEVELS */
+    int32_t max_refine;  /* iterative-refinement steps allowed (SOG_MIXED) */
+    double tol;          /* target ||b - A x||_2 / ||b||_2 (SOG_MIXED), e.g. 1e-10 */
+    int32_t gemm_split;  /* 0 = auto; FP64 tile products split into 1 or 4 output quadrants */
+    int32_t reserved[7];
+} sog_options;
+
+typedef struct {
+    int32_t status;          /* SOG_* of the solve */
+    int32_t iterations;      /* refinement steps taken */
+    double rel_resid;        /* ||b - A x||_2 / ||b||_2, worst right-hand side */
+    double backward_error;   /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), worst rhs */
+    int64_t nan_count;
+    double min_pivot;        /* smallest |u_ii| seen by the last factorisation */
+    int32_t clamped_pivots;  /* pivots raised to +-1e-9 (the reference's clamp) */
+    int32_t reserved[5];
+} sog_solve_stats;
+
+/* Last error message of the calling thread ("" if none). */
+const char *sog_last_error(void);
+/* Build identification, e.g. "soglu_gb300 sm_103a". */
+const char *sog_version(void);
+
+/* ---- host planner ----------------------------------------------------------
+ * Replaces the planning half of SOGLU::solveLU (solver.cpp:121-170) and
+ * SOGLU::decompose_solveLU (solver.cpp:50-110): GOrder::Reorder +
+ * GOrder::sortInBlock (GPSOrder.cpp:55-650), config::set (config.cpp:41),
+ * blockMatrixLU + copyOperatorL2 + blockPlan (BlockPlanner.cpp:103-374,
+ * 865-1577). I/J are 0-based; symmetric = lower triangle given (mtx.cpp:60,
+ * solver.cpp:132-149; the LL^T path is not built: symmetric returns SOG_EINVAL).
+ * threads = OpenMP threads for the ordering search (0 = default). */
+int sog_plan_build(int32_t n, int64_t nnz, int32_t symmetric, const int32_t *I, const int32_t *J,
+                   const double *V, int32_t threads, sog_plan **out);
+int sog_plan_get_info(const sog_plan *plan, sog_plan_info *info);
+/* Copy out the plan: new_to_old[n] (GOrder::newOrder), ops[nops] in the
+ * reference's stage order, lleaf/uleaf [n_*leaf][3] = {bi, bj, block id}. Any
+ * pointer may be NULL to skip that array. */
+int sog_plan_export(const sog_plan *plan, int32_t *new_to_old, sog_op *ops, int32_t *lleaf, int32_t *uleaf);
+/* Dense input tiles (n_input x 64 x 64, row-major) for values V in the
+ * triplet order given to sog_plan_build (BlockPlanner::iniBlockStorage,
+ * BlockPlanner.cpp:1491-1539, padded rows get a unit diagonal). */
+int sog_plan_input_tiles(const sog_plan *plan, const double *V, double *tiles);
+/* Import a DAG produced elsewhere (e.g. the reference planner's data::graph
+ * and L/U quadtree leaves) instead of building one; no ordering is attached
+ * (identity), input tiles then come through sog_factor_tiles. */
+int sog_plan_import(int32_t block_rows, int32_t storage_count, int32_t n_input, const sog_op *ops, int64_t nops,
+                    const int32_t *lleaf, int64_t n_lleaf, const int32_t *uleaf, int64_t n_uleaf, sog_plan **out);
+void sog_plan_destroy(sog_plan *plan);
+
+/* ---- device context ----------------------------------------------------------
+ * The device block-pool arena that replaces memutil's per-thread block pools
+ * (memutil.cpp:74-113). pool_bytes = 0: 90% of free device memory. */
+int sog_ctx_create(int32_t device, uint64_t pool_bytes, sog_ctx **out);
+void sog_ctx_destroy(sog_ctx *ctx);
+/* bytes of the pool in use / total */
+int sog_ctx_pool_usage(const sog_ctx *ctx, uint64_t *used, uint64_t *total);
+
+/* ---- one system --------------------------------------------------------------
+ * Upload the plan's DAG and allocate its tiles in the pool (admission: returns
+ * SOG_ENOMEM without side effects when the pool cannot hold them). */
+int sog_system_create(sog_ctx *ctx, const sog_plan *plan, const sog_options *opt, sog_system **out);
+/* bytes of pool this plan needs under opt (for admission decisions) */
+int sog_system_bytes(const sog_plan *plan, const sog_options *opt, uint64_t *bytes);
+/* BlockPlanner::calculate (BlockPlanner.cpp:376-651) on values V (host, the
+ * triplet order of sog_plan_build). Returns after the factors are resident. */
+int sog_factor(sog_system *sys, const double *V);
+/* Same with V already on the device (device pointer). */
+int sog_factor_device(sog_system *sys, const double *V_dev);
+/* BlockPlanner::calculate with input tiles given directly (host,
+ * n_input x 64 x 64 row-major FP64, block id k+1 at index k). */
+int sog_factor_tiles(sog_system *sys, const double *tiles);
+/* Solve with the resident factors. b and x are host arrays of nrhs right-hand
+ * sides, each of length n, in the ORIGINAL ordering (rhs-major: b[r*n + i]).
+ * Replaces BlockPlanner::solve + GOrder::reOrderResult (BlockPlanner.cpp:834,
+ * GPSOrder.cpp:41). SOG_MIXED refines in FP64 on the original matrix. */
+int sog_solve(sog_system *sys, int32_t nrhs, const double *b, double *x, sog_solve_stats *stats);
+/* Same with device pointers. */
+int sog_solve_device(sog_system *sys, int32_t nrhs, const double *b_dev, double *x_dev, sog_solve_stats *stats);
+/* BlockPlanner::solve exactly: b_ext / x_ext are host arrays of length n_ext
+ * in the planner's (permuted, padded) ordering; one right-hand side; no
+ * refinement. */
+int sog_solve_permuted(sog_system *sys, const double *b_ext, double *x_ext);
+/* Copy resident L/U leaf tiles (in plan leaf order) to host, FP64. */
+int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
+/* Device time of the last factor / solve in milliseconds (CUDA events on the
+ * context's stream). */
+int sog_system_last_times(const sog_system *sys, double *factor_ms, double *solve_ms);
+void sog_system_destroy(sog_system *sys);
+/* Task-graph summary: counts[10] = {tasks, dependency levels, queue items,
+ * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid}. */
+int sog_system_task_info(const sog_system *sys, int64_t *counts);
+
+/* ---- failure handling (no reference counterpart: the reference has no
+ * device waits) ------------------------------------------------------------
+ * Bound, in milliseconds, on any single device-side wait (ready-queue slot in
+ * the factor, row readiness in the solve; default 10 s). A wait that runs out
+ * sets a status bit, the kernel returns, the call returns SOG_ETIMEOUT and the
+ * context stays usable. */
+int sog_system_set_wait_limit(sog_system *sys, double ms);
+/* Testing hook: raise one task's dependency count so it never becomes ready
+ * (host-side fault injection); sog_debug_unpoison restores the graph. */
+int sog_debug_poison_task(sog_system *sys, int32_t task);
+int sog_debug_unpoison(sog_system *sys);
+
+/* ---- outer drop-in --------------------------------------------------------------
+ * SOGLU::solveLU (solver.cpp:121-184): plan, factor and solve one system on
+ * device 0; x_out receives n values in the original ordering. */
+int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_t *index_i, const int32_t *index_j,
+                  const double *vals, const double *b, double *x_out, int32_t precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOGLU_GB300_H */

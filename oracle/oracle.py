@@ -1,0 +1,78 @@
+"""ORACLE — test infrastructure, not the product.
+
+ctypes wrapper around oracle/soglu_oracle.c, the plain-C restatement of the
+reference's executor path (BlockPlanner::calculate, BlockPlanner.cpp:376-651,
+and BlockPlanner::solve, BlockPlanner.cpp:652-862). Only tests/, the smoke
+check and bench.py's CPU-baseline leg use it, as the checker or as the timed
+CPU baseline. Pinned against the compiled reference through tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "soglu_oracle.c")
+SO = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build() -> str:
+    """Compile liboracle.so (portable flags; OpenMP)."""
+    if not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(SRC):
+        subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", SRC, "-o", SO, "-lm"], check=True)
+    return SO
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(SO)
+        P = C.c_void_p
+        L.oracle_calculate.argtypes = [C.c_int64, P, C.c_int32, P, C.c_int]
+        L.oracle_calculate.restype = C.c_int
+        L.oracle_solve.argtypes = [C.c_int32, C.c_int64, P, C.c_int64, P, P, P, P]
+        L.oracle_solve.restype = C.c_int64
+        _lib = L
+    return _lib
+
+
+def calculate(ops: np.ndarray, storage_count: int, input_tiles: np.ndarray, threads: int = 0) -> np.ndarray:
+    """Run the op DAG; returns all tiles (storage_count x 64 x 64), block id = index."""
+    ops = np.ascontiguousarray(ops, dtype=np.int32).reshape(-1, 6)
+    tiles = np.zeros((storage_count, 64, 64), np.float64)
+    n_in = input_tiles.shape[0]
+    tiles[1:1 + n_in] = input_tiles
+    rc = lib().oracle_calculate(ops.shape[0], ops.ctypes.data, storage_count, tiles.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle_calculate failed ({rc})")
+    return tiles
+
+
+def solve(block_rows: int, L: np.ndarray, U: np.ndarray, tiles: np.ndarray, b_ext: np.ndarray):
+    """Block forward/back substitution; returns (x_ext, nan_count)."""
+    L = np.ascontiguousarray(L, dtype=np.int32)
+    U = np.ascontiguousarray(U, dtype=np.int32)
+    b = np.array(b_ext, dtype=np.float64, copy=True)
+    x = np.zeros(block_rows * 64, np.float64)
+    nan = lib().oracle_solve(block_rows, L.shape[0], L.ctypes.data, U.shape[0], U.ctypes.data, tiles.ctypes.data,
+                             b.ctypes.data, x.ctypes.data)
+    return x, int(nan)
+
+
+def solve_system(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, storage_count, input_tiles, L, U,
+                 b: np.ndarray, threads: int = 0):
+    """Full executor path in the original ordering: permute b (padded rows = 1,
+    solver.cpp:159-161), calculate, substitute, un-permute (GPSOrder.cpp:41-53)."""
+    tiles = calculate(ops, storage_count, input_tiles, threads)
+    b_ext = np.ones(block_rows * 64)
+    b_ext[:n] = np.asarray(b)[perm_new_to_old]
+    x_ext, nan = solve(block_rows, L, U, tiles, b_ext)
+    x = np.empty(n)
+    x[perm_new_to_old] = x_ext[:n]
+    return x, tiles, nan

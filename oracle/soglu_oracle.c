@@ -1,0 +1,285 @@
+/*
+ * ORACLE — test infrastructure, not the product. Only tests/, the smoke check
+ * in __graft_entry__.py and the CPU-baseline leg of bench.py load this code,
+ * as the checker or as the timed CPU baseline; the GPU executor never calls it.
+ *
+ * A plain-C restatement of the reference's executor path for one system:
+ *   oracle_calculate : BlockPlanner::calculate (BlockPlanner.cpp:376-651) with
+ *                      the unit ops of MatrixStdDouble.cpp
+ *   oracle_solve     : BlockPlanner::solve (BlockPlanner.cpp:652-862)
+ * on dense 64x64 row-major FP64 tiles indexed by block id. Like the reference
+ * it runs each stage's ops in parallel (OpenMP), serialising ops that write
+ * the same block, and skips all-zero 8x8 sub-tiles in the block products
+ * (the mask skipping of MatrixStdDouble.cpp:2043-2507).
+ *
+ * Pinning: tests compare this restatement with the compiled reference
+ * (oracle/_ref/ref_solve, built from the reference sources by
+ * oracle/build_ref.sh) through golden fixtures under tests/golden/.
+ */
+#include <math.h>
+#include <omp.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define B 64
+#define TILE (B * B)
+
+enum { OP_INV = 0, OP_LU = 1, OP_LOWERINV = 2, OP_UPPERINV = 3, OP_SUB = 4, OP_MUL = 8, OP_MULNEG = 9 };
+
+/* 8x8 occupancy: bit kb of m[ib] set when sub-tile (ib, kb) has a nonzero. */
+static void occupancy(const double *t, uint8_t m[8]) {
+    for (int ib = 0; ib < 8; ib++) {
+        uint8_t bits = 0;
+        for (int r = 0; r < 8; r++) {
+            const double *row = t + (ib * 8 + r) * B;
+            for (int kb = 0; kb < 8; kb++) {
+                if (bits & (1u << kb)) continue;
+                for (int c = 0; c < 8; c++)
+                    if (row[kb * 8 + c] != 0.0) { bits |= (uint8_t)(1u << kb); break; }
+            }
+        }
+        m[ib] = bits;
+    }
+}
+
+/* C += sign * A * B over nonzero 8x8 sub-tiles (MatrixStdDouble.cpp:2043 mul, :237 mulneg). */
+static void tile_gemm(double *restrict c, const double *restrict a, const double *restrict b, double sign) {
+    uint8_t ma[8], mb[8];
+    occupancy(a, ma);
+    occupancy(b, mb);
+    for (int ib = 0; ib < 8; ib++) {
+        for (int kb = 0; kb < 8; kb++) {
+            if (!(ma[ib] & (1u << kb))) continue;
+            for (int jb = 0; jb < 8; jb++) {
+                if (!(mb[kb] & (1u << jb))) continue;
+                for (int i = ib * 8; i < ib * 8 + 8; i++) {
+                    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int k = kb * 8; k < kb * 8 + 8; k++) {
+                        double av = a[i * B + k];
+                        const double *brow = b + k * B + jb * 8;
+                        for (int j = 0; j < 8; j++) acc[j] += av * brow[j];
+                    }
+                    double *crow = c + i * B + jb * 8;
+                    for (int j = 0; j < 8; j++) crow[j] += sign * acc[j];
+                }
+            }
+        }
+    }
+}
+
+/* Unpivoted Doolittle LU, unit-diagonal L, pivots |u_ii| < 1e-9 clamped to
+ * +-1e-9 (ludcmpSimple, MatrixStdDouble.cpp:2711-2784). */
+static void tile_lu(const double *a, double *l, double *u) {
+    memset(l, 0, sizeof(double) * TILE);
+    memset(u, 0, sizeof(double) * TILE);
+    for (int i = 0; i < B; i++) {
+        for (int j = i; j < B; j++) {
+            double s = 0;
+            for (int k = 0; k < i; k++) s += l[i * B + k] * u[k * B + j];
+            u[i * B + j] = a[i * B + j] - s;
+        }
+        double p = u[i * B + i];
+        if (p < 1e-9 && p > -1e-9) p = (p < 0) ? -1e-9 : 1e-9;
+        u[i * B + i] = p;
+        double r = 1.0 / p;
+        for (int j = i + 1; j < B; j++) {
+            double s = 0;
+            for (int k = 0; k < i; k++) s += l[j * B + k] * u[k * B + i];
+            l[j * B + i] = r * (a[j * B + i] - s);
+        }
+        l[i * B + i] = 1.0;
+    }
+}
+
+/* Y = L^-1, lower triangle of l incl. its diagonal (inv_lower, MatrixStdDouble.cpp:2787-2802). */
+static void tile_inv_lower(const double *l, double *y) {
+    memset(y, 0, sizeof(double) * TILE);
+    for (int i = 0; i < B; i++) {
+        double q = 1.0 / l[i * B + i];
+        y[i * B + i] = q;
+        for (int j = 0; j < i; j++) {
+            double s = 0;
+            for (int k = j; k < i; k++) s += l[i * B + k] * y[k * B + j];
+            y[i * B + j] = -s * q;
+        }
+    }
+}
+
+/* Y = U^-1 by Gauss-Jordan from the bottom row (inv_upper, MatrixStdDouble.cpp:2829-2866). */
+static void tile_inv_upper(const double *u, double *y) {
+    memset(y, 0, sizeof(double) * TILE);
+    for (int i = 0; i < B; i++) y[i * B + i] = 1.0;
+    for (int j = B - 1; j >= 0; j--) {
+        for (int i = j - 1; i >= 0; i--) {
+            double scale = u[i * B + j] / u[j * B + j];
+            for (int k = j; k < B; k++) y[i * B + k] -= scale * y[j * B + k];
+        }
+        double rate = 1.0 / u[j * B + j];
+        for (int k = j; k < B; k++) y[j * B + k] *= rate;
+    }
+}
+
+typedef struct {
+    int32_t op, src, src2, res, res2, stage;
+} op6;
+
+static int cmp_i64(const void *x, const void *y) {
+    int64_t a = *(const int64_t *)x, b = *(const int64_t *)y;
+    return (a > b) - (a < b);
+}
+
+/*
+ * Execute a stage-sorted op list. tiles[id*4096 ...] holds block `id`; input
+ * tiles are filled by the caller, every other tile must be zero on entry.
+ * Returns 0, or -1 on a malformed DAG.
+ */
+int oracle_calculate(int64_t nops, const int32_t *ops_flat, int32_t storage_count, double *tiles, int threads) {
+    const op6 *ops = (const op6 *)ops_flat;
+    if (threads > 0) omp_set_num_threads(threads);
+    for (int64_t i = 0; i < nops; i++) {
+        const op6 *o = &ops[i];
+        if (o->res < 0 || o->res >= storage_count || o->src < 0 || o->src >= storage_count || o->src2 < 0 ||
+            o->src2 >= storage_count || o->res2 < 0 || o->res2 >= storage_count)
+            return -1;
+        if (i > 0 && ops[i - 1].stage > o->stage) return -1;
+    }
+    /* group ops of a stage by result so that same-result writers run in one
+     * thread, in graph order (the reference's streams, BlockPlanner.cpp:402-416) */
+    int64_t *perm = (int64_t *)malloc(sizeof(int64_t) * (nops + 1));
+    int64_t *heads = (int64_t *)malloc(sizeof(int64_t) * (nops + 1));
+    if (!perm || !heads) { free(perm); free(heads); return -2; }
+    int64_t s0 = 0;
+    while (s0 < nops) {
+        int64_t s1 = s0;
+        while (s1 < nops && ops[s1].stage == ops[s0].stage) s1++;
+        /* gather same-result ops, keeping graph order among them: sort keys
+         * (result << 32 | position) */
+        int64_t n = s1 - s0;
+        for (int64_t k = 0; k < n; k++) perm[k] = ((int64_t)ops[s0 + k].res << 32) | k;
+        qsort(perm, (size_t)n, sizeof(int64_t), cmp_i64);
+        for (int64_t k = 0; k < n; k++) perm[k] = s0 + (perm[k] & 0xffffffffLL);
+        int64_t nh = 0;
+        for (int64_t k = 0; k < n; k++)
+            if (k == 0 || ops[perm[k]].res != ops[perm[k - 1]].res) heads[nh++] = k;
+        heads[nh] = n;
+#pragma omp parallel for schedule(dynamic)
+        for (int64_t h = 0; h < nh; h++) {
+            for (int64_t k = heads[h]; k < heads[h + 1]; k++) {
+                const op6 *o = &ops[perm[k]];
+                double *r = tiles + (int64_t)o->res * TILE;
+                const double *a = tiles + (int64_t)o->src * TILE;
+                const double *b2 = tiles + (int64_t)o->src2 * TILE;
+                switch (o->op) {
+                    case OP_LU: tile_lu(a, r, tiles + (int64_t)o->res2 * TILE); break;
+                    case OP_LOWERINV: tile_inv_lower(a, r); break;
+                    case OP_UPPERINV: tile_inv_upper(a, r); break;
+                    case OP_MUL: tile_gemm(r, a, b2, 1.0); break;
+                    case OP_MULNEG: tile_gemm(r, a, b2, -1.0); break;
+                    case OP_SUB: /* r = src2 - src; copy / negate when one is absent (BlockPlanner.cpp:553-572) */
+                        for (int e = 0; e < TILE; e++) {
+                            double v = 0;
+                            if (o->src2 > 0) v = b2[e];
+                            if (o->src > 0) v -= a[e];
+                            r[e] = v;
+                        }
+                        break;
+                    default: break;
+                }
+            }
+        }
+        s0 = s1;
+    }
+    free(perm);
+    free(heads);
+    return 0;
+}
+
+/*
+ * Block forward (unit-L) and back (U) substitution over the L/U leaves
+ * (lowerSolver / upperSolver / updateVector, BlockPlanner.cpp:669-832).
+ * leaves: {bi, bj, id} triples. b (length block_rows*64) is overwritten with
+ * the forward-eliminated right-hand side, as the reference does; x receives
+ * the solution (length block_rows*64). Returns the number of NaNs in x.
+ */
+int64_t oracle_solve(int32_t block_rows, int64_t nl, const int32_t *lleaf, int64_t nu, const int32_t *uleaf,
+                     const double *tiles, double *b, double *x) {
+    const int R = block_rows;
+    int64_t n = (int64_t)R * B;
+    double *y = (double *)calloc((size_t)n, sizeof(double));
+    int64_t *lp = (int64_t *)calloc((size_t)R + 1, sizeof(int64_t));
+    int64_t *up = (int64_t *)calloc((size_t)R + 1, sizeof(int64_t));
+    int32_t *ld = (int32_t *)calloc((size_t)R, sizeof(int32_t));
+    int32_t *ud = (int32_t *)calloc((size_t)R, sizeof(int32_t));
+    int64_t *li = (int64_t *)malloc(sizeof(int64_t) * (nl + 1));
+    int64_t *ui = (int64_t *)malloc(sizeof(int64_t) * (nu + 1));
+    for (int64_t k = 0; k < nl; k++) if (lleaf[3 * k] != lleaf[3 * k + 1]) lp[lleaf[3 * k] + 1]++;
+    for (int64_t k = 0; k < nu; k++) if (uleaf[3 * k] != uleaf[3 * k + 1]) up[uleaf[3 * k] + 1]++;
+    for (int i = 0; i < R; i++) { lp[i + 1] += lp[i]; up[i + 1] += up[i]; }
+    int64_t *lf = (int64_t *)malloc(sizeof(int64_t) * (R + 1));
+    int64_t *uf = (int64_t *)malloc(sizeof(int64_t) * (R + 1));
+    memcpy(lf, lp, sizeof(int64_t) * (R + 1));
+    memcpy(uf, up, sizeof(int64_t) * (R + 1));
+    for (int64_t k = 0; k < nl; k++) {
+        if (lleaf[3 * k] == lleaf[3 * k + 1]) ld[lleaf[3 * k]] = lleaf[3 * k + 2];
+        else li[lf[lleaf[3 * k]]++] = k;
+    }
+    for (int64_t k = 0; k < nu; k++) {
+        if (uleaf[3 * k] == uleaf[3 * k + 1]) ud[uleaf[3 * k]] = uleaf[3 * k + 2];
+        else ui[uf[uleaf[3 * k]]++] = k;
+    }
+    /* forward: y_i = L_ii^-1 (b_i - sum_j L_ij y_j) */
+    for (int i = 0; i < R; i++) {
+        double *bi = b + (int64_t)i * B;
+        for (int64_t q = lp[i]; q < lp[i + 1]; q++) {
+            int64_t k = li[q];
+            const double *t = tiles + (int64_t)lleaf[3 * k + 2] * TILE;
+            const double *yj = y + (int64_t)lleaf[3 * k + 1] * B;
+            for (int r = 0; r < B; r++) {
+                double s = 0;
+                for (int c = 0; c < B; c++) s += t[r * B + c] * yj[c];
+                bi[r] -= s;
+            }
+        }
+        double *yi = y + (int64_t)i * B;
+        if (ld[i] > 0) {
+            const double *t = tiles + (int64_t)ld[i] * TILE;
+            for (int r = 0; r < B; r++) {
+                double s = 0;
+                for (int c = 0; c < r; c++) s += t[r * B + c] * yi[c];
+                bi[r] -= s;
+                yi[r] = bi[r] / t[r * B + r];
+            }
+        }
+    }
+    /* backward: x_i = U_ii^-1 (y_i - sum_j U_ij x_j) */
+    for (int i = R - 1; i >= 0; i--) {
+        double *yi = y + (int64_t)i * B;
+        for (int64_t q = up[i]; q < up[i + 1]; q++) {
+            int64_t k = ui[q];
+            const double *t = tiles + (int64_t)uleaf[3 * k + 2] * TILE;
+            const double *xj = x + (int64_t)uleaf[3 * k + 1] * B;
+            for (int r = 0; r < B; r++) {
+                double s = 0;
+                for (int c = 0; c < B; c++) s += t[r * B + c] * xj[c];
+                yi[r] -= s;
+            }
+        }
+        double *xi = x + (int64_t)i * B;
+        if (ud[i] > 0) {
+            const double *t = tiles + (int64_t)ud[i] * TILE;
+            for (int r = B - 1; r >= 0; r--) {
+                double s = 0;
+                for (int c = r + 1; c < B; c++) s += t[r * B + c] * xi[c];
+                yi[r] -= s;
+                xi[r] = yi[r] / t[r * B + r];
+            }
+        } else {
+            for (int r = 0; r < B; r++) xi[r] = 0;
+        }
+    }
+    int64_t nans = 0;
+    for (int64_t k = 0; k < n; k++) if (isnan(x[k])) nans++;
+    free(y); free(lp); free(up); free(ld); free(ud); free(li); free(ui); free(lf); free(uf);
+    return nans;
+}

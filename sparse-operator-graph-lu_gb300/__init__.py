@@ -1,0 +1,295 @@
+"""soglu_gb300: GB300 (sm_103a) executor for sparse-operator-graph-LU's
+factor-and-solve path, driven through the C ABI of include/soglu_gb300.h.
+
+The reference's public entry point is SOGLU::solveLU (solver.cpp:121); its
+executor boundary is BlockPlanner::calculate / BlockPlanner::solve
+(BlockPlanner.cpp:376, :834). This module mirrors them:
+
+    solveLU(dim, rows, cols, vals, b)        -> x          (solver.cpp:121)
+    Plan(n, rows, cols, vals)                 host planner (GPSOrder + BlockPlanner)
+    System(Context(), plan).factor(vals)      BlockPlanner::calculate on the GPU
+    System.solve(b)                           BlockPlanner::solve + reOrderResult
+
+There is no CPU fallback: without the built library or a CUDA device every
+call raises SOGError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libsoglu_gb300.so")
+
+SOG_OK, SOG_EINVAL, SOG_ENOMEM, SOG_EPIVOT, SOG_ENAN, SOG_ETIMEOUT, SOG_ECUDA, SOG_ENOCONV, SOG_ESTATE, SOG_ENODEV = range(10)
+FP64, MIXED = 0, 1
+EXEC_PERSISTENT, EXEC_LEVELS = 0, 1
+OP_NAMES = ["inv", "lu", "lowerInv", "upperInv", "sub", "add", "neg", "copy", "mul", "mulneg", "llt", "mult", "noop"]
+_CODES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "EPIVOT", 4: "ENAN", 5: "ETIMEOUT", 6: "ECUDA", 7: "ENOCONV",
+          8: "ESTATE", 9: "ENODEV"}
+
+
+class SOGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_CODES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("n", C.c_int32), ("n_ext", C.c_int32), ("block_rows", C.c_int32), ("block_rows_l2", C.c_int32),
+                ("block_size_l2", C.c_int32), ("storage_count", C.c_int32), ("n_input", C.c_int32),
+                ("stages", C.c_int32), ("nops", C.c_int64), ("n_lleaf", C.c_int64), ("n_uleaf", C.c_int64),
+                ("nnz", C.c_int64), ("op_count", C.c_int64 * 13), ("coarse_ops", C.c_int64),
+                ("fine_ops_emitted", C.c_int64), ("t_order", C.c_double), ("t_plan", C.c_double)]
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
+                ("gemm_split", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_resid", C.c_double),
+                ("backward_error", C.c_double), ("nan_count", C.c_int64), ("min_pivot", C.c_double),
+                ("clamped_pivots", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+# every symbol declared in include/soglu_gb300.h
+EXPORTS = [
+    "sog_last_error", "sog_version", "sog_plan_build", "sog_plan_get_info", "sog_plan_export", "sog_plan_input_tiles",
+    "sog_plan_import", "sog_plan_destroy", "sog_ctx_create", "sog_ctx_destroy", "sog_ctx_pool_usage",
+    "sog_system_create", "sog_system_bytes", "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve",
+    "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
+    "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
+    "sog_debug_unpoison", "soglu_solveLU",
+]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree native library (built by build.py / __graft_entry__.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SOGError(SOG_ENODEV, f"native library not built: {LIB_PATH} (run build.py)")
+    L = C.CDLL(LIB_PATH)
+    P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "sog_last_error": ([], C.c_char_p), "sog_version": ([], C.c_char_p),
+        "sog_plan_build": ([I32, I64, I32, P, P, P, I32, P], I32),
+        "sog_plan_get_info": ([P, P], I32), "sog_plan_export": ([P, P, P, P, P], I32),
+        "sog_plan_input_tiles": ([P, P, P], I32),
+        "sog_plan_import": ([I32, I32, I32, P, I64, P, I64, P, I64, P], I32),
+        "sog_plan_destroy": ([P], None), "sog_ctx_create": ([I32, C.c_uint64, P], I32),
+        "sog_ctx_destroy": ([P], None), "sog_ctx_pool_usage": ([P, P, P], I32),
+        "sog_system_create": ([P, P, P, P], I32), "sog_system_bytes": ([P, P, P], I32),
+        "sog_factor": ([P, P], I32), "sog_factor_device": ([P, P], I32), "sog_factor_tiles": ([P, P], I32),
+        "sog_solve": ([P, I32, P, P, P], I32), "sog_solve_device": ([P, I32, P, P, P], I32),
+        "sog_solve_permuted": ([P, P, P], I32), "sog_system_export_factors": ([P, P, P], I32),
+        "sog_system_last_times": ([P, P, P], I32), "sog_system_destroy": ([P], None),
+        "sog_system_task_info": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
+        "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
+        "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(code: int) -> None:
+    if code != SOG_OK:
+        raise SOGError(code, lib().sog_last_error().decode())
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Plan:
+    """Host planner output for one sparsity pattern (GOrder + BlockPlanner)."""
+
+    def __init__(self, n: int, rows, cols, vals=None, symmetric: bool = False, threads: int = 0, _handle=None):
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+            self.nnz = 0
+        else:
+            self.rows = np.ascontiguousarray(rows, dtype=np.int32)
+            self.cols = np.ascontiguousarray(cols, dtype=np.int32)
+            v = None if vals is None else np.ascontiguousarray(vals, dtype=np.float64)
+            self.nnz = int(self.rows.size)
+            _check(lib().sog_plan_build(int(n), self.nnz, int(symmetric), _p(self.rows), _p(self.cols),
+                                        None if v is None else _p(v), int(threads), C.byref(self._h)))
+        self.info = PlanInfo()
+        _check(lib().sog_plan_get_info(self._h, C.byref(self.info)))
+
+    @classmethod
+    def imported(cls, block_rows: int, storage_count: int, n_input: int, ops: np.ndarray, lleaf: np.ndarray,
+                 uleaf: np.ndarray) -> "Plan":
+        """Wrap a DAG produced elsewhere (e.g. the reference planner's)."""
+        ops = np.ascontiguousarray(ops, dtype=np.int32).reshape(-1, 6)
+        lleaf = np.ascontiguousarray(lleaf, dtype=np.int32).reshape(-1, 3)
+        uleaf = np.ascontiguousarray(uleaf, dtype=np.int32).reshape(-1, 3)
+        h = C.c_void_p()
+        _check(lib().sog_plan_import(block_rows, storage_count, n_input, _p(ops), ops.shape[0], _p(lleaf),
+                                     lleaf.shape[0], _p(uleaf), uleaf.shape[0], C.byref(h)))
+        return cls(0, None, None, _handle=h)
+
+    def info_dict(self) -> dict:
+        d = {k: getattr(self.info, k) for k, _ in PlanInfo._fields_ if k != "op_count"}
+        d["ops"] = {OP_NAMES[i]: int(self.info.op_count[i]) for i in range(13) if self.info.op_count[i]}
+        return d
+
+    def export(self):
+        """(new_to_old[n], ops[nops, 6] = op,src,src2,result,result2,stage, L[k,3], U[k,3])."""
+        i = self.info
+        perm = np.empty(max(i.n, 1), np.int32)
+        ops = np.empty((max(i.nops, 1), 6), np.int32)
+        L = np.empty((max(i.n_lleaf, 1), 3), np.int32)
+        U = np.empty((max(i.n_uleaf, 1), 3), np.int32)
+        _check(lib().sog_plan_export(self._h, _p(perm), _p(ops), _p(L), _p(U)))
+        return perm[:i.n], ops[:i.nops], L[:i.n_lleaf], U[:i.n_uleaf]
+
+    def input_tiles(self, vals) -> np.ndarray:
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        t = np.empty((self.info.n_input, 64, 64), np.float64)
+        _check(lib().sog_plan_input_tiles(self._h, _p(v), _p(t)))
+        return t
+
+    def bytes_needed(self, precision: int = FP64) -> int:
+        o = Options(precision=precision)
+        out = C.c_uint64()
+        _check(lib().sog_system_bytes(self._h, C.byref(o), C.byref(out)))
+        return int(out.value)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.sog_plan_destroy(self._h)
+            self._h = None
+
+
+class Context:
+    """One GPU, one stream, the device block-pool arena."""
+
+    def __init__(self, device: int = 0, pool_bytes: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().sog_ctx_create(device, pool_bytes, C.byref(self._h)))
+
+    def pool_usage(self):
+        u, t = C.c_uint64(), C.c_uint64()
+        _check(lib().sog_ctx_pool_usage(self._h, C.byref(u), C.byref(t)))
+        return int(u.value), int(t.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sog_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+
+class System:
+    """One system resident in the device pool: factor once, solve many."""
+
+    def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
+                 max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0):
+        self.ctx, self.plan = ctx, plan
+        self.n = plan.info.n
+        self._h = C.c_void_p()
+        self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
+                           gemm_split=gemm_split)
+        _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
+
+    def factor(self, vals) -> None:
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        if v.shape != (self.plan.nnz,):
+            raise ValueError(f"values must have shape ({self.plan.nnz},)")
+        _check(lib().sog_factor(self._h, _p(v)))
+
+    def factor_device(self, vals_ptr: int) -> None:
+        _check(lib().sog_factor_device(self._h, C.c_void_p(vals_ptr)))
+
+    def factor_tiles(self, tiles) -> None:
+        t = np.ascontiguousarray(tiles, dtype=np.float64)
+        if t.shape != (self.plan.info.n_input, 64, 64):
+            raise ValueError(f"tiles must have shape ({self.plan.info.n_input}, 64, 64)")
+        _check(lib().sog_factor_tiles(self._h, _p(t)))
+
+    def solve(self, b, allow_noconv: bool = False):
+        """x (same shape as b: (n,) or (k, n)) and the solve statistics."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if b.ndim not in (1, 2) or b.shape[-1] != self.n:
+            raise ValueError(f"right-hand side must have shape (n,) or (k, n) with n = {self.n}")
+        k = 1 if b.ndim == 1 else b.shape[0]
+        x = np.empty_like(b)
+        st = SolveStats()
+        rc = lib().sog_solve(self._h, k, _p(b), _p(x), C.byref(st))
+        if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
+            _check(rc)
+        return x, st.as_dict()
+
+    def solve_device(self, nrhs: int, b_ptr: int, x_ptr: int) -> dict:
+        st = SolveStats()
+        _check(lib().sog_solve_device(self._h, nrhs, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(st)))
+        return st.as_dict()
+
+    def solve_permuted(self, b_ext) -> np.ndarray:
+        b = np.ascontiguousarray(b_ext, dtype=np.float64)
+        if b.shape != (self.plan.info.block_rows * 64,):
+            raise ValueError("b_ext must have the padded length block_rows * 64")
+        x = np.empty_like(b)
+        _check(lib().sog_solve_permuted(self._h, _p(b), _p(x)))
+        return x
+
+    def export_factors(self):
+        i = self.plan.info
+        L = np.empty((i.n_lleaf, 64, 64), np.float64)
+        U = np.empty((i.n_uleaf, 64, 64), np.float64)
+        _check(lib().sog_system_export_factors(self._h, _p(L), _p(U)))
+        return L, U
+
+    def last_times(self):
+        f, s = C.c_double(), C.c_double()
+        _check(lib().sog_system_last_times(self._h, C.byref(f), C.byref(s)))
+        return f.value, s.value
+
+    def task_info(self) -> dict:
+        c = np.zeros(10, np.int64)
+        _check(lib().sog_system_task_info(self._h, _p(c)))
+        keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "grid"]
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def set_wait_limit(self, ms: float) -> None:
+        _check(lib().sog_system_set_wait_limit(self._h, ms))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sog_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+
+def solveLU(dim: int, rows, cols, vals, b, symmetric: bool = False, precision: int = FP64) -> np.ndarray:
+    """Drop-in for SOGLU::solveLU (solver.cpp:121-184): x in the original ordering."""
+    r = np.ascontiguousarray(rows, dtype=np.int32)
+    c = np.ascontiguousarray(cols, dtype=np.int32)
+    v = np.ascontiguousarray(vals, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty(dim, np.float64)
+    _check(lib().soglu_solveLU(dim, r.size, int(symmetric), _p(r), _p(c), _p(v), _p(bb), _p(x), precision))
+    return x

@@ -1,0 +1,102 @@
+// Launch interface between the host runtime (runtime.cpp) and the sm_103a
+// kernels (factor.cu, solve.cu). Plain structs of device pointers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sog {
+
+// status word bits (DevStatus::flags)
+enum : int32_t {
+    ST_TIMEOUT = 1,      // a bounded wait expired
+    ST_BAD_ITEM = 2,     // queue delivered an out-of-range item
+    ST_SOLVE_TIMEOUT = 4,
+};
+
+struct DevStatus {
+    int32_t flags;
+    int32_t clamped;                       // pivots clamped to +-1e-9
+    unsigned long long min_pivot_bits;     // min |u_ii| as double bits (non-negative doubles order as integers)
+    unsigned long long max_growth_bits;    // max |u_ij| / max |a_ij| per diagonal block, double bits
+    int32_t timeout_where;                 // debugging aid: item index at timeout
+    int32_t pad;
+};
+
+struct DevTasks {
+    int32_t ntasks;
+    int64_t total_items;
+    const uint8_t* kind;
+    const uint8_t* parts;
+    const int32_t *out, *out2, *a, *b;
+    const int32_t *pair_ptr, *pair_a, *pair_b;
+    const int32_t *succ_ptr, *succ;
+    int32_t* dep;         // working dependency counters
+    int32_t* parts_left;  // working per-task part counters
+    int32_t* queue;       // ready items (task << 2 | part); -1 = not yet filled
+    int32_t* head;        // next slot to claim
+    int32_t* tail;        // next slot to fill
+    DevStatus* status;
+    unsigned long long wait_limit_ns;  // bound on any single queue wait
+};
+
+// ---- factor (factor.cu) ----
+// tiles: block id -> tiles + id*4096 elements. double => SOG_FP64, float => SOG_MIXED.
+int factor_persistent_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
+int factor_persistent_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
+int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, cudaStream_t s);
+int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, cudaStream_t s);
+// persistent grid size (CTAs co-resident on the device)
+int factor_persistent_grid(bool fp64, int num_sms);
+size_t factor_smem_bytes(bool fp64);
+
+// value scatter into input tiles: tiles[tile[k]*4096 + off[k]] = V[k] (tile < 0: skip)
+void scatter_values_launch(const double* V, const int32_t* tile, const int16_t* off, int64_t nnz,
+                           const int32_t* pad_tile, const int16_t* pad_off, int64_t npad, double* tiles64,
+                           float* tiles32, cudaStream_t s);
+// FP64 input tiles -> FP32 input tiles (first n elements)
+void convert_tiles_launch(const double* src, float* dst, int64_t n, cudaStream_t s);
+void widen_tiles_launch(const float* src, double* dst, int64_t n, cudaStream_t s);
+
+// ---- solve (solve.cu) ----
+struct DevSolve {
+    int32_t block_rows;
+    // block-row CSR of off-diagonal L (j < i) and U (j > i) leaves; L sorted by
+    // ascending j, U by descending j (the order their operands become ready)
+    const int32_t *l_ptr, *l_col, *l_id;
+    const int32_t *u_ptr, *u_col, *u_id;
+    const int32_t *l_diag, *u_diag;  // diagonal block id per block row
+    int32_t* flags;                  // per block row readiness epoch
+    DevStatus* status;
+    unsigned long long wait_limit_ns;
+};
+// In-place block substitution on vec (n_ext x nrhs, row-major), lower then
+// upper. epoch: a fresh even number per call (forward uses epoch, backward epoch+1).
+int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int epoch, int grid,
+                    cudaStream_t st);
+int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
+                    cudaStream_t st);
+int trisolve_grid(bool fp64, int nrhs, int num_sms);
+
+// CSR of the permuted, padded matrix for FP64 residuals
+struct DevCSR {
+    int32_t n;
+    const int32_t *ptr, *col;
+    const double* val;
+};
+// r = b - A x (all n x nrhs row-major). Per-rhs reductions over rows < n_stat:
+// red[c*6 + {0..5}] = {sum r^2, sum b^2, max|r|, max|x|, max|b|, max row abs sum of A}
+constexpr int RED = 6;
+void residual_launch(const DevCSR& A, const double* b, const double* x, double* r, int nrhs, double* red,
+                     int n_stat, cudaStream_t s);
+// csr_val[pos[k]] = V[k] for pos[k] >= 0
+void scatter_csr_launch(const double* V, const int32_t* pos, int64_t nnz, double* csr_val, cudaStream_t s);
+void cast_f64_to_f32_launch(const double* src, float* dst, int64_t n, cudaStream_t s);
+void axpy_f32_to_f64_launch(const float* d, double* x, int64_t n, int assign, cudaStream_t s);
+// original-order rhs-major (nrhs x n) <-> permuted padded row-major (n_ext x nrhs)
+void gather_rhs_launch(const double* b, const int32_t* new_to_old, int n, int n_ext, int nrhs, double* out,
+                       cudaStream_t s);
+void scatter_solution_launch(const double* xe, const int32_t* old_to_new, int n, int nrhs, double* x,
+                             cudaStream_t s);
+int count_nonfinite_launch(const double* x, int64_t n, unsigned long long* counter, cudaStream_t s);
+
+}  // namespace sog

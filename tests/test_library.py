@@ -1,0 +1,70 @@
+"""The C-ABI library loads and exports every entry point include/soglu_gb300.h
+declares; host-only entry points work without a GPU; device entry points fail
+loudly (no CPU fallback)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, gpu_available
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "soglu_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:sog|soglu)_[A-Za-z_0-9]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(sg):
+    L = ctypes.CDLL(sg.LIB_PATH)
+    syms = header_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(L, s), f"{s} declared but not exported"
+    assert sorted(sg.EXPORTS) == syms
+
+
+def test_version_and_error_string(sg):
+    assert b"sm_103a" in sg.lib().sog_version()
+    with pytest.raises(sg.SOGError):
+        sg.Plan(-1, np.zeros(0), np.zeros(0), np.zeros(0))
+    assert len(sg.lib().sog_last_error()) > 0
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-device path")
+def test_no_device_is_an_error_not_a_fallback(sg, wl):
+    with pytest.raises(sg.SOGError) as e:
+        sg.Context()
+    assert e.value.code in (sg.SOG_ENODEV, sg.SOG_ECUDA)
+    s = wl.lap2d(16)
+    with pytest.raises(sg.SOGError):
+        sg.solveLU(s.n, s.rows, s.cols, s.vals, s.b)
+
+
+def test_cli_plans_like_the_reference(sg, wl, tmp_path):
+    s = wl.lap2d(32)
+    wl.write_mtx(str(tmp_path / "a.mtx"), s)
+    wl.write_rhs(str(tmp_path / "a_b.mtx"), s.b)
+    exe = os.path.join(ROOT, "sparse-operator-graph-lu_gb300", "bin", "solve")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert "usage" in r.stdout
+    r = subprocess.run([exe, str(tmp_path / "a.mtx")], capture_output=True, text=True, timeout=120)
+    assert "op count: 173 storage: 386" in r.stdout
+    if not gpu_available():
+        assert r.returncode != 0  # no device: loud failure
+
+
+def test_mtx_reader_acceptance_rules(sg, tmp_path):
+    """Reader rules of mtx.cpp:44-117: '%' lines and lines of <= 3 chars are
+    skipped, zero values dropped, out-of-range rows dropped."""
+    p = tmp_path / "r.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real general\n% comment\n\n"
+                 "64 64 70\n" + "".join(f"{i} {i} 4\n" for i in range(1, 65)) +
+                 "1 2 0\n65 1 7\n1 2 -1\n2 1 -1\n")
+    exe = os.path.join(ROOT, "sparse-operator-graph-lu_gb300", "bin", "solve")
+    r = subprocess.run([exe, str(p)], capture_output=True, text=True, timeout=60)
+    # 66 accepted entries, n = 64 -> 2 block rows, one lu per block row
+    assert "inputSize: 64" in r.stdout and "op count: 2" in r.stdout

@@ -1,0 +1,56 @@
+"""Pin the oracle (oracle/soglu_oracle.c, a C restatement of the reference's
+executor path) against the compiled reference's own outputs stored in
+tests/golden/: solution vectors and L/U tiles."""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_cases, rhs_of
+
+
+@pytest.mark.parametrize("name", ["lap2d_8", "lap2d_32", "lap2d_128", "var3d_16", "cd_40", "cd_17", "band_3000",
+                                  "band_130"])
+def test_oracle_solution_matches_reference(sg, wl, oracle, name):
+    s = golden_cases(wl)[name]()
+    g = golden(name)
+    # run the oracle on the REFERENCE's own DAG and ordering
+    n_input = sg.Plan(s.n, s.rows, s.cols, s.vals).info.n_input
+    tiles_in = sg.Plan(s.n, s.rows, s.cols, s.vals).input_tiles(s.vals)
+    stats = dict(l.split("=") for l in str(g["stats"]).split())
+    R = int(stats["block_rows"])
+    x, tiles, nan = oracle.solve_system(g["perm"], s.n, R, g["dag"], int(stats["storage_count"]), tiles_in,
+                                        g["lleaf"], g["uleaf"], rhs_of(s))
+    assert nan == 0
+    rel = np.linalg.norm(x - g["x"]) / np.linalg.norm(g["x"])
+    assert rel <= 1e-12, rel
+    if "tiles" in g:
+        nl = len(g["lleaf"])
+        for k, (_, _, bid) in enumerate(g["lleaf"]):
+            np.testing.assert_allclose(tiles[bid], g["tiles"][k], rtol=0, atol=1e-12)
+        for k, (_, _, bid) in enumerate(g["uleaf"]):
+            np.testing.assert_allclose(tiles[bid], g["tiles"][nl + k], rtol=0, atol=1e-12)
+    assert n_input > 0
+
+
+def test_oracle_reference_accuracy(sg, wl, oracle):
+    """Known-answer check: b = A x_true."""
+    s = wl.varcoef3d(12)
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    x, _, _ = oracle.solve_system(perm, s.n, p.info.block_rows, ops, p.info.storage_count, p.input_tiles(s.vals),
+                                  L, U, s.b)
+    assert np.linalg.norm(x - s.x_true) / np.linalg.norm(s.x_true) < 1e-10
+
+
+def test_oracle_detects_planted_error(sg, wl, oracle):
+    """A mistake planted in the oracle's inputs (one DAG op dropped) is caught
+    by the same comparison the tests rely on."""
+    s = wl.lap2d(32)
+    g = golden("lap2d_32")
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    stats = dict(l.split("=") for l in str(g["stats"]).split())
+    dag = g["dag"].copy()
+    k = int(np.nonzero(dag[:, 0] == 8)[0][0])  # first mul
+    dag = np.delete(dag, k, axis=0)
+    x, _, _ = oracle.solve_system(g["perm"], s.n, int(stats["block_rows"]), dag, int(stats["storage_count"]),
+                                  p.input_tiles(s.vals), g["lleaf"], g["uleaf"], s.b)
+    assert np.linalg.norm(x - g["x"]) / np.linalg.norm(g["x"]) > 1e-6

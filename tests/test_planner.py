@@ -1,0 +1,113 @@
+"""Host planner vs the reference planner (golden fixtures from the compiled
+reference): permutation, op DAG and L/U leaves must be identical, op for op."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden, golden_cases, load_package
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def triplet_hash(s):
+    h = hashlib.sha256()
+    h.update(np.int64(s.n).tobytes())
+    h.update(s.rows.tobytes()); h.update(s.cols.tobytes()); h.update(s.vals.tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", ["lap2d_8", "lap2d_32", "lap2d_128", "var3d_16", "cd_40", "cd_17", "band_3000",
+                                  "band_130", "zdiag_600"])
+def test_plan_matches_reference(sg, wl, name):
+    s = golden_cases(wl)[name]()
+    g = golden(name)
+    assert triplet_hash(s) == str(g["ahash"]), "generator drifted from the fixture"
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    np.testing.assert_array_equal(perm, g["perm"])
+    assert ops.shape == g["dag"].shape
+    np.testing.assert_array_equal(ops, g["dag"])
+    key = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]
+    np.testing.assert_array_equal(key(L), key(g["lleaf"]))
+    np.testing.assert_array_equal(key(U), key(g["uleaf"]))
+    stats = dict(l.split("=") for l in str(g["stats"]).split())
+    assert p.info.storage_count == int(stats["storage_count"])
+    assert p.info.stages == int(stats["stages"])
+    assert p.info.coarse_ops == int(stats["coarse_ops"])
+    assert p.info.fine_ops_emitted == int(stats["fine_ops_emitted"])
+
+
+def test_plan_48cube_matches_reference_hashes(sg, wl):
+    """The bench configuration (3D var-coef 48^3, 1.08M ops): full-size DAG identity."""
+    s = wl.varcoef3d(48)
+    g = golden("var3d_48")
+    assert triplet_hash(s) == str(g["ahash"])
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    assert _sha(perm) == str(g["permhash"])
+    assert _sha(ops) == str(g["daghash"])
+    assert _sha(L) == str(g["lleafhash"]) and _sha(U) == str(g["uleafhash"])
+    info = p.info_dict()
+    assert info["nops"] == 1082718 and info["stages"] == 11904
+    assert info["ops"] == {"lu": 2048, "lowerInv": 3679, "upperInv": 3679, "sub": 72926, "mul": 839513,
+                           "mulneg": 160873}
+
+
+def test_config_rounding(sg, wl):
+    # block rows = next power of two strictly above n/64 (config.cpp:30-49)
+    for side, br in ((8, 2), (16, 8), (32, 32), (128, 512)):
+        s = wl.lap2d(side)
+        assert sg.Plan(s.n, s.rows, s.cols, s.vals).info.block_rows == br
+
+
+def test_input_tiles_scatter(sg, wl):
+    s = wl.lap2d(32)
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    t = p.input_tiles(s.vals)
+    # reassemble the permuted matrix from tiles and compare with P A P^T
+    A = np.zeros((s.n, s.n))
+    A[s.rows, s.cols] = s.vals
+    Ap = A[np.ix_(perm, perm)]
+    R = p.info.block_rows
+    full = np.zeros((R * 64, R * 64))
+    # input tile k carries block id k+1, allocated in (block row, block col)
+    # order of the permuted triplets (BlockPlanner.cpp:1491-1520)
+    o2n = np.argsort(perm)
+    keys = sorted({(i // 64, j // 64) for i, j in zip(o2n[s.rows], o2n[s.cols])})
+    for k, (bi, bj) in enumerate(keys):
+        full[bi * 64:(bi + 1) * 64, bj * 64:(bj + 1) * 64] = t[k]
+    np.testing.assert_array_equal(full[:s.n, :s.n], Ap)
+
+
+@pytest.mark.parametrize("bad", ["symmetric", "index", "zero_block"])
+def test_plan_rejects_bad_input(sg, wl, bad):
+    s = wl.lap2d(16)
+    rows, cols, vals = s.rows.copy(), s.cols.copy(), s.vals.copy()
+    sym = False
+    if bad == "symmetric":
+        sym = True
+    elif bad == "index":
+        rows[3] = s.n + 5
+    else:  # drop every entry of block row 0 -> structurally zero diagonal block
+        keep = (rows >= 64) & (cols >= 64)
+        rows, cols, vals = rows[keep], cols[keep], vals[keep]
+    with pytest.raises(sg.SOGError) as e:
+        sg.Plan(s.n, rows, cols, vals, symmetric=sym)
+    assert e.value.code == sg.SOG_EINVAL
+
+
+def test_disconnected_and_isolated_nodes(sg):
+    # two decoupled chains plus isolated diagonal-only rows: ordering covers all nodes
+    n = 300
+    r, c, v = [], [], []
+    for i in range(n):
+        r.append(i); c.append(i); v.append(4.0)
+        if i % 3 != 2 and i + 3 < n:
+            r += [i, i + 3]; c += [i + 3, i]; v += [-1.0, -1.0]
+    p = sg.Plan(n, np.array(r), np.array(c), np.array(v))
+    perm = p.export()[0]
+    assert sorted(perm.tolist()) == list(range(n))
