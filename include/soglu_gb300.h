@@ -120,6 +120,10 @@ int sog_ctx_create(int32_t device, uint64_t pool_bytes, sog_ctx **out);
 void sog_ctx_destroy(sog_ctx *ctx);
 /* bytes of the pool in use / total */
 int sog_ctx_pool_usage(const sog_ctx *ctx, uint64_t *used, uint64_t *total);
+/* The context's CUDA stream (a cudaStream_t) — every kernel of every system
+ * on this context is launched on it, so callers can order and time work
+ * against it with their own events. */
+int sog_ctx_stream(const sog_ctx *ctx, void **stream);
 
 /* ---- one system --------------------------------------------------------------
  * Upload the plan's DAG and allocate its tiles in the pool (admission: returns
@@ -152,8 +156,9 @@ int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
  * context's stream). */
 int sog_system_last_times(const sog_system *sys, double *factor_ms, double *solve_ms);
 void sog_system_destroy(sog_system *sys);
-/* Task-graph summary: counts[10] = {tasks, dependency levels, queue items,
- * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid}. */
+/* Task-graph summary: counts[11] = {tasks, dependency levels, queue items,
+ * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid,
+ * kernel launches issued by this system so far}. */
 int sog_system_task_info(const sog_system *sys, int64_t *counts);
 
 /* ---- failure handling (no reference counterpart: the reference has no

@@ -62,7 +62,7 @@ class SolveStats(C.Structure):
 # every symbol declared in include/soglu_gb300.h
 EXPORTS = [
     "sog_last_error", "sog_version", "sog_plan_build", "sog_plan_get_info", "sog_plan_export", "sog_plan_input_tiles",
-    "sog_plan_import", "sog_plan_destroy", "sog_ctx_create", "sog_ctx_destroy", "sog_ctx_pool_usage",
+    "sog_plan_import", "sog_plan_destroy", "sog_ctx_create", "sog_ctx_destroy", "sog_ctx_pool_usage", "sog_ctx_stream",
     "sog_system_create", "sog_system_bytes", "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve",
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
     "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
@@ -88,7 +88,7 @@ def lib() -> C.CDLL:
         "sog_plan_input_tiles": ([P, P, P], I32),
         "sog_plan_import": ([I32, I32, I32, P, I64, P, I64, P, I64, P], I32),
         "sog_plan_destroy": ([P], None), "sog_ctx_create": ([I32, C.c_uint64, P], I32),
-        "sog_ctx_destroy": ([P], None), "sog_ctx_pool_usage": ([P, P, P], I32),
+        "sog_ctx_destroy": ([P], None), "sog_ctx_pool_usage": ([P, P, P], I32), "sog_ctx_stream": ([P, P], I32),
         "sog_system_create": ([P, P, P, P], I32), "sog_system_bytes": ([P, P, P], I32),
         "sog_factor": ([P, P], I32), "sog_factor_device": ([P, P], I32), "sog_factor_tiles": ([P, P], I32),
         "sog_solve": ([P, I32, P, P, P], I32), "sog_solve_device": ([P, I32, P, P, P], I32),
@@ -185,6 +185,12 @@ class Context:
         self._h = C.c_void_p()
         _check(lib().sog_ctx_create(device, pool_bytes, C.byref(self._h)))
 
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer (every kernel runs on it)."""
+        s = C.c_void_p()
+        _check(lib().sog_ctx_stream(self._h, C.byref(s)))
+        return int(s.value or 0)
+
     def pool_usage(self):
         u, t = C.c_uint64(), C.c_uint64()
         _check(lib().sog_ctx_pool_usage(self._h, C.byref(u), C.byref(t)))
@@ -266,9 +272,9 @@ class System:
         return f.value, s.value
 
     def task_info(self) -> dict:
-        c = np.zeros(10, np.int64)
+        c = np.zeros(11, np.int64)
         _check(lib().sog_system_task_info(self._h, _p(c)))
-        keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "grid"]
+        keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "grid", "launches"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def set_wait_limit(self, ms: float) -> None:

@@ -158,6 +158,7 @@ struct sog_system {
     bool factored = false;
     float t_factor = 0, t_solve = 0;
     int grid_factor = 0;
+    int64_t launches = 0;  // kernels launched by this system
     DevStatus last{};
     std::vector<Leaf> L, U;
 };
@@ -299,10 +300,12 @@ int run_factor(sog_system* s) {
             const int a = g.level_ptr[l], b = g.level_ptr[l + 1];
             rc = s->fp64 ? factor_level_launch(s->dt, (double*)s->tiles, s->d_level_items + a, b - a, st)
                          : factor_level_launch(s->dt, (float*)s->tiles, s->d_level_items + a, b - a, st);
+            s->launches++;
         }
     } else {
         rc = s->fp64 ? factor_persistent_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
                      : factor_persistent_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
+        s->launches++;
     }
     if (rc) return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->e1, st));
@@ -320,6 +323,7 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
     int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, c->stream)
                      : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, c->stream);
     s->epoch += 2;
+    s->launches += 2;
     if (rc) return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     return SOG_OK;
 }
@@ -355,20 +359,26 @@ int solve_chunk(sog_system* s, int nc, sog_solve_stats* stats) {
         CK(cudaMemcpyAsync(s->d_xext, s->d_bext, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st));
         if ((r = trisolve(s, s->d_xext, nc))) return r;
         if (s->csr.ptr) {
+            s->launches++;
             residual_launch(s->csr, s->d_bext, s->d_xext, s->d_r, nc, s->d_red, s->n, st);
             if ((r = read_norms(s, nc, nm))) return r;
         }
     } else {
+        s->launches++;
         cast_f64_to_f32_launch(s->d_bext, s->d_v32, ne, st);
         if ((r = trisolve(s, s->d_v32, nc))) return r;
+        s->launches++;
         axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 1, st);
         if (s->csr.ptr) {
             for (;;) {
+                s->launches++;
                 residual_launch(s->csr, s->d_bext, s->d_xext, s->d_r, nc, s->d_red, s->n, st);
                 if ((r = read_norms(s, nc, nm))) return r;
                 if (nm.rel <= s->opt.tol || iters >= s->opt.max_refine || std::isnan(nm.rel)) break;
+                s->launches++;
                 cast_f64_to_f32_launch(s->d_r, s->d_v32, ne, st);
                 if ((r = trisolve(s, s->d_v32, nc))) return r;
+                s->launches++;
                 axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 0, st);
                 iters++;
             }
@@ -398,13 +408,16 @@ int solve_device_impl(sog_system* s, int nrhs, const double* b_dev, double* x_de
     int worst = SOG_OK;
     for (int c0 = 0; c0 < nrhs; c0 += 64) {
         const int nc = std::min(64, nrhs - c0);
+        s->launches++;
         gather_rhs_launch(b_dev + (size_t)c0 * s->n, s->d_n2o, s->n, s->n_ext, nc, s->d_bext, st);
         r = solve_chunk(s, nc, stats);
         if (r && r != SOG_ENOCONV) return r;
         if (r) worst = r;
+        s->launches++;
         scatter_solution_launch(s->d_xext, s->d_o2n, s->n, nc, x_dev + (size_t)c0 * s->n, st);
     }
     CK(cudaEventRecord(c->e1, st));
+    s->launches++;
     count_nonfinite_launch(x_dev, (int64_t)s->n * nrhs, s->d_cnt, st);
     unsigned long long bad = 0;
     CK(cudaMemcpyAsync(&bad, s->d_cnt, sizeof(bad), cudaMemcpyDeviceToHost, st));
@@ -459,6 +472,12 @@ void sog_ctx_destroy(sog_ctx* c) {
     if (c->e1) cudaEventDestroy(c->e1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+int sog_ctx_stream(const sog_ctx* c, void** stream) {
+    if (!c || !stream) return fail(SOG_EINVAL, "NULL argument");
+    *stream = (void*)c->stream;
+    return SOG_OK;
 }
 
 int sog_ctx_pool_usage(const sog_ctx* c, uint64_t* used, uint64_t* total) {
@@ -664,9 +683,11 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
     const uint64_t eb = elem_bytes(s->opt);
     CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
     // input tile k (0-based, as the scatter map counts) is block id k+1
+    s->launches++;
     scatter_values_launch(V_dev, s->d_sc_tile, s->d_sc_off, s->ntrip, s->d_pad_tile, s->d_pad_off, s->npad,
                           s->fp64 ? (double*)s->tiles + 4096 : nullptr, s->fp64 ? nullptr : (float*)s->tiles + 4096,
                           st);
+    s->launches++;
     scatter_csr_launch(V_dev, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
     return run_factor(s);
 }
@@ -692,6 +713,7 @@ int sog_factor_tiles(sog_system* s, const double* tiles) {
         double* stage = static_cast<double*>(c->pool.alloc(n * 8));
         if (!stage) return fail(SOG_ENOMEM, "block pool exhausted (staging)");
         CK(cudaMemcpyAsync(stage, tiles, n * 8, cudaMemcpyHostToDevice, c->stream));
+        s->launches++;
         convert_tiles_launch(stage, (float*)s->tiles + 4096, (int64_t)n, c->stream);
         CK(cudaStreamSynchronize(c->stream));
         c->pool.release(stage, n * 8);
@@ -725,7 +747,9 @@ int sog_solve(sog_system* s, int32_t nrhs, const double* b, double* x, sog_solve
     if (!r || r == SOG_ENOCONV) {
         r = solve_device_impl(s, nrhs, db, dx, stats);
         if (!r || r == SOG_ENOCONV || r == SOG_ENAN) {
-            if (cudaMemcpy(x, dx, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) r = fail(SOG_ECUDA, "download failed");
+            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)
+                r = fail(SOG_ECUDA, "download failed");
         }
     }
     c->pool.release(db, bytes);
@@ -746,8 +770,10 @@ int sog_solve_permuted(sog_system* s, const double* b_ext, double* x_ext) {
     if (s->fp64) {
         if ((r = trisolve(s, s->d_xext, 1))) return r;
     } else {
+        s->launches++;
         cast_f64_to_f32_launch(s->d_xext, s->d_v32, ne, c->stream);
         if ((r = trisolve(s, s->d_v32, 1))) return r;
+        s->launches++;
         axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 1, c->stream);
     }
     CK(cudaEventRecord(c->e1, c->stream));
@@ -819,6 +845,7 @@ int sog_system_task_info(const sog_system* s, int64_t* counts) {
     counts[3] = g.gemm_pairs;
     for (int k = 0; k < 5; k++) counts[4 + k] = g.count[k];
     counts[9] = s->grid_factor;
+    counts[10] = s->launches;
     return SOG_OK;
 }
 
