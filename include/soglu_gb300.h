@@ -156,10 +156,26 @@ int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
  * context's stream). */
 int sog_system_last_times(const sog_system *sys, double *factor_ms, double *solve_ms);
 void sog_system_destroy(sog_system *sys);
+/* Build the device task graph of a plan on the host only (no device):
+ * counts[12] = {tasks, dependency levels, queue items, tile-product pairs,
+ * GEMM, LU, LINV, UINV, SUB tasks, fused Schur subs, added diagonal-inverse
+ * blocks, critical-path length in tasks}. */
+int sog_plan_task_graph_info(const sog_plan *plan, int32_t gemm_split, int64_t *counts);
 /* Task-graph summary: counts[11] = {tasks, dependency levels, queue items,
  * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid,
  * kernel launches issued by this system so far}. */
 int sog_system_task_info(const sog_system *sys, int64_t *counts);
+
+/* ---- profiling (no reference counterpart: the reference prints phase
+ * timers only, solver.cpp:53-118) ---------------------------------------------
+ * Per-task device timestamps (globaltimer ns) of the next factorisations:
+ * task_trace[4*t] = {ready, ~start, end, SM id} (start is stored inverted;
+ * ready = 0 for tasks ready at launch), row_trace[4*i] = {lower start, lower
+ * end, upper start, upper end} of the last substitution. */
+int sog_system_trace_enable(sog_system *sys, int32_t on);
+int sog_system_trace_get(sog_system *sys, uint64_t *task_trace, uint64_t *row_trace, int32_t *task_kind);
+/* Task graph export: succ_ptr[tasks+1], succ[...], npairs[tasks] (GEMM operand pairs). */
+int sog_system_task_graph(const sog_system *sys, int32_t *succ_ptr, int32_t *succ, int32_t *npairs);
 
 /* ---- failure handling (no reference counterpart: the reference has no
  * device waits) ------------------------------------------------------------

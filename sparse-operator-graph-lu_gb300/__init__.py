@@ -66,7 +66,8 @@ EXPORTS = [
     "sog_system_create", "sog_system_bytes", "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve",
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
     "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
-    "sog_debug_unpoison", "soglu_solveLU",
+    "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
+    "sog_system_task_graph", "sog_plan_task_graph_info",
 ]
 
 _lib = None
@@ -97,6 +98,8 @@ def lib() -> C.CDLL:
         "sog_system_task_info": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
         "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
+        "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
+        "sog_system_task_graph": ([P, P, P, P], I32), "sog_plan_task_graph_info": ([P, I32, P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -165,6 +168,14 @@ class Plan:
         t = np.empty((self.info.n_input, 64, 64), np.float64)
         _check(lib().sog_plan_input_tiles(self._h, _p(v), _p(t)))
         return t
+
+    def task_graph_info(self, gemm_split: int = 1) -> dict:
+        """Device task graph built on the host (no GPU needed)."""
+        c = np.zeros(12, np.int64)
+        _check(lib().sog_plan_task_graph_info(self._h, gemm_split, _p(c)))
+        keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "fused_subs",
+                "added_inverses", "critical_path"]
+        return dict(zip(keys, (int(v) for v in c)))
 
     def bytes_needed(self, precision: int = FP64) -> int:
         o = Options(precision=precision)
@@ -276,6 +287,29 @@ class System:
         _check(lib().sog_system_task_info(self._h, _p(c)))
         keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "grid", "launches"]
         return dict(zip(keys, (int(v) for v in c)))
+
+    def trace_enable(self, on: bool = True) -> None:
+        _check(lib().sog_system_trace_enable(self._h, int(on)))
+
+    def trace_get(self):
+        """(tasks[t] = (ready_ns, start_ns, end_ns, sm), kinds[t], rows[i] = (l0, l1, u0, u1))."""
+        ti = self.task_info()
+        tt = np.zeros((ti["tasks"], 4), np.uint64)
+        rt = np.zeros((self.plan.info.block_rows, 4), np.uint64)
+        kind = np.zeros(ti["tasks"], np.int32)
+        _check(lib().sog_system_trace_get(self._h, _p(tt), _p(rt), _p(kind)))
+        tt[:, 1] = ~tt[:, 1]
+        return tt, kind, rt
+
+    def task_graph(self):
+        """(succ_ptr, succ, npairs) of the device task graph."""
+        ti = self.task_info()
+        sp = np.zeros(ti["tasks"] + 1, np.int32)
+        _check(lib().sog_system_task_graph(self._h, _p(sp), None, None))
+        sc = np.zeros(max(int(sp[-1]), 1), np.int32)
+        npairs = np.zeros(ti["tasks"], np.int32)
+        _check(lib().sog_system_task_graph(self._h, _p(sp), _p(sc), _p(npairs)))
+        return sp, sc[:sp[-1]], npairs
 
     def set_wait_limit(self, ms: float) -> None:
         _check(lib().sog_system_set_wait_limit(self._h, ms))

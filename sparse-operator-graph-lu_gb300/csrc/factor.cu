@@ -8,6 +8,9 @@
 // FP64 path: tile products on the FP64 tensor pipe (DMMA, mma.sync m8n8k4).
 // Mixed path: FP32 tiles, tile products as split-precision TF32 (3 products:
 // hi*hi + hi*lo + lo*hi, FP32 accumulation).
+// Operand tiles stream into shared memory with cp.async (L2 only: tiles are
+// produced by other SMs during the same launch), double-buffered over the
+// operand pairs of a product so the next pair loads while this one computes.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -20,16 +23,18 @@ namespace {
 
 constexpr int NT = 256;  // threads per CTA for every task kind
 constexpr int LD = 65;   // padded leading dimension of square smem tiles
+constexpr unsigned FULL = 0xffffffffu;
 
 // smem footprints (elements of T)
-constexpr int F64_GEMM_ELEMS = 32 * 68 + 64 * 40;
-constexpr int F32_GEMM_ELEMS = 64 * 68 + 64 * 72;
-constexpr int TWO_TILES = 2 * 64 * LD + 64;
+constexpr int F64_STAGE = 32 * 68 + 64 * 40;  // A quadrant rows + B quadrant columns
+constexpr int F32_STAGE = 64 * 68 + 64 * 72;  // full A and B tiles
+constexpr int INV_ELEMS = 64 * LD + 2 * 64;   // source tile + double-buffered row
+constexpr int LU_ELEMS = 2 * 64 + 2 * 64;     // double-buffered row + pivots + reciprocals
 
 template <typename T>
 constexpr int smem_elems() {
-    return sizeof(T) == 8 ? (F64_GEMM_ELEMS > TWO_TILES ? F64_GEMM_ELEMS : TWO_TILES)
-                          : (F32_GEMM_ELEMS > TWO_TILES ? F32_GEMM_ELEMS : TWO_TILES);
+    constexpr int g = 2 * (sizeof(T) == 8 ? F64_STAGE : F32_STAGE);
+    return g > INV_ELEMS ? g : INV_ELEMS;
 }
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -37,12 +42,22 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
-// ---------------------------------------------------------------- tile loads
-// Load a 64x64 tile from global (L2, bypassing L1: tiles are produced by other
-// SMs during the same launch) into smem with leading dimension LD.
 template <typename T>
 __device__ __forceinline__ void load_tile(const T* __restrict__ g, T* s) {
     for (int e = threadIdx.x; e < 4096; e += NT) s[(e >> 6) * LD + (e & 63)] = __ldcg(g + e);
@@ -55,46 +70,61 @@ __device__ __forceinline__ void dmma_8x8x4(double (&c)[2], double a, double b) {
                  : "d"(a), "d"(b));
 }
 
-// C[quadrant q] = sum_p s_p A_p[rows] * B_p[cols] for one 32x32 output quadrant.
-// 8 warps: warp w owns rows (w&3)*8..+8 and columns (w>>2)*16..+16 (two 8x8 MMA tiles).
+// C[quadrant q] = init[quadrant q] + sum_p s_p A_p[rows] * B_p[cols] for one 32x32
+// output quadrant. 8 warps: warp w owns rows (w&3)*8..+8 and columns
+// (w>>2)*16..+16 (two 8x8 MMA tiles). Pairs stream through two smem stages.
 __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles, int task, int q, double* sm) {
-    double* sA = sm;            // [32][68]
-    double* sB = sm + 32 * 68;  // [64][40]
     const int r0 = (q >> 1) * 32, c0 = (q & 1) * 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3, rg = warp & 3, ch = warp >> 2;
-    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
     const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
-    for (int p = p0; p < p1; p++) {
-        const int pa = tk.pair_a[p];
+    auto issue = [&](int p, int s) {
+        double* sA = sm + s * F64_STAGE;
+        double* sB = sA + 32 * 68;
         const int pbs = tk.pair_b[p];
-        const double sgn = pbs < 0 ? -1.0 : 1.0;
-        const int pb = pbs < 0 ? -pbs : pbs;
-        const double* A = tiles + (size_t)pa * 4096 + r0 * 64;
-        const double* Bm = tiles + (size_t)pb * 4096 + c0;
-        __syncthreads();
+        const double* A = tiles + (size_t)tk.pair_a[p] * 4096 + r0 * 64;
+        const double* B = tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096 + c0;
         for (int i = tid; i < 1024; i += NT) {
-            const int row = i >> 5, c2 = (i & 31) * 2;
-            double2 v = __ldcg(reinterpret_cast<const double2*>(A + row * 64 + c2));
-            sA[row * 68 + c2] = v.x * sgn;
-            sA[row * 68 + c2 + 1] = v.y * sgn;
+            const int ra = i >> 5, ca = (i & 31) * 2;
+            cp_async16(sA + ra * 68 + ca, A + ra * 64 + ca);
+            const int rb = i >> 4, cb = (i & 15) * 2;
+            cp_async16(sB + rb * 40 + cb, B + rb * 64 + cb);
         }
-        for (int i = tid; i < 1024; i += NT) {
-            const int row = i >> 4, c2 = (i & 15) * 2;
-            double2 v = __ldcg(reinterpret_cast<const double2*>(Bm + row * 64 + c2));
-            sB[row * 40 + c2] = v.x;
-            sB[row * 40 + c2 + 1] = v.y;
+        cp_commit();
+    };
+    double acc[2][2];
+    const int init = tk.a[task];
+#pragma unroll
+    for (int nt = 0; nt < 2; nt++) {
+        if (init > 0) {
+            const double2 v = __ldcg(reinterpret_cast<const double2*>(
+                tiles + (size_t)init * 4096 + (r0 + rg * 8 + g) * 64 + c0 + ch * 16 + nt * 8 + 2 * t));
+            acc[nt][0] = v.x;
+            acc[nt][1] = v.y;
+        } else {
+            acc[nt][0] = acc[nt][1] = 0.0;
+        }
+    }
+    if (p0 < p1) issue(p0, 0);
+    for (int p = p0; p < p1; p++) {
+        const int s = (p - p0) & 1;
+        if (p + 1 < p1) {
+            issue(p + 1, s ^ 1);
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
         }
         __syncthreads();
+        const double* sA = sm + s * F64_STAGE;
+        const double* sB = sA + 32 * 68;
+        const double sgn = tk.pair_b[p] < 0 ? -1.0 : 1.0;
 #pragma unroll
         for (int k0 = 0; k0 < 64; k0 += 4) {
-            const double a = sA[(rg * 8 + g) * 68 + k0 + t];
+            const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
 #pragma unroll
-            for (int nt = 0; nt < 2; nt++) {
-                const double b = sB[(k0 + t) * 40 + ch * 16 + nt * 8 + g];
-                dmma_8x8x4(acc[nt], a, b);
-            }
+            for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, sB[(k0 + t) * 40 + ch * 16 + nt * 8 + g]);
         }
+        __syncthreads();
     }
     double* C = tiles + (size_t)tk.out[task] * 4096;
 #pragma unroll
@@ -118,38 +148,56 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Full 64x64 output per CTA. 8 warps: warp w owns rows (w&3)*16..+16 and
-// columns (w>>2)*32..+32 (four m16n8 tiles).
+// C = init + sum_p s_p A_p * B_p, full 64x64 per CTA. 8 warps: warp w owns rows
+// (w&3)*16..+16 and columns (w>>2)*32..+32 (four m16n8 tiles).
 __device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm) {
-    float* sA = sm;            // [64][68]
-    float* sB = sm + 64 * 68;  // [64][72]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3, rt = warp & 3, cg = warp >> 2;
-    float acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
     const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
-    for (int p = p0; p < p1; p++) {
-        const int pa = tk.pair_a[p];
+    auto issue = [&](int p, int s) {
+        float* sA = sm + s * F32_STAGE;
+        float* sB = sA + 64 * 68;
         const int pbs = tk.pair_b[p];
-        const float sgn = pbs < 0 ? -1.f : 1.f;
-        const int pb = pbs < 0 ? -pbs : pbs;
-        const float* A = tiles + (size_t)pa * 4096;
-        const float* Bm = tiles + (size_t)pb * 4096;
-        __syncthreads();
+        const float* A = tiles + (size_t)tk.pair_a[p] * 4096;
+        const float* B = tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096;
         for (int i = tid; i < 1024; i += NT) {
             const int row = i >> 4, c4 = (i & 15) * 4;
-            float4 v = __ldcg(reinterpret_cast<const float4*>(A + row * 64 + c4));
-            v.x *= sgn; v.y *= sgn; v.z *= sgn; v.w *= sgn;
-            *reinterpret_cast<float4*>(sA + row * 68 + c4) = v;
-            float4 w = __ldcg(reinterpret_cast<const float4*>(Bm + row * 64 + c4));
-            *reinterpret_cast<float4*>(sB + row * 72 + c4) = w;
+            cp_async16(sA + row * 68 + c4, A + row * 64 + c4);
+            cp_async16(sB + row * 72 + c4, B + row * 64 + c4);
+        }
+        cp_commit();
+    };
+    float acc[4][4];
+    const int init = tk.a[task];
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+        if (init > 0) {
+            const float* I = tiles + (size_t)init * 4096 + (rt * 16 + g) * 64 + cg * 32 + nt * 8 + 2 * t;
+            const float2 u = __ldcg(reinterpret_cast<const float2*>(I));
+            const float2 v = __ldcg(reinterpret_cast<const float2*>(I + 8 * 64));
+            acc[nt][0] = u.x; acc[nt][1] = u.y; acc[nt][2] = v.x; acc[nt][3] = v.y;
+        } else {
+            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+        }
+    }
+    if (p0 < p1) issue(p0, 0);
+    for (int p = p0; p < p1; p++) {
+        const int s = (p - p0) & 1;
+        if (p + 1 < p1) {
+            issue(p + 1, s ^ 1);
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
         }
         __syncthreads();
+        const float* sA = sm + s * F32_STAGE;
+        const float* sB = sA + 64 * 68;
+        const float sgn = tk.pair_b[p] < 0 ? -1.f : 1.f;
 #pragma unroll 2
         for (int k0 = 0; k0 < 64; k0 += 8) {
-            float af[4] = {sA[(rt * 16 + g) * 68 + k0 + t], sA[(rt * 16 + g + 8) * 68 + k0 + t],
-                           sA[(rt * 16 + g) * 68 + k0 + t + 4], sA[(rt * 16 + g + 8) * 68 + k0 + t + 4]};
+            const float af[4] = {sgn * sA[(rt * 16 + g) * 68 + k0 + t], sgn * sA[(rt * 16 + g + 8) * 68 + k0 + t],
+                                 sgn * sA[(rt * 16 + g) * 68 + k0 + t + 4],
+                                 sgn * sA[(rt * 16 + g + 8) * 68 + k0 + t + 4]};
             uint32_t ahi[4], alo[4];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -159,17 +207,18 @@ __device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int
 #pragma unroll
             for (int nt = 0; nt < 4; nt++) {
                 const int col = cg * 32 + nt * 8 + g;
-                float bf[2] = {sB[(k0 + t) * 72 + col], sB[(k0 + t + 4) * 72 + col]};
+                const float b0 = sB[(k0 + t) * 72 + col], b1 = sB[(k0 + t + 4) * 72 + col];
                 uint32_t bhi[2], blo[2];
-                bhi[0] = to_tf32(bf[0]);
-                bhi[1] = to_tf32(bf[1]);
-                blo[0] = to_tf32(bf[0] - __uint_as_float(bhi[0]));
-                blo[1] = to_tf32(bf[1] - __uint_as_float(bhi[1]));
+                bhi[0] = to_tf32(b0);
+                bhi[1] = to_tf32(b1);
+                blo[0] = to_tf32(b0 - __uint_as_float(bhi[0]));
+                blo[1] = to_tf32(b1 - __uint_as_float(bhi[1]));
                 mma_tf32(acc[nt], alo, bhi);
                 mma_tf32(acc[nt], ahi, blo);
                 mma_tf32(acc[nt], ahi, bhi);
             }
         }
+        __syncthreads();
     }
     float* C = tiles + (size_t)tk.out[task] * 4096;
 #pragma unroll
@@ -182,103 +231,139 @@ __device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int
 }
 
 // ---------------------------------------------------------------- LU of a diagonal block
-// Right-looking unpivoted LU; pivots with |u_kk| < 1e-9 are clamped to
-// +-1e-9 (sign kept, 0 -> +1e-9) exactly as ludcmpSimple does
-// (MatrixStdDouble.cpp:2751-2761). L is unit lower, U upper. The pivot test,
-// the clamp and the growth ratio are evaluated in FP64 in both precisions.
+// Right-looking unpivoted LU held in registers: thread t owns row t>>2,
+// columns (t&3) + 4m (m = 0..15). Step k: the four owners of row k scale it by
+// the pivot into a shared row buffer (double-buffered, so one barrier per step),
+// every lower row applies the rank-1 update, and the owner of column k turns
+// its entry into l_ik. Pivots with |u_kk| < 1e-9 are clamped to +-1e-9 (sign
+// kept, 0 -> +1e-9) as ludcmpSimple does (MatrixStdDouble.cpp:2751-2761); the
+// pivot test, clamp and growth ratio are evaluated in FP64 in both precisions.
 template <typename T>
 __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
-    T* S = sm;                 // [64][LD]
-    T* piv = sm + 64 * LD;     // [64]
+    T* rowbuf = sm;          // [2][64]
+    T* piv = sm + 128;       // [64] clamped pivots
+    T* rpiv = sm + 192;      // [64] their reciprocals
+    __shared__ int s_clamped;
+    __shared__ unsigned long long s_minp;
     __shared__ float s_maxa, s_maxu;
-    const int tid = threadIdx.x;
-    if (tid == 0) { s_maxa = 0.f; s_maxu = 0.f; }
-    const T* A = tiles + (size_t)tk.a[task] * 4096;
-    __syncthreads();
+    const int tid = threadIdx.x, lane = tid & 31, r = tid >> 2, q = tid & 3;
+    if (tid == 0) {
+        s_clamped = 0;
+        s_minp = dbits(1e300);
+        s_maxa = 0.f;
+        s_maxu = 0.f;
+    }
+    const T* A = tiles + (size_t)tk.a[task] * 4096 + r * 64 + q;
+    T a[16];
     float ma = 0.f;
-    for (int e = tid; e < 4096; e += NT) {
-        T v = __ldcg(A + e);
-        S[(e >> 6) * LD + (e & 63)] = v;
-        ma = fmaxf(ma, fabsf((float)v));
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+        a[m] = __ldcg(A + 4 * m);
+        ma = fmaxf(ma, fabsf((float)a[m]));
     }
-    for (int o = 16; o > 0; o >>= 1) ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
-    if ((tid & 31) == 0) atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
     __syncthreads();
+#pragma unroll
     for (int k = 0; k < 64; k++) {
-        double pd = (double)S[k * LD + k];
-        const bool clamp = (pd < 1e-9 && pd > -1e-9);
-        if (clamp) pd = pd < 0 ? -1e-9 : 1e-9;
-        const T p = (T)pd;
-        const T rp = T(1) / p;
-        for (int i = k + 1 + tid; i < 64; i += NT) S[i * LD + k] *= rp;
-        if (tid == 0) {
-            piv[k] = p;
-            if (clamp) atomicAdd(&tk.status->clamped, 1);
-            double ap = fabs((double)S[k * LD + k]);
-            atomicMin(&tk.status->min_pivot_bits, dbits(ap));
+        const int km = k >> 2, kq = k & 3;
+        T* rb = rowbuf + (k & 1) * 64;
+        const T aik = __shfl_sync(FULL, a[km], (lane & ~3) | kq);  // a[r][k] for this thread's row
+        if (r == k) {
+            double pd = (double)aik;
+            const bool cl = (pd < 1e-9 && pd > -1e-9);
+            if (cl) pd = pd < 0 ? -1e-9 : 1e-9;
+            const T p = (T)pd;
+            const T rp = T(1) / p;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int c = q + 4 * m;
+                if (c > k) rb[c] = a[m] * rp;
+            }
+            if (q == 0) {
+                piv[k] = p;
+                rpiv[k] = rp;
+                if (cl) atomicAdd(&s_clamped, 1);
+                atomicMin(&s_minp, dbits(fabs((double)aik)));
+            }
         }
         __syncthreads();
-        const int m = 63 - k;
-        for (int idx = tid; idx < m * m; idx += NT) {
-            const int i = k + 1 + idx / m, j = k + 1 + idx % m;
-            S[i * LD + j] -= S[i * LD + k] * S[k * LD + j];
+        if (r > k) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int c = q + 4 * m;
+                if (c > k) a[m] -= aik * rb[c];
+            }
+            if (q == kq) a[km] = aik * rpiv[k];
         }
-        __syncthreads();
     }
-    T* L = tiles + (size_t)tk.out[task] * 4096;
-    T* U = tiles + (size_t)tk.out2[task] * 4096;
+    T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
+    T* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + q;
     float mu = 0.f;
-    for (int e = tid; e < 4096; e += NT) {
-        const int i = e >> 6, j = e & 63;
-        const T s = S[i * LD + j];
-        L[e] = i > j ? s : (i == j ? T(1) : T(0));
-        const T u = i < j ? s : (i == j ? piv[i] : T(0));
-        U[e] = u;
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+        const int c = q + 4 * m;
+        L[4 * m] = r > c ? a[m] : (r == c ? T(1) : T(0));
+        const T u = r < c ? a[m] : (r == c ? piv[r] : T(0));
+        U[4 * m] = u;
         mu = fmaxf(mu, fabsf((float)u));
     }
-    for (int o = 16; o > 0; o >>= 1) mu = fmaxf(mu, __shfl_xor_sync(0xffffffffu, mu, o));
-    if ((tid & 31) == 0) atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
+    for (int o = 16; o > 0; o >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(FULL, ma, o));
+        mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
+    }
+    if (lane == 0) {
+        atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
+        atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
+    }
     __syncthreads();
-    if (tid == 0 && s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
+    if (tid == 0) {
+        if (s_clamped) atomicAdd(&tk.status->clamped, s_clamped);
+        atomicMin(&tk.status->min_pivot_bits, s_minp);
+        if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
+    }
 }
 
 // ---------------------------------------------------------------- triangular inverses
-// Column-parallel: 4 threads per column j (tid = 4*j + s) split each inner
-// product and combine with shuffles. Y = L^-1 uses only the lower triangle of
-// the source including its diagonal (inv_lower, MatrixStdDouble.cpp:2787-2802);
-// Y = U^-1 only the upper triangle (inv_upper, MatrixStdDouble.cpp:2829-2866).
+// Y = L^-1 by forward elimination on the identity, Y = U^-1 by backward
+// elimination, the working rows held in registers (thread t owns row t>>2,
+// columns (t&3) + 4m) and one barrier per step. Y = L^-1 reads only the lower
+// triangle of the source including its diagonal (inv_lower,
+// MatrixStdDouble.cpp:2787-2802); Y = U^-1 only the upper triangle (inv_upper,
+// MatrixStdDouble.cpp:2829-2866).
 template <typename T, bool LOWER>
 __device__ void inv_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
-    T* M = sm;            // source [64][LD]
-    T* Y = sm + 64 * LD;  // result [64][LD]
+    T* M = sm;                  // source [64][LD]
+    T* rowbuf = sm + 64 * LD;   // [2][64]
+    const int tid = threadIdx.x, r = tid >> 2, q = tid & 3;
     load_tile(tiles + (size_t)tk.a[task] * 4096, M);
+    T w[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) w[m] = (q + 4 * m == r) ? T(1) : T(0);
     __syncthreads();
-    const int j = threadIdx.x >> 2, s = threadIdx.x & 3;
-    for (int step = 0; step < 64; step++) {
-        const int i = LOWER ? step : 63 - step;
-        T part = T(0);
-        if (LOWER) {
-            if (i > j)
-                for (int k = j + s; k < i; k += 4) part += M[i * LD + k] * Y[k * LD + j];
-        } else {
-            if (i < j)
-                for (int k = i + 1 + s; k <= j; k += 4) part += M[i * LD + k] * Y[k * LD + j];
+#pragma unroll
+    for (int kk = 0; kk < 64; kk++) {
+        const int k = LOWER ? kk : 63 - kk;
+        T* rb = rowbuf + (kk & 1) * 64;
+        if (r == k) {
+            const T d = T(1) / M[k * LD + k];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                w[m] *= d;
+                rb[q + 4 * m] = w[m];
+            }
         }
-        part += __shfl_xor_sync(0xffffffffu, part, 1);
-        part += __shfl_xor_sync(0xffffffffu, part, 2);
-        if (s == 0) {
-            const T q = T(1) / M[i * LD + i];
-            T y;
-            if (i == j) y = q;
-            else if (LOWER ? (i > j) : (i < j)) y = -part * q;
-            else y = T(0);
-            Y[i * LD + j] = y;
+        __syncthreads();
+        if (LOWER ? (r > k) : (r < k)) {
+            const T mk = M[r * LD + k];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int c = q + 4 * m;
+                if (LOWER ? (c <= k) : (c >= k)) w[m] -= mk * rb[c];
+            }
         }
-        __syncwarp();
     }
-    __syncthreads();
-    T* out = tiles + (size_t)tk.out[task] * 4096;
-    for (int e = threadIdx.x; e < 4096; e += NT) out[e] = Y[(e >> 6) * LD + (e & 63)];
+    T* out = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
+#pragma unroll
+    for (int m = 0; m < 16; m++) out[4 * m] = w[m];
 }
 
 // R = A2 - A1; copy / negate when one side is absent (BlockPlanner.cpp:553-572)
@@ -288,6 +373,7 @@ __device__ void sub_task(const DevTasks& tk, T* __restrict__ tiles, int task) {
     const T* X = tiles + (size_t)a2 * 4096;
     const T* Z = tiles + (size_t)a1 * 4096;
     T* R = tiles + (size_t)tk.out[task] * 4096;
+#pragma unroll 4
     for (int e = threadIdx.x; e < 4096; e += NT) {
         T v = a2 > 0 ? __ldcg(X + e) : T(0);
         if (a1 > 0) v -= __ldcg(Z + e);
@@ -300,9 +386,14 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
     switch (tk.kind[task]) {
         case K_GEMM:
             if constexpr (sizeof(T) == 8) {
-                if (tk.parts[task] == 4) gemm_f64_quadrant(tk, tiles, task, part, sm);
-                else
-                    for (int q = 0; q < 4; q++) gemm_f64_quadrant(tk, tiles, task, q, sm);
+                if (tk.parts[task] == 4) {
+                    gemm_f64_quadrant(tk, tiles, task, part, sm);
+                } else {
+                    for (int q = 0; q < 4; q++) {
+                        gemm_f64_quadrant(tk, tiles, task, q, sm);
+                        __syncthreads();
+                    }
+                }
             } else {
                 gemm_f32_full(tk, tiles, task, sm);
             }
@@ -315,67 +406,106 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
     }
 }
 
-// Mark an item done; the last part of a task releases its successors, and a
-// successor whose last dependency this was is appended to the ready queue.
-// Called by warp 0 after the CTA's writes are complete.
-__device__ void complete_item(const DevTasks& tk, int task) {
+// Append `cnt` items of task t (parts from..parts-1) to the ready queue.
+__device__ __forceinline__ void push_task(const DevTasks& tk, int t, int from) {
+    const int np = tk.parts[t];
+    const int pos = atomicAdd(tk.tail, np - from);
+    for (int p = from; p < np; p++) atomicExch(&tk.queue[pos + p - from], (t << 2) | p);
+}
+
+// Called by warp 0 once the CTA's writes for an item are complete. The last
+// part of a task releases its successors; of those that become ready, the one
+// with the longest remaining path is kept to run next on this CTA (no queue
+// round trip on the critical chain) and the others are queued. Returns the
+// kept item or -1.
+__device__ int complete_item(const DevTasks& tk, int task) {
     const int lane = threadIdx.x & 31;
     int last = 0;
     if (lane == 0) {
         __threadfence();
         last = (tk.parts[task] == 1) || (atomicSub(&tk.parts_left[task], 1) == 1);
     }
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();
-    const int s0 = tk.succ_ptr[task], s1 = tk.succ_ptr[task + 1];
-    for (int k = s0 + lane; k < s1; k += 32) {
-        const int s = tk.succ[k];
-        if (atomicSub(&tk.dep[s], 1) == 1) {
-            __threadfence();
-            const int np = tk.parts[s];
-            const int pos = atomicAdd(tk.tail, np);
-            for (int p = 0; p < np; p++) atomicExch(&tk.queue[pos + p], (s << 2) | p);
+    last = __shfl_sync(FULL, last, 0);
+    int keep = -1, keep_prio = -1;
+    if (last) {
+        const int s0 = tk.succ_ptr[task], s1 = tk.succ_ptr[task + 1];
+        for (int base = s0; base < s1; base += 32) {
+            const int k = base + lane;
+            int s = -1;
+            if (k < s1) {
+                s = tk.succ[k];
+                if (atomicSub(&tk.dep[s], 1) != 1) s = -1;
+                else if (tk.trace) tk.trace[4 * (size_t)s] = globaltimer_ns();
+            }
+            unsigned m = __ballot_sync(FULL, s >= 0);
+            if (m) __threadfence();
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                const int t = __shfl_sync(FULL, s, l);
+                if (lane == 0) {
+                    const int pr = tk.prio[t];
+                    if (pr > keep_prio) {
+                        if (keep >= 0) push_task(tk, keep, 0);
+                        keep = t;
+                        keep_prio = pr;
+                    } else {
+                        push_task(tk, t, 0);
+                    }
+                }
+            }
         }
+        if (lane == 0 && keep >= 0 && tk.parts[keep] > 1) push_task(tk, keep, 1);
     }
+    if (lane == 0) {
+        __threadfence();
+        atomicAdd(tk.done, 1);
+    }
+    return __shfl_sync(FULL, keep >= 0 ? (keep << 2) : -1, 0);
 }
 
-__device__ __forceinline__ int ld_acquire(const int* p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Each CTA claims the next queue slot, waits (bounded) until a producer has
-// filled it, runs the item and releases successors. Every slot is filled
-// exactly once because every task becomes ready exactly once, so the loop
-// ends when all slots are claimed; no CTA ever waits inside a task.
+// Each CTA runs the item it kept from its last completion, else claims the
+// next queue slot and waits (bounded) until a producer fills it. The launch
+// ends when every item has completed; no CTA ever waits inside a task.
 template <typename T>
 __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
-    __shared__ int s_item, s_stop;
+    __shared__ int s_item, s_next, s_stop;
+    if (threadIdx.x == 0) s_next = -1;
     for (;;) {
         if (threadIdx.x == 0) {
-            int item = -1;
-            const int slot = atomicAdd(tk.head, 1);
-            if (slot < tk.total_items) {
-                const unsigned long long t0 = globaltimer_ns();
-                unsigned ns = 32;
-                while ((item = ld_acquire(tk.queue + slot)) < 0) {
-                    if (globaltimer_ns() - t0 > tk.wait_limit_ns) {
-                        atomicOr(&tk.status->flags, ST_TIMEOUT);
-                        tk.status->timeout_where = slot;
-                        item = -2;
-                        break;
+            int item = s_next;
+            s_next = -1;
+            if (item < 0) {
+                const int slot = atomicAdd(tk.head, 1);
+                if (slot < tk.total_items) {
+                    const unsigned long long t0 = globaltimer_ns();
+                    unsigned spins = 0;
+                    while ((item = ld_acquire(tk.queue + slot)) < 0) {
+                        if ((++spins & 15) == 0) {
+                            if (ld_acquire(tk.done) >= tk.total_items) { item = -1; break; }
+                            if (globaltimer_ns() - t0 > tk.wait_limit_ns) {
+                                atomicOr(&tk.status->flags, ST_TIMEOUT);
+                                tk.status->timeout_where = slot;
+                                item = -1;
+                                break;
+                            }
+                        }
+                        __nanosleep(64);
                     }
-                    __nanosleep(ns);
-                    if (ns < 1024) ns *= 2;
+                    if (item >= 0 && (item >> 2) >= tk.ntasks) {
+                        atomicOr(&tk.status->flags, ST_BAD_ITEM);
+                        item = -1;
+                    }
                 }
-                if (item >= 0 && (item >> 2) >= tk.ntasks) {
-                    atomicOr(&tk.status->flags, ST_BAD_ITEM);
-                    item = -2;
-                }
+            }
+            if (item >= 0 && tk.trace) {
+                unsigned smid;
+                asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+                unsigned long long* tr = tk.trace + 4 * (size_t)(item >> 2);
+                atomicMax(tr + 1, ~globaltimer_ns());  // start = min over parts, stored inverted
+                tr[3] = smid;
             }
             __threadfence();
             s_item = item;
@@ -384,11 +514,16 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
         const int item = s_item;
         if (item < 0) break;
         run_item<T>(tk, tiles, item >> 2, item & 3, sm);
-        __threadfence();
         __syncthreads();
-        if (threadIdx.x < 32) complete_item(tk, item >> 2);
-        // a timeout anywhere stops every CTA at its next claim
-        if (threadIdx.x == 0) s_stop = (ld_acquire(&tk.status->flags) & ST_TIMEOUT) ? 1 : 0;
+        if (threadIdx.x < 32) {
+            if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 2) + 2, globaltimer_ns());
+            const int keep = complete_item(tk, item >> 2);
+            if (threadIdx.x == 0) {
+                s_next = keep;
+                // a timeout anywhere stops every CTA at its next claim
+                s_stop = (ld_acquire(&tk.status->flags) & ST_TIMEOUT) ? 1 : 0;
+            }
+        }
         __syncthreads();
         if (s_stop) break;
     }

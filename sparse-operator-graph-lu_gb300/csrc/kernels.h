@@ -27,7 +27,10 @@ struct DevTasks {
     int64_t total_items;
     const uint8_t* kind;
     const uint8_t* parts;
+    // out/out2: result blocks; a: source (LU/inverses), minuend (SUB) or initial
+    // tile of a product (GEMM, 0 = zero); b: subtrahend (SUB)
     const int32_t *out, *out2, *a, *b;
+    const int32_t* prio;  // longest path to a sink, for choosing which ready successor to keep
     const int32_t *pair_ptr, *pair_a, *pair_b;
     const int32_t *succ_ptr, *succ;
     int32_t* dep;         // working dependency counters
@@ -35,8 +38,11 @@ struct DevTasks {
     int32_t* queue;       // ready items (task << 2 | part); -1 = not yet filled
     int32_t* head;        // next slot to claim
     int32_t* tail;        // next slot to fill
+    int32_t* done;        // completed items
     DevStatus* status;
     unsigned long long wait_limit_ns;  // bound on any single queue wait
+    // optional per-task trace (4 x u64 per task: ready, start, end, sm id), NULL = off
+    unsigned long long* trace;
 };
 
 // ---- factor (factor.cu) ----
@@ -65,16 +71,20 @@ struct DevSolve {
     const int32_t *l_ptr, *l_col, *l_id;
     const int32_t *u_ptr, *u_col, *u_id;
     const int32_t *l_diag, *u_diag;  // diagonal block id per block row
+    const int32_t *l_dinv, *u_dinv;  // block id of the inverse of each diagonal block
     int32_t* flags;                  // per block row readiness epoch
     DevStatus* status;
     unsigned long long wait_limit_ns;
+    // optional trace (4 x u64 per block row: lower start/end, upper start/end), NULL = off
+    unsigned long long* trace;
 };
 // In-place block substitution on vec (n_ext x nrhs, row-major), lower then
-// upper. epoch: a fresh even number per call (forward uses epoch, backward epoch+1).
-int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int epoch, int grid,
-                    cudaStream_t st);
-int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
-                    cudaStream_t st);
+// upper, in chunks of up to 8 columns. epoch: readiness tag, advanced by 2 per
+// chunk (lower publishes epoch, upper epoch+1); launches counts kernels.
+int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int& epoch, int grid,
+                    cudaStream_t st, int& launches);
+int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int& epoch, int grid,
+                    cudaStream_t st, int& launches);
 int trisolve_grid(bool fp64, int nrhs, int num_sms);
 
 // CSR of the permuted, padded matrix for FP64 residuals

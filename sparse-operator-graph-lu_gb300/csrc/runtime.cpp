@@ -159,6 +159,8 @@ struct sog_system {
     float t_factor = 0, t_solve = 0;
     int grid_factor = 0;
     int64_t launches = 0;  // kernels launched by this system
+    unsigned long long* trace = nullptr;  // optional timing trace (tasks, then block rows)
+    uint64_t trace_bytes = 0;
     DevStatus last{};
     std::vector<Leaf> L, U;
 };
@@ -290,9 +292,10 @@ int run_factor(sog_system* s) {
     CK(cudaMemsetAsync(s->dt.queue, 0xff, sizeof(int32_t) * g.total_items, st));
     if (s->nready)
         CK(cudaMemcpyAsync(s->dt.queue, s->d_ready0, sizeof(int32_t) * s->nready, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(s->dt.head, s->d_counters0, sizeof(int32_t) * 2, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->dt.head, s->d_counters0, sizeof(int32_t) * 3, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.status, s->d_status0, sizeof(DevStatus), cudaMemcpyDeviceToDevice, st));
     (void)fs;
+    if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(unsigned long long) * 4 * g.ntasks, st));
     CK(cudaEventRecord(c->e0, st));
     int rc = 0;
     if (s->opt.executor == SOG_EXEC_LEVELS) {
@@ -320,10 +323,10 @@ int run_factor(sog_system* s) {
 int trisolve(sog_system* s, void* vec, int nrhs) {
     sog_ctx* c = s->ctx;
     const int grid = std::min(s->R, trisolve_grid(s->fp64, nrhs, c->num_sms));
-    int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, c->stream)
-                     : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, c->stream);
-    s->epoch += 2;
-    s->launches += 2;
+    int nl = 0;
+    int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, c->stream, nl)
+                     : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, c->stream, nl);
+    s->launches += nl;
     if (rc) return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     return SOG_OK;
 }
@@ -524,8 +527,20 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->U = p.U;
     int gemm_parts = o.gemm_split == 1 ? 1 : (o.gemm_split == 4 ? 4 : (s->fp64 ? 4 : 1));
     if (!s->fp64) gemm_parts = 1;
+    // inverses of the diagonal factor blocks for the substitution (reused
+    // where the DAG already computes them)
+    std::vector<Op> ops2 = p.ops;
+    int32_t storage2 = p.storage_count;
+    std::vector<int32_t> ldinv, udinv;
+    add_diag_inverses(ops2, storage2, s->R, p.L, p.U, ldinv, udinv);
+    s->storage = storage2;
+    std::vector<int32_t> outputs;
+    for (const Leaf& lf : p.L) outputs.push_back(lf.id);
+    for (const Leaf& lf : p.U) outputs.push_back(lf.id);
+    for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
+    for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
     try {
-        s->tg = build_tasks(p.ops, p.storage_count, p.n_input, gemm_parts);
+        s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts);
     } catch (const std::exception& e) {
         delete s;
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
@@ -558,7 +573,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // task arrays
     std::vector<int32_t> parts32(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) parts32[t] = g.parts[t];
-    std::vector<int32_t> counters0 = {0, (int32_t)g.ready_items.size()};
+    std::vector<int32_t> counters0 = {0, (int32_t)g.ready_items.size(), 0};
     std::vector<DevStatus> st0 = {fresh_status()};
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),
@@ -568,7 +583,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_succ = L.add<int32_t>(g.succ.size()), o_ndep0 = L.add<int32_t>(g.ntasks),
              o_dep = L.add<int32_t>(g.ntasks), o_parts0 = L.add<int32_t>(g.ntasks),
              o_pleft = L.add<int32_t>(g.ntasks), o_queue = L.add<int32_t>(g.total_items),
-             o_ready = L.add<int32_t>(g.ready_items.size()), o_cnt0 = L.add<int32_t>(2), o_cnt = L.add<int32_t>(2),
+             o_ready = L.add<int32_t>(g.ready_items.size()), o_cnt0 = L.add<int32_t>(3), o_cnt = L.add<int32_t>(3),
+             o_prio = L.add<int32_t>(g.ntasks), o_ldinv = L.add<int32_t>(s->R), o_udinv = L.add<int32_t>(s->R),
              o_levels = L.add<int32_t>(g.level_items.size()), o_st0 = L.add<DevStatus>(1), o_st = L.add<DevStatus>(1),
              o_lptr = L.add<int32_t>(lptr.size()), o_lcol = L.add<int32_t>(lcol.size()),
              o_lid = L.add<int32_t>(lid.size()), o_uptr = L.add<int32_t>(uptr.size()),
@@ -604,6 +620,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.out2 = put(A, o_out2, g.out2, st);
     dt.a = put(A, o_a, g.a, st);
     dt.b = put(A, o_b, g.b, st);
+    dt.prio = put(A, o_prio, g.prio, st);
     dt.pair_ptr = put(A, o_pptr, g.pair_ptr, st);
     dt.pair_a = put(A, o_pa, g.pair_a, st);
     dt.pair_b = put(A, o_pb, g.pair_b, st);
@@ -619,6 +636,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->d_counters0 = put(A, o_cnt0, counters0, st);
     dt.head = reinterpret_cast<int32_t*>(A + o_cnt);
     dt.tail = dt.head + 1;
+    dt.done = dt.head + 2;
     s->d_level_items = put(A, o_levels, g.level_items, st);
     s->d_status0 = put(A, o_st0, st0, st);
     dt.status = reinterpret_cast<DevStatus*>(A + o_st);
@@ -633,6 +651,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     ds.u_id = put(A, o_uid, uid, st);
     ds.l_diag = put(A, o_ldiag, ldiag, st);
     ds.u_diag = put(A, o_udiag, udiag, st);
+    ds.l_dinv = put(A, o_ldinv, ldinv, st);
+    ds.u_dinv = put(A, o_udinv, udinv, st);
     ds.flags = reinterpret_cast<int32_t*>(A + o_flags);
     cudaMemsetAsync(ds.flags, 0, sizeof(int32_t) * s->R, st);
     ds.status = dt.status;
@@ -670,6 +690,7 @@ void sog_system_destroy(sog_system* s) {
     c->pool.release(s->tiles, s->tiles_bytes);
     c->pool.release(s->aux, s->aux_bytes);
     c->pool.release(s->vecs, s->vec_bytes);
+    c->pool.release(s->trace, s->trace_bytes);
     delete s;
 }
 
@@ -833,6 +854,77 @@ int sog_debug_unpoison(sog_system* s) {
     if (!s) return fail(SOG_EINVAL, "bad argument");
     CK(cudaSetDevice(s->ctx->device));
     CK(cudaMemcpy(s->d_ndep0, s->tg.ndep.data(), sizeof(int32_t) * s->tg.ntasks, cudaMemcpyHostToDevice));
+    return SOG_OK;
+}
+
+int sog_system_trace_enable(sog_system* s, int32_t on) {
+    if (!s) return fail(SOG_EINVAL, "NULL system");
+    sog_ctx* c = s->ctx;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!on) {
+        c->pool.release(s->trace, s->trace_bytes);
+        s->trace = nullptr;
+        s->dt.trace = nullptr;
+        s->ds.trace = nullptr;
+        return SOG_OK;
+    }
+    if (s->trace) return SOG_OK;
+    s->trace_bytes = sizeof(unsigned long long) * 4 * ((uint64_t)s->tg.ntasks + s->R);
+    s->trace = static_cast<unsigned long long*>(c->pool.alloc(s->trace_bytes));
+    if (!s->trace) return fail(SOG_ENOMEM, "block pool exhausted (trace)");
+    CK(cudaMemset(s->trace, 0, s->trace_bytes));
+    s->dt.trace = s->trace;
+    s->ds.trace = s->trace + 4 * (uint64_t)s->tg.ntasks;
+    return SOG_OK;
+}
+
+int sog_system_trace_get(sog_system* s, uint64_t* task_trace, uint64_t* row_trace, int32_t* task_kind) {
+    if (!s || !s->trace) return fail(SOG_ESTATE, "trace not enabled");
+    CK(cudaSetDevice(s->ctx->device));
+    CK(cudaStreamSynchronize(s->ctx->stream));
+    if (task_trace)
+        CK(cudaMemcpy(task_trace, s->trace, sizeof(uint64_t) * 4 * s->tg.ntasks, cudaMemcpyDeviceToHost));
+    if (row_trace)
+        CK(cudaMemcpy(row_trace, s->trace + 4 * (uint64_t)s->tg.ntasks, sizeof(uint64_t) * 4 * s->R,
+                      cudaMemcpyDeviceToHost));
+    if (task_kind)
+        for (int32_t t = 0; t < s->tg.ntasks; t++) task_kind[t] = s->tg.kind[t];
+    return SOG_OK;
+}
+
+int sog_system_task_graph(const sog_system* s, int32_t* succ_ptr, int32_t* succ, int32_t* npairs) {
+    if (!s) return fail(SOG_EINVAL, "NULL system");
+    const TaskGraph& g = s->tg;
+    if (succ_ptr) std::memcpy(succ_ptr, g.succ_ptr.data(), sizeof(int32_t) * (g.ntasks + 1));
+    if (succ) std::memcpy(succ, g.succ.data(), sizeof(int32_t) * g.succ.size());
+    if (npairs)
+        for (int32_t t = 0; t < g.ntasks; t++) npairs[t] = g.pair_ptr[t + 1] - g.pair_ptr[t];
+    return SOG_OK;
+}
+
+int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* counts) {
+    if (!plan || !counts) return fail(SOG_EINVAL, "NULL argument");
+    const Plan& p = plan->p;
+    try {
+        std::vector<Op> ops2 = p.ops;
+        int32_t storage2 = p.storage_count;
+        std::vector<int32_t> ldinv, udinv, outputs;
+        add_diag_inverses(ops2, storage2, p.cfg.block_rows, p.L, p.U, ldinv, udinv);
+        for (const Leaf& lf : p.L) outputs.push_back(lf.id);
+        for (const Leaf& lf : p.U) outputs.push_back(lf.id);
+        TaskGraph g = build_tasks(ops2, storage2, p.n_input, outputs, gemm_split == 4 ? 4 : 1);
+        counts[0] = g.ntasks;
+        counts[1] = g.nlevels;
+        counts[2] = g.total_items;
+        counts[3] = g.gemm_pairs;
+        for (int k = 0; k < 5; k++) counts[4 + k] = g.count[k];
+        counts[9] = g.fused_subs;
+        counts[10] = storage2 - p.storage_count;
+        counts[11] = g.ntasks ? *std::max_element(g.prio.begin(), g.prio.end()) + 1 : 0;
+    } catch (const std::exception& e) {
+        return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
+    }
     return SOG_OK;
 }
 

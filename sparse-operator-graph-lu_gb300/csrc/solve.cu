@@ -42,110 +42,163 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// smem: Ts[64][LD] | Vs[64*nrhs] | Acc[64*nrhs]
-template <typename T>
-__global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int nrhs,
+// One launch per triangle and per chunk of NR right-hand-side columns
+// [c0, c0+NR) of vec (n_ext x ld, row-major). For block row i the warps split
+// its off-diagonal blocks: each warp waits (bounded) only for the row its
+// block multiplies, stages that row's NR-column slice in shared memory and
+// accumulates block * slice in registers (lane l: rows 2l, 2l+1). The warp
+// partials and b_i are combined, multiplied by the precomputed inverse of the
+// diagonal block, and the row is published with a release store.
+// smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR]
+template <typename T, int NR>
+__global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld, int c0,
                                                       int epoch, int lower) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* Ts = reinterpret_cast<T*>(smem_raw);
-    T* Vs = Ts + 64 * LD;
-    T* Acc = Vs + 64 * nrhs;
+    constexpr int NV = 64 * NR;
+    T* part = reinterpret_cast<T*>(smem_raw);
+    T* ybuf = part + 8 * NV;
+    T* acc = ybuf + 8 * NV;
     __shared__ int s_stop;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int R = s.block_rows;
-    const int nv = 64 * nrhs;
-    const int my_epoch = lower ? epoch : epoch + 1;
     const int* ptr = lower ? s.l_ptr : s.u_ptr;
     const int* col = lower ? s.l_col : s.u_col;
     const int* ids = lower ? s.l_id : s.u_id;
-    const int* diag = lower ? s.l_diag : s.u_diag;
+    const int* dinv = lower ? s.l_dinv : s.u_dinv;
     if (tid == 0) s_stop = 0;
+    __syncthreads();
+    T* yw = ybuf + warp * NV;
     for (int k = blockIdx.x; k < R; k += gridDim.x) {
         const int i = lower ? k : R - 1 - k;
-        for (int e = tid; e < nv; e += NT) Acc[e] = __ldcg(vec + (size_t)i * nv + e);
-        for (int q = ptr[i]; q < ptr[i + 1]; q++) {
+        if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
+        const T* Dm = tiles + (size_t)dinv[i] * 4096;
+        // warm L1 with this lane's slice of the diagonal inverse
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
+        T pa[NR], pb[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
+        bool stop = false;
+        for (int q = ptr[i] + warp; q < ptr[i + 1]; q += 8) {
             const int j = col[q];
-            if (tid == 0) {
+            const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
+            // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
+#pragma unroll
+            for (int o = 0; o < 128; o += 128 / (int)sizeof(T)) asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
+            if (lane == 0) {
                 const unsigned long long t0 = globaltimer_ns();
-                unsigned ns = 32;
-                while (ld_acquire(s.flags + j) != my_epoch) {
+                while (ld_acquire(s.flags + j) != epoch) {
                     if (globaltimer_ns() - t0 > s.wait_limit_ns) {
                         atomicOr(&s.status->flags, ST_SOLVE_TIMEOUT);
                         s_stop = 1;
                         break;
                     }
-                    __nanosleep(ns);
-                    if (ns < 512) ns *= 2;
+                    __nanosleep(32);
                 }
                 __threadfence();
             }
-            __syncthreads();
-            if (s_stop) return;
-            const T* B = tiles + (size_t)ids[q] * 4096;
-            const T* vj = vec + (size_t)j * nv;
-            if (nrhs == 1) {
-                if (tid < 64) Vs[tid] = __ldcg(vj + tid);
-                __syncthreads();
-                // warp w: rows w*8..w*8+7; lanes stream the row (coalesced)
-                for (int r = warp * 8; r < warp * 8 + 8; r++) {
-                    T v = __ldcg(B + r * 64 + lane) * Vs[lane] + __ldcg(B + r * 64 + lane + 32) * Vs[lane + 32];
-                    v = warp_sum(v);
-                    if (lane == 0) Acc[r] -= v;
-                }
-            } else {
-                for (int e = tid; e < 4096; e += NT) Ts[(e >> 6) * LD + (e & 63)] = __ldcg(B + e);
-                for (int e = tid; e < nv; e += NT) Vs[e] = __ldcg(vj + e);
-                __syncthreads();
-                for (int e = tid; e < nv; e += NT) {
-                    const int r = e / nrhs, c = e - r * nrhs;
-                    T acc = T(0);
+            __syncwarp();
+            if (*(volatile int*)&s_stop) {
+                stop = true;
+                break;
+            }
+            const T* vj = vec + (size_t)j * 64 * ld + c0;
+            for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
+            __syncwarp();
 #pragma unroll 8
-                    for (int kk = 0; kk < 64; kk++) acc += Ts[r * LD + kk] * Vs[kk * nrhs + c];
-                    Acc[e] -= acc;
+            for (int c = 0; c < 64; c++) {
+                const T b0 = __ldg(B + c), b1 = __ldg(B + 64 + c);
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    const T y = yw[c * NR + r];
+                    pa[r] += b0 * y;
+                    pb[r] += b1 * y;
                 }
             }
-            __syncthreads();
+            __syncwarp();
         }
-        // diagonal block: row-sequential substitution, one warp per rhs column
-        const T* D = tiles + (size_t)diag[i] * 4096;
-        for (int e = tid; e < 4096; e += NT) Ts[(e >> 6) * LD + (e & 63)] = __ldcg(D + e);
+        T* pw = part + warp * NV;
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            pw[(2 * lane) * NR + r] = pa[r];
+            pw[(2 * lane + 1) * NR + r] = pb[r];
+        }
         __syncthreads();
-        for (int c = warp; c < nrhs; c += NT / 32) {
-            for (int step = 0; step < 64; step++) {
-                const int r = lower ? step : 63 - step;
-                T v = T(0);
-                if (lower) {
-                    if (lane < r) v += Ts[r * LD + lane] * Acc[lane * nrhs + c];
-                    if (lane + 32 < r) v += Ts[r * LD + lane + 32] * Acc[(lane + 32) * nrhs + c];
-                } else {
-                    if (lane > r) v += Ts[r * LD + lane] * Acc[lane * nrhs + c];
-                    if (lane + 32 > r) v += Ts[r * LD + lane + 32] * Acc[(lane + 32) * nrhs + c];
-                }
-                v = warp_sum(v);
-                if (lane == 0) Acc[r * nrhs + c] = (Acc[r * nrhs + c] - v) / Ts[r * LD + r];
-                __syncwarp();
+        if (s_stop || stop) return;
+        for (int e = tid; e < NV; e += NT) {
+            T v = __ldcg(vec + ((size_t)i * 64 + e / NR) * ld + c0 + (e % NR));
+#pragma unroll
+            for (int w = 0; w < 8; w++) v -= part[w * NV + e];
+            acc[e] = v;
+        }
+        __syncthreads();
+        // y_i = inv(D_ii) * acc: warp w rows 8w..8w+7, four lanes per row
+        {
+            const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
+            T y[NR];
+#pragma unroll
+            for (int r = 0; r < NR; r++) y[r] = T(0);
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+                const T d = __ldg(Dm + row * 64 + cb + c);
+#pragma unroll
+                for (int r = 0; r < NR; r++) y[r] += d * acc[(cb + c) * NR + r];
+            }
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                y[r] += __shfl_xor_sync(0xffffffffu, y[r], 1);
+                y[r] += __shfl_xor_sync(0xffffffffu, y[r], 2);
+            }
+            if ((lane & 3) == 0) {
+#pragma unroll
+                for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
             }
         }
-        __syncthreads();
-        for (int e = tid; e < nv; e += NT) vec[(size_t)i * nv + e] = Acc[e];
         __threadfence();
         __syncthreads();
-        if (tid == 0) st_release(s.flags + i, my_epoch);
+        if (tid == 0) {
+            st_release(s.flags + i, epoch);
+            if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
+        }
     }
 }
 
-template <typename T>
-size_t trisolve_smem(int nrhs) {
-    return (64 * LD + 2 * 64 * (size_t)nrhs) * sizeof(T);
+template <typename T, int NR>
+size_t trisolve_smem() {
+    return (size_t)(17 * 64 * NR) * sizeof(T);
+}
+
+template <typename T, int NR>
+int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int& epoch, int grid, cudaStream_t st) {
+    const size_t smem = trisolve_smem<T, NR>();
+    cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, epoch, 1);
+    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, epoch + 1, 0);
+    epoch += 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <typename T>
-int trisolve_impl(const DevSolve& s, const T* tiles, T* vec, int nrhs, int epoch, int grid, cudaStream_t st) {
-    const size_t smem = trisolve_smem<T>(nrhs);
-    cudaFuncSetAttribute(trisolve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    trisolve_kernel<T><<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, epoch, 1);
-    trisolve_kernel<T><<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, epoch, 0);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+int trisolve_impl(const DevSolve& s, const T* tiles, T* vec, int nrhs, int& epoch, int grid, cudaStream_t st,
+                  int& launches) {
+    int rc = 0;
+    for (int c0 = 0; c0 < nrhs && rc == 0;) {
+        const int left = nrhs - c0;
+        if (left >= 8) { rc = trisolve_chunk<T, 8>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 8; }
+        else if (left >= 4) { rc = trisolve_chunk<T, 4>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 4; }
+        else if (left >= 2) { rc = trisolve_chunk<T, 2>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 2; }
+        else { rc = trisolve_chunk<T, 1>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 1; }
+        launches += 2;
+    }
+    return rc;
+}
+
+template <typename T, int NR>
+int occupancy_grid(int num_sms) {
+    int per_sm = 0;
+    const size_t smem = trisolve_smem<T, NR>();
+    cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trisolve_kernel<T, NR>, NT, smem);
+    return (per_sm < 1 ? 1 : per_sm) * num_sms;
 }
 
 // r = b - A x over CSR rows; per-rhs reductions red[c*5 + {0..4}] =
@@ -227,27 +280,30 @@ __global__ void nonfinite_kernel(const double* __restrict__ x, int64_t n, unsign
 
 }  // namespace
 
-int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int epoch, int grid,
-                    cudaStream_t st) {
-    return trisolve_impl<double>(s, tiles, vec, nrhs, epoch, grid, st);
+int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int& epoch, int grid,
+                    cudaStream_t st, int& launches) {
+    return trisolve_impl<double>(s, tiles, vec, nrhs, epoch, grid, st, launches);
 }
-int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
-                    cudaStream_t st) {
-    return trisolve_impl<float>(s, tiles, vec, nrhs, epoch, grid, st);
+int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int& epoch, int grid,
+                    cudaStream_t st, int& launches) {
+    return trisolve_impl<float>(s, tiles, vec, nrhs, epoch, grid, st, launches);
 }
 int trisolve_grid(bool fp64, int nrhs, int num_sms) {
-    int per_sm = 0;
+    // the smallest occupancy over the chunk widths this nrhs uses
+    int g = 1 << 30;
+    auto take = [&](int v) { g = v < g ? v : g; };
     if (fp64) {
-        const size_t smem = trisolve_smem<double>(nrhs);
-        cudaFuncSetAttribute(trisolve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trisolve_kernel<double>, NT, smem);
+        if (nrhs >= 8) take(occupancy_grid<double, 8>(num_sms));
+        if (nrhs % 8 >= 4) take(occupancy_grid<double, 4>(num_sms));
+        if (nrhs % 4 >= 2) take(occupancy_grid<double, 2>(num_sms));
+        if (nrhs % 2 == 1) take(occupancy_grid<double, 1>(num_sms));
     } else {
-        const size_t smem = trisolve_smem<float>(nrhs);
-        cudaFuncSetAttribute(trisolve_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trisolve_kernel<float>, NT, smem);
+        if (nrhs >= 8) take(occupancy_grid<float, 8>(num_sms));
+        if (nrhs % 8 >= 4) take(occupancy_grid<float, 4>(num_sms));
+        if (nrhs % 4 >= 2) take(occupancy_grid<float, 2>(num_sms));
+        if (nrhs % 2 == 1) take(occupancy_grid<float, 1>(num_sms));
     }
-    if (per_sm < 1) per_sm = 1;
-    return per_sm * num_sms;
+    return g;
 }
 
 void residual_launch(const DevCSR& A, const double* b, const double* x, double* r, int nrhs, double* red,

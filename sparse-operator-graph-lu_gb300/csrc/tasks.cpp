@@ -2,27 +2,34 @@
 
 #include <algorithm>
 #include <stdexcept>
+#include <unordered_map>
 
 namespace sog {
 
-TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input, int gemm_parts) {
+TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input,
+                      const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs) {
     if (gemm_parts != 1 && gemm_parts != 4) throw std::runtime_error("gemm_parts must be 1 or 4");
-    TaskGraph g;
-    g.storage_count = storage_count;
     const int64_t nops = (int64_t)ops.size();
     std::vector<int32_t> producer(storage_count, -1);  // block -> task
-    std::vector<int64_t> first_write(storage_count, -1);
+    std::vector<int32_t> readers(storage_count, 0);
     auto check_id = [&](int32_t id) {
         if (id < 0 || id >= storage_count) throw std::runtime_error("block id out of range in DAG");
     };
     // pass 1: one task per produced block (LU: per result pair)
-    std::vector<int32_t> op_task(nops);
+    struct T0 {
+        uint8_t kind;
+        int32_t out, out2, a, b;
+        std::vector<int32_t> pa, pb;
+        bool dead = false;
+    };
+    std::vector<T0> tl;
     for (int64_t i = 0; i < nops; i++) {
         const Op& o = ops[i];
         check_id(o.src); check_id(o.src2); check_id(o.res); check_id(o.res2);
         if (o.res <= 0) throw std::runtime_error("op without result");
-        if (o.res <= n_input || (o.res2 > 0 && o.res2 <= n_input))
-            throw std::runtime_error("op writes an input block");
+        if (o.res <= n_input || (o.res2 > 0 && o.res2 <= n_input)) throw std::runtime_error("op writes an input block");
+        if (o.src > 0) readers[o.src]++;
+        if (o.src2 > 0) readers[o.src2]++;
         uint8_t k;
         switch (o.op) {
             case OP_MUL: case OP_MULNEG: k = K_GEMM; break;
@@ -33,60 +40,92 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
             default: throw std::runtime_error("unsupported op kind " + std::to_string(o.op));
         }
         int32_t t = producer[o.res];
-        if (t >= 0) {
-            if (k != K_GEMM || g.kind[t] != K_GEMM) throw std::runtime_error("block written by more than one non-accumulating op");
-            op_task[i] = t;
-            continue;
+        if (t >= 0 && (k != K_GEMM || tl[t].kind != K_GEMM))
+            throw std::runtime_error("block written by more than one non-accumulating op");
+        if (t < 0) {
+            t = (int32_t)tl.size();
+            T0 x;
+            x.kind = k;
+            x.out = o.res;
+            x.out2 = k == K_LU ? o.res2 : 0;
+            x.a = k == K_SUB ? o.src2 : (k == K_GEMM ? 0 : o.src);
+            x.b = k == K_SUB ? o.src : 0;
+            tl.push_back(std::move(x));
+            producer[o.res] = t;
+            if (k == K_LU) {
+                if (o.res2 <= 0 || producer[o.res2] >= 0) throw std::runtime_error("bad LU result pair");
+                producer[o.res2] = t;
+            }
         }
-        t = g.ntasks++;
-        g.kind.push_back(k);
-        g.parts.push_back(k == K_GEMM ? (uint8_t)gemm_parts : 1);
-        g.out.push_back(o.res);
-        g.out2.push_back(k == K_LU ? o.res2 : 0);
-        if (k == K_SUB) { g.a.push_back(o.src2); g.b.push_back(o.src); }
-        else if (k == K_GEMM) { g.a.push_back(0); g.b.push_back(0); }
-        else { g.a.push_back(o.src); g.b.push_back(0); }
-        producer[o.res] = t;
-        first_write[o.res] = i;
-        if (k == K_LU) {
-            if (o.res2 <= 0 || producer[o.res2] >= 0) throw std::runtime_error("bad LU result pair");
-            producer[o.res2] = t;
-            first_write[o.res2] = i;
+        if (k == K_GEMM) {
+            if (o.src <= 0 || o.src2 <= 0) throw std::runtime_error("mul with absent operand");
+            tl[t].pa.push_back(o.src);
+            tl[t].pb.push_back(o.op == OP_MULNEG ? -o.src2 : o.src2);
         }
-        op_task[i] = t;
     }
-    // pass 2: GEMM operand pairs in op order
-    std::vector<int32_t> npairs(g.ntasks, 0);
-    for (int64_t i = 0; i < nops; i++)
-        if (g.kind[op_task[i]] == K_GEMM) npairs[op_task[i]]++;
+    // fuse  S = D - X  with  X = GEMM (X read only by S, not an output)
+    std::vector<char> is_out(storage_count, 0);
+    for (int32_t id : outputs) {
+        check_id(id);
+        is_out[id] = 1;
+    }
+    int64_t fused = 0;
+    if (fuse_subs) {
+        for (size_t s = 0; s < tl.size(); s++) {
+            T0& S = tl[s];
+            if (S.kind != K_SUB || S.b <= 0) continue;
+            const int32_t x = S.b;
+            const int32_t g = producer[x];
+            if (g < 0 || tl[g].kind != K_GEMM || tl[g].a != 0 || readers[x] != 1 || is_out[x]) continue;
+            T0& G = tl[g];
+            for (auto& v : G.pb) v = -v;
+            G.a = S.a;  // initial tile D (0: none)
+            producer[x] = -1;
+            G.out = S.out;
+            producer[S.out] = g;
+            S.dead = true;
+            fused++;
+        }
+    }
+    // renumber live tasks
+    std::vector<int32_t> newid(tl.size(), -1);
+    TaskGraph g;
+    g.storage_count = storage_count;
+    g.fused_subs = fused;
+    for (size_t t = 0; t < tl.size(); t++)
+        if (!tl[t].dead) newid[t] = g.ntasks++;
     g.pair_ptr.assign(g.ntasks + 1, 0);
-    for (int32_t t = 0; t < g.ntasks; t++) g.pair_ptr[t + 1] = g.pair_ptr[t] + npairs[t];
-    g.pair_a.resize(g.pair_ptr[g.ntasks]);
-    g.pair_b.resize(g.pair_ptr[g.ntasks]);
-    std::vector<int32_t> fill(g.pair_ptr.begin(), g.pair_ptr.end() - 1);
-    for (int64_t i = 0; i < nops; i++) {
-        const Op& o = ops[i];
-        int32_t t = op_task[i];
-        if (g.kind[t] != K_GEMM) continue;
-        if (o.src <= 0 || o.src2 <= 0) throw std::runtime_error("mul with absent operand");
-        int32_t p = fill[t]++;
-        g.pair_a[p] = o.src;
-        g.pair_b[p] = o.op == OP_MULNEG ? -o.src2 : o.src2;
+    for (size_t t = 0; t < tl.size(); t++) {
+        if (tl[t].dead) continue;
+        const T0& x = tl[t];
+        g.kind.push_back(x.kind);
+        g.parts.push_back(x.kind == K_GEMM ? (uint8_t)gemm_parts : 1);
+        g.out.push_back(x.out);
+        g.out2.push_back(x.out2);
+        g.a.push_back(x.a);
+        g.b.push_back(x.b);
+        g.pair_a.insert(g.pair_a.end(), x.pa.begin(), x.pa.end());
+        g.pair_b.insert(g.pair_b.end(), x.pb.begin(), x.pb.end());
+        g.pair_ptr[newid[t] + 1] = (int32_t)g.pair_a.size();
     }
-    g.gemm_pairs = g.pair_ptr[g.ntasks];
-    // pass 3: dependencies (read-after-write on produced blocks)
+    for (int32_t b = 0; b < storage_count; b++)
+        if (producer[b] >= 0) producer[b] = newid[producer[b]];
+    g.gemm_pairs = (int64_t)g.pair_a.size();
+    // dependencies from each task's sources
     std::vector<std::vector<int32_t>> preds(g.ntasks);
-    for (int64_t i = 0; i < nops; i++) {
-        const Op& o = ops[i];
-        int32_t t = op_task[i];
-        for (int32_t s : {o.src, o.src2}) {
-            if (s <= 0) continue;
-            if (s <= n_input) continue;
-            int32_t pt = producer[s];
-            if (pt < 0) throw std::runtime_error("read of a block that no op produces");
-            if (first_write[s] > i) throw std::runtime_error("block read before it is written");
-            if (pt == t) throw std::runtime_error("task reads its own result");
-            preds[t].push_back(pt);
+    auto dep_on = [&](int32_t t, int32_t src) {
+        if (src <= 0 || src <= n_input) return;
+        const int32_t pt = producer[src];
+        if (pt < 0) throw std::runtime_error("read of a block that no op produces");
+        if (pt == t) throw std::runtime_error("task reads its own result");
+        preds[t].push_back(pt);
+    };
+    for (int32_t t = 0; t < g.ntasks; t++) {
+        dep_on(t, g.a[t]);
+        if (g.kind[t] == K_SUB) dep_on(t, g.b[t]);
+        for (int32_t p = g.pair_ptr[t]; p < g.pair_ptr[t + 1]; p++) {
+            dep_on(t, g.pair_a[p]);
+            dep_on(t, g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]);
         }
     }
     g.ndep.assign(g.ntasks, 0);
@@ -104,19 +143,27 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
     std::vector<int32_t> sf(g.succ_ptr.begin(), g.succ_ptr.end() - 1);
     for (int32_t t = 0; t < g.ntasks; t++)
         for (int32_t q : preds[t]) g.succ[sf[q]++] = t;
-    // levels: tasks are created in op order, and producers precede readers
+    // topological order (Kahn); levels = longest path from a source
+    std::vector<int32_t> indeg(g.ndep), order;
+    order.reserve(g.ntasks);
+    for (int32_t t = 0; t < g.ntasks; t++)
+        if (indeg[t] == 0) order.push_back(t);
     g.level.assign(g.ntasks, 0);
-    for (int32_t t = 0; t < g.ntasks; t++) {
-        int32_t lv = 0;
-        for (int32_t q : preds[t]) lv = std::max(lv, g.level[q] + 1);
-        g.level[t] = lv;
-        g.nlevels = std::max(g.nlevels, lv + 1);
+    for (size_t h = 0; h < order.size(); h++) {
+        const int32_t t = order[h];
+        for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++) {
+            const int32_t s = g.succ[k];
+            g.level[s] = std::max(g.level[s], g.level[t] + 1);
+            if (--indeg[s] == 0) order.push_back(s);
+        }
     }
-    // longest path to a sink, for the initial ready order
-    std::vector<int32_t> height(g.ntasks, 0);
-    for (int32_t t = g.ntasks - 1; t >= 0; t--)
-        for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++)
-            height[t] = std::max(height[t], height[g.succ[k]] + 1);
+    if ((int32_t)order.size() != g.ntasks) throw std::runtime_error("cycle in the op DAG");
+    for (int32_t t = 0; t < g.ntasks; t++) g.nlevels = std::max(g.nlevels, g.level[t] + 1);
+    g.prio.assign(g.ntasks, 0);
+    for (int32_t h = g.ntasks - 1; h >= 0; h--) {
+        const int32_t t = order[h];
+        for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++) g.prio[t] = std::max(g.prio[t], g.prio[g.succ[k]] + 1);
+    }
     g.level_ptr.assign(g.nlevels + 1, 0);
     for (int32_t t = 0; t < g.ntasks; t++) g.level_ptr[g.level[t] + 1] += g.parts[t];
     for (int32_t l = 0; l < g.nlevels; l++) g.level_ptr[l + 1] += g.level_ptr[l];
@@ -127,12 +174,43 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
     std::vector<int32_t> roots;
     for (int32_t t = 0; t < g.ntasks; t++)
         if (g.ndep[t] == 0) roots.push_back(t);
-    std::stable_sort(roots.begin(), roots.end(), [&](int32_t x, int32_t y) { return height[x] > height[y]; });
+    std::stable_sort(roots.begin(), roots.end(), [&](int32_t x, int32_t y) { return g.prio[x] > g.prio[y]; });
     for (int32_t t : roots)
         for (int p = 0; p < g.parts[t]; p++) g.ready_items.push_back((t << 2) | p);
-    g.total_items = 0;
-    for (int32_t t = 0; t < g.ntasks; t++) { g.total_items += g.parts[t]; g.count[g.kind[t]]++; }
+    for (int32_t t = 0; t < g.ntasks; t++) {
+        g.total_items += g.parts[t];
+        g.count[g.kind[t]]++;
+    }
     return g;
+}
+
+void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+                       const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv) {
+    std::unordered_map<int32_t, int32_t> have_l, have_u;
+    for (const Op& o : ops) {
+        if (o.op == OP_LOWERINV) have_l[o.src] = o.res;
+        if (o.op == OP_UPPERINV) have_u[o.src] = o.res;
+    }
+    linv.assign(block_rows, 0);
+    uinv.assign(block_rows, 0);
+    int32_t seq = ops.empty() ? 0 : ops.back().seq;
+    int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    for (int side = 0; side < 2; side++) {
+        const std::vector<Leaf>& lv = side == 0 ? L : U;
+        auto& have = side == 0 ? have_l : have_u;
+        auto& dst = side == 0 ? linv : uinv;
+        for (const Leaf& lf : lv) {
+            if (lf.bi != lf.bj) continue;
+            auto it = have.find(lf.id);
+            if (it != have.end()) {
+                dst[lf.bi] = it->second;
+                continue;
+            }
+            const int32_t id = storage_count++;
+            ops.push_back({side == 0 ? OP_LOWERINV : OP_UPPERINV, lf.id, 0, id, 0, stage, ++seq, 0});
+            dst[lf.bi] = id;
+        }
+    }
 }
 
 }  // namespace sog

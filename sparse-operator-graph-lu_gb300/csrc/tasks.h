@@ -3,11 +3,16 @@
 // The reference executes its DAG stage by stage with a barrier per stage and
 // serialises all writers of one block in one thread (BlockPlanner.cpp:397-592).
 // Here every block is produced by exactly one task:
-//   GEMM : C = sum_k (+/-) A_k * B_k over all mul/mulneg ops writing C
+//   GEMM : C = init + sum_k (+/-) A_k * B_k over all mul/mulneg ops writing C
 //   LU   : (L, U) = lu(A)            LINV : Y = L^-1      UINV : Y = U^-1
 //   SUB  : R = A2 - A1 (either side may be absent: copy / negate)
 // and a task depends only on the tasks producing the blocks it reads, so a
 // persistent kernel can run any ready task without stage barriers.
+//
+// A Schur-complement update S = D - (sum of products) arrives from the planner
+// as a product into a temporary block followed by a sub (BlockPlanner.cpp:
+// 921-923); when the temporary has no other reader the two are fused into one
+// GEMM task with initial tile D and negated products.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -23,24 +28,34 @@ struct TaskGraph {
     int32_t ntasks = 0;
     int32_t storage_count = 0;
     std::vector<uint8_t> kind, parts;
-    std::vector<int32_t> out, out2, a, b;      // block ids (SUB: a = minuend src2, b = subtrahend src)
+    std::vector<int32_t> out, out2, a, b;      // block ids (see kernels.h DevTasks)
     std::vector<int32_t> pair_ptr;             // ntasks+1; GEMM operand pairs
     std::vector<int32_t> pair_a, pair_b;       // pair_b < 0: subtract A*B(|pair_b|)
     std::vector<int32_t> succ_ptr, succ;       // successor tasks
     std::vector<int32_t> ndep;                 // predecessor task count
     std::vector<int32_t> level;                // dependency level, 0-based
+    std::vector<int32_t> prio;                 // longest path (tasks) to a sink
     std::vector<int32_t> level_ptr;            // nlevels+1 offsets into level_items
     std::vector<int32_t> level_items;          // (task << 2 | part), grouped by level
     std::vector<int32_t> ready_items;          // initially ready items, longest path first
     int32_t nlevels = 0;
     int64_t total_items = 0;                   // sum of parts
     int64_t gemm_pairs = 0;
+    int64_t fused_subs = 0;
     int64_t count[5] = {0, 0, 0, 0, 0};
 };
 
-// Throws std::runtime_error if the DAG has a block written by ops of
-// different kinds, a read of a block nobody produces (and not an input), or
-// an id out of range. gemm_parts: parts per GEMM task (1 or 4).
-TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input, int gemm_parts);
+// outputs: block ids that must be materialised (the L/U leaves). Throws
+// std::runtime_error on a block written by ops of different kinds, a read of a
+// block nobody produces (and not an input), an id out of range, or a cycle.
+// gemm_parts: parts per GEMM task (1 or 4).
+TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input,
+                      const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs = true);
+
+// Appends, for every diagonal L (U) block without one already in the DAG, a
+// lowerInv (upperInv) op; returns per block row the id of the inverse of the
+// diagonal L and U blocks. storage_count grows by the number of new blocks.
+void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+                       const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv);
 
 }  // namespace sog

@@ -111,3 +111,29 @@ def test_disconnected_and_isolated_nodes(sg):
     p = sg.Plan(n, np.array(r), np.array(c), np.array(v))
     perm = p.export()[0]
     assert sorted(perm.tolist()) == list(range(n))
+
+
+@pytest.mark.parametrize("name", ["lap2d_32", "var3d_16", "band_3000", "cd_17"])
+def test_task_graph(sg, wl, name):
+    """Device task graph (host-built): every op becomes part of exactly one
+    task, each Schur sub is fused into its product, levels <= the reference's
+    stages, acyclic (the builder checks)."""
+    s = golden_cases(wl)[name]()
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    info = p.info_dict()
+    tg = p.task_graph_info(gemm_split=1)
+    ops = info["ops"]
+    assert tg["lu"] == ops.get("lu", 0)
+    assert tg["pairs"] == ops.get("mul", 0) + ops.get("mulneg", 0)
+    assert tg["sub"] + tg["fused_subs"] == ops.get("sub", 0)
+    assert tg["linv"] + tg["uinv"] == ops.get("lowerInv", 0) + ops.get("upperInv", 0) + tg["added_inverses"]
+    assert tg["levels"] <= info["stages"]
+    assert tg["critical_path"] == tg["levels"]
+    tg4 = p.task_graph_info(gemm_split=4)
+    assert tg4["items"] == tg["items"] + 3 * tg["gemm"]
+
+
+def test_task_graph_48cube(sg, wl):
+    s = wl.varcoef3d(48)
+    tg = sg.Plan(s.n, s.rows, s.cols, s.vals).task_graph_info()
+    assert tg["fused_subs"] > 40000 and tg["levels"] < 11904
