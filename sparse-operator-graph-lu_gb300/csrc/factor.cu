@@ -28,13 +28,14 @@ constexpr unsigned FULL = 0xffffffffu;
 // smem footprints (elements of T)
 constexpr int F64_STAGE = 32 * 68 + 64 * 40;  // A quadrant rows + B quadrant columns
 constexpr int F32_STAGE = 64 * 68 + 64 * 72;  // full A and B tiles
-constexpr int INV_ELEMS = 64 * LD + 2 * 64;   // source tile + double-buffered row
-constexpr int LU_ELEMS = 2 * 64 + 2 * 64;     // double-buffered row + pivots + reciprocals
+constexpr int INV_ELEMS = 64 * LD + 16 * 64 + 64;  // source tile + 2 x 8 finished rows + reciprocals
+constexpr int LU_ELEMS = 32 * 64 + 3 * 64;          // 2 x 8 pivot rows of A and of L^-1 + pivot data
 
 template <typename T>
 constexpr int smem_elems() {
     constexpr int g = 2 * (sizeof(T) == 8 ? F64_STAGE : F32_STAGE);
-    return g > INV_ELEMS ? g : INV_ELEMS;
+    constexpr int t = INV_ELEMS > LU_ELEMS ? INV_ELEMS : LU_ELEMS;
+    return g > t ? g : t;
 }
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -238,61 +239,77 @@ __device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int
 // its entry into l_ik. Pivots with |u_kk| < 1e-9 are clamped to +-1e-9 (sign
 // kept, 0 -> +1e-9) as ludcmpSimple does (MatrixStdDouble.cpp:2751-2761); the
 // pivot test, clamp and growth ratio are evaluated in FP64 in both precisions.
-template <typename T>
+//
+// With WITH_LINV the elimination runs on the augmented block [A | I]: the same
+// multipliers applied to the identity leave L^-1 in the right half, so the
+// inverse of the unit lower factor (lowerInv of this LU's L, which the
+// recursion always needs next) comes out of the same 64 steps.
+__device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double fast_rcp(double x) { return __drcp_rn(x); }
+
+template <typename T, bool WITH_LINV>
 __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
-    T* rowbuf = sm;          // [2][64]
-    T* piv = sm + 128;       // [64] clamped pivots
-    T* rpiv = sm + 192;      // [64] their reciprocals
-    __shared__ int s_clamped;
-    __shared__ unsigned long long s_minp;
+    T* rowbuf = sm;          // [2][8][64] scaled pivot rows of A for the current block
+    T* wbuf = sm + 1024;     // [2][8][64] rows of the running L^-1 for the current block
+    T* piv = sm + 2048;      // [64] clamped pivots
+    T* rpiv = piv + 64;      // [64] their reciprocals
+    T* raw = piv + 128;      // [64] pivots before the clamp
     __shared__ float s_maxa, s_maxu;
-    const int tid = threadIdx.x, lane = tid & 31, r = tid >> 2, q = tid & 3;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, r = tid >> 2, q = tid & 3;
     if (tid == 0) {
-        s_clamped = 0;
-        s_minp = dbits(1e300);
         s_maxa = 0.f;
         s_maxu = 0.f;
     }
     const T* A = tiles + (size_t)tk.a[task] * 4096 + r * 64 + q;
-    T a[16];
+    T a[16], w[16];
     float ma = 0.f;
 #pragma unroll
     for (int m = 0; m < 16; m++) {
         a[m] = __ldcg(A + 4 * m);
         ma = fmaxf(ma, fabsf((float)a[m]));
+        if (WITH_LINV) w[m] = (q + 4 * m == r) ? T(1) : T(0);
     }
     __syncthreads();
+    (void)warp;
+    // One pivot per step: the four owners of row k publish it (scaled by the
+    // pivot reciprocal) and their row of L^-1; after one CTA barrier every
+    // lower row applies the rank-1 update. Buffers alternate by step so one
+    // barrier per step suffices. (A variant factoring 8-row panels inside one
+    // warp with 8 CTA barriers measured slower on GB300: the single-warp panel
+    // serialises more than the barriers cost.)
 #pragma unroll
     for (int k = 0; k < 64; k++) {
         const int km = k >> 2, kq = k & 3;
-        T* rb = rowbuf + (k & 1) * 64;
+        T* ub = rowbuf + (k & 1) * 64;
+        T* wb = wbuf + (k & 1) * 64;
         const T aik = __shfl_sync(FULL, a[km], (lane & ~3) | kq);  // a[r][k] for this thread's row
         if (r == k) {
-            double pd = (double)aik;
-            const bool cl = (pd < 1e-9 && pd > -1e-9);
-            if (cl) pd = pd < 0 ? -1e-9 : 1e-9;
-            const T p = (T)pd;
-            const T rp = T(1) / p;
+            // clamp |u_kk| < 1e-9 to +-1e-9 (0 -> +1e-9), in the working precision
+            const T tiny = T(1e-9);
+            const T p = (aik < tiny && aik > -tiny) ? (aik < T(0) ? -tiny : tiny) : aik;
+            const T rp = fast_rcp(p);
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int c = q + 4 * m;
-                if (c > k) rb[c] = a[m] * rp;
+                if (c > k) ub[c] = a[m] * rp;
+                if (WITH_LINV && c <= k) wb[c] = w[m];
             }
             if (q == 0) {
                 piv[k] = p;
                 rpiv[k] = rp;
-                if (cl) atomicAdd(&s_clamped, 1);
-                atomicMin(&s_minp, dbits(fabs((double)aik)));
+                raw[k] = aik;
             }
         }
         __syncthreads();
         if (r > k) {
+            const T lik = aik * rpiv[k];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int c = q + 4 * m;
-                if (c > k) a[m] -= aik * rb[c];
+                if (c > k) a[m] -= aik * ub[c];
+                if (WITH_LINV && c <= k) w[m] -= lik * wb[c];
             }
-            if (q == kq) a[km] = aik * rpiv[k];
+            if (q == kq) a[km] = lik;
         }
     }
     T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
@@ -306,6 +323,11 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         U[4 * m] = u;
         mu = fmaxf(mu, fabsf((float)u));
     }
+    if (WITH_LINV) {
+        T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+#pragma unroll
+        for (int m = 0; m < 16; m++) W[4 * m] = w[m];
+    }
     for (int o = 16; o > 0; o >>= 1) {
         ma = fmaxf(ma, __shfl_xor_sync(FULL, ma, o));
         mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
@@ -315,10 +337,24 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
     }
     __syncthreads();
-    if (tid == 0) {
-        if (s_clamped) atomicAdd(&tk.status->clamped, s_clamped);
-        atomicMin(&tk.status->min_pivot_bits, s_minp);
-        if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
+    // pivot statistics in FP64, off the elimination's critical chain
+    if (tid < 32) {
+        double mn = 1e300;
+        int cl = 0;
+        for (int k = lane; k < 64; k += 32) {
+            const double v = fabs((double)raw[k]);
+            mn = fmin(mn, v);
+            cl += v < 1e-9;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
+            cl += __shfl_xor_sync(FULL, cl, o);
+        }
+        if (lane == 0) {
+            if (cl) atomicAdd(&tk.status->clamped, cl);
+            atomicMin(&tk.status->min_pivot_bits, dbits(mn));
+            if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
+        }
     }
 }
 
@@ -332,19 +368,24 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
 template <typename T, bool LOWER>
 __device__ void inv_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
     T* M = sm;                  // source [64][LD]
-    T* rowbuf = sm + 64 * LD;   // [2][64]
-    const int tid = threadIdx.x, r = tid >> 2, q = tid & 3;
+    T* rowbuf = sm + 64 * LD;   // [2][8][64] finished rows of Y for the current block
+    T* rdiag = rowbuf + 1024;   // [64] reciprocals of the diagonal
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, r = tid >> 2, q = tid & 3;
     load_tile(tiles + (size_t)tk.a[task] * 4096, M);
     T w[16];
 #pragma unroll
     for (int m = 0; m < 16; m++) w[m] = (q + 4 * m == r) ? T(1) : T(0);
     __syncthreads();
+    if (tid < 64) rdiag[tid] = T(1) / M[tid * LD + tid];
+    __syncthreads();
+    (void)lane;
+    (void)warp;
 #pragma unroll
     for (int kk = 0; kk < 64; kk++) {
         const int k = LOWER ? kk : 63 - kk;
         T* rb = rowbuf + (kk & 1) * 64;
         if (r == k) {
-            const T d = T(1) / M[k * LD + k];
+            const T d = rdiag[k];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 w[m] *= d;
@@ -398,7 +439,10 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                 gemm_f32_full(tk, tiles, task, sm);
             }
             break;
-        case K_LU: lu_task<T>(tk, tiles, task, sm); break;
+        case K_LU:
+            if (tk.b[task] > 0) lu_task<T, true>(tk, tiles, task, sm);
+            else lu_task<T, false>(tk, tiles, task, sm);
+            break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;
         case K_UINV: inv_task<T, false>(tk, tiles, task, sm); break;
         case K_SUB: sub_task<T>(tk, tiles, task); break;
@@ -406,11 +450,11 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
     }
 }
 
-// Append `cnt` items of task t (parts from..parts-1) to the ready queue.
-__device__ __forceinline__ void push_task(const DevTasks& tk, int t, int from) {
-    const int np = tk.parts[t];
-    const int pos = atomicAdd(tk.tail, np - from);
-    for (int p = from; p < np; p++) atomicExch(&tk.queue[pos + p - from], (t << 2) | p);
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Called by warp 0 once the CTA's writes for an item are complete. The last
@@ -426,7 +470,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
         last = (tk.parts[task] == 1) || (atomicSub(&tk.parts_left[task], 1) == 1);
     }
     last = __shfl_sync(FULL, last, 0);
-    int keep = -1, keep_prio = -1;
+    int keep = -1, keep_prio = -1;  // warp-uniform
     if (last) {
         const int s0 = tk.succ_ptr[task], s1 = tk.succ_ptr[task + 1];
         for (int base = s0; base < s1; base += 32) {
@@ -437,31 +481,52 @@ __device__ int complete_item(const DevTasks& tk, int task) {
                 if (atomicSub(&tk.dep[s], 1) != 1) s = -1;
                 else if (tk.trace) tk.trace[4 * (size_t)s] = globaltimer_ns();
             }
-            unsigned m = __ballot_sync(FULL, s >= 0);
-            if (m) __threadfence();
-            while (m) {
-                const int l = __ffs(m) - 1;
-                m &= m - 1;
-                const int t = __shfl_sync(FULL, s, l);
+            if (!__any_sync(FULL, s >= 0)) continue;
+            // the highest-priority newly ready task of this batch (ties: lowest lane)
+            int best = s >= 0 ? tk.prio[s] : -1, bl = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const int ob = __shfl_xor_sync(FULL, best, o), ol = __shfl_xor_sync(FULL, bl, o);
+                if (ob > best || (ob == best && ol < bl)) { best = ob; bl = ol; }
+            }
+            if (best > keep_prio) {  // keep it; the lane that found it queues the previous keep instead
+                const int t = __shfl_sync(FULL, s, bl);
+                if (lane == bl) s = keep;
+                keep = t;
+                keep_prio = best;
+            }
+            // queue the rest: one tail reservation for the whole batch, then release stores
+            const int np = s >= 0 ? tk.parts[s] : 0;
+            int incl = np;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(FULL, incl, 31);
+            if (total) {
+                int base_pos = 0;
                 if (lane == 0) {
-                    const int pr = tk.prio[t];
-                    if (pr > keep_prio) {
-                        if (keep >= 0) push_task(tk, keep, 0);
-                        keep = t;
-                        keep_prio = pr;
-                    } else {
-                        push_task(tk, t, 0);
-                    }
+                    __threadfence();
+                    base_pos = atomicAdd(tk.tail, total);
                 }
+                base_pos = __shfl_sync(FULL, base_pos, 0) + incl - np;
+                for (int p = 0; p < np; p++) st_release(&tk.queue[base_pos + p], (s << 4) | p);
             }
         }
-        if (lane == 0 && keep >= 0 && tk.parts[keep] > 1) push_task(tk, keep, 1);
+        if (keep >= 0) {
+            __threadfence();  // the kept task's inputs, released by their producers, are visible here
+            const int np = tk.parts[keep];
+            if (np > 1) {
+                int base_pos = 0;
+                if (lane == 0) base_pos = atomicAdd(tk.tail, np - 1);
+                base_pos = __shfl_sync(FULL, base_pos, 0);
+                if (lane > 0 && lane < np) st_release(&tk.queue[base_pos + lane - 1], (keep << 4) | lane);
+            }
+        }
     }
-    if (lane == 0) {
-        __threadfence();
-        atomicAdd(tk.done, 1);
-    }
-    return __shfl_sync(FULL, keep >= 0 ? (keep << 2) : -1, 0);
+    if (lane == 0) red_release_add(tk.done, 1);
+    return keep >= 0 ? (keep << 4) : -1;
 }
 
 // Each CTA runs the item it kept from its last completion, else claims the
@@ -494,7 +559,7 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
                         }
                         __nanosleep(64);
                     }
-                    if (item >= 0 && (item >> 2) >= tk.ntasks) {
+                    if (item >= 0 && (item >> 4) >= tk.ntasks) {
                         atomicOr(&tk.status->flags, ST_BAD_ITEM);
                         item = -1;
                     }
@@ -503,7 +568,7 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
             if (item >= 0 && tk.trace) {
                 unsigned smid;
                 asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-                unsigned long long* tr = tk.trace + 4 * (size_t)(item >> 2);
+                unsigned long long* tr = tk.trace + 4 * (size_t)(item >> 4);
                 atomicMax(tr + 1, ~globaltimer_ns());  // start = min over parts, stored inverted
                 tr[3] = smid;
             }
@@ -513,11 +578,11 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T>(tk, tiles, item >> 2, item & 3, sm);
+        run_item<T>(tk, tiles, item >> 4, item & 15, sm);
         __syncthreads();
         if (threadIdx.x < 32) {
-            if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 2) + 2, globaltimer_ns());
-            const int keep = complete_item(tk, item >> 2);
+            if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
+            const int keep = complete_item(tk, item >> 4);
             if (threadIdx.x == 0) {
                 s_next = keep;
                 // a timeout anywhere stops every CTA at its next claim
@@ -534,7 +599,7 @@ __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles,
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const int item = items[blockIdx.x];
-    run_item<T>(tk, tiles, item >> 2, item & 3, sm);
+    run_item<T>(tk, tiles, item >> 4, item & 15, sm);
 }
 
 template <typename T>

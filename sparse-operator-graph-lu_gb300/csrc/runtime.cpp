@@ -922,6 +922,7 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
         counts[9] = g.fused_subs;
         counts[10] = storage2 - p.storage_count;
         counts[11] = g.ntasks ? *std::max_element(g.prio.begin(), g.prio.end()) + 1 : 0;
+        counts[12] = g.fused_inverses;
     } catch (const std::exception& e) {
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
     }

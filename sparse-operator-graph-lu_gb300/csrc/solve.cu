@@ -94,9 +94,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     }
                     __nanosleep(32);
                 }
-                __threadfence();
             }
-            __syncwarp();
+            __syncwarp();  // lane 0's acquire orders the warp's reads of row j after it
             if (*(volatile int*)&s_stop) {
                 stop = true;
                 break;
@@ -153,9 +152,9 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
             }
         }
-        __threadfence();
         __syncthreads();
         if (tid == 0) {
+            __threadfence();  // the row written by all threads (ordered by the barrier) before the flag
             st_release(s.flags + i, epoch);
             if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
         }

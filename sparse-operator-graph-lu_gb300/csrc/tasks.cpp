@@ -87,11 +87,25 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
             fused++;
         }
     }
+    // fuse  Y = L^-1  into the LU task producing L: the LU sweep on [A | I]
+    // yields L^-1 with the same multipliers (LU task field b = Y)
+    int64_t fused_inv = 0;
+    for (size_t s = 0; s < tl.size(); s++) {
+        T0& X = tl[s];
+        if (X.dead || X.kind != K_LINV || X.a <= 0) continue;
+        const int32_t t = producer[X.a];
+        if (t < 0 || tl[t].kind != K_LU || tl[t].out != X.a || tl[t].b != 0) continue;
+        tl[t].b = X.out;
+        producer[X.out] = t;
+        X.dead = true;
+        fused_inv++;
+    }
     // renumber live tasks
     std::vector<int32_t> newid(tl.size(), -1);
     TaskGraph g;
     g.storage_count = storage_count;
     g.fused_subs = fused;
+    g.fused_inverses = fused_inv;
     for (size_t t = 0; t < tl.size(); t++)
         if (!tl[t].dead) newid[t] = g.ntasks++;
     g.pair_ptr.assign(g.ntasks + 1, 0);
@@ -170,13 +184,13 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
     g.level_items.resize(g.level_ptr[g.nlevels]);
     std::vector<int32_t> lf(g.level_ptr.begin(), g.level_ptr.end() - 1);
     for (int32_t t = 0; t < g.ntasks; t++)
-        for (int p = 0; p < g.parts[t]; p++) g.level_items[lf[g.level[t]]++] = (t << 2) | p;
+        for (int p = 0; p < g.parts[t]; p++) g.level_items[lf[g.level[t]]++] = (t << 4) | p;
     std::vector<int32_t> roots;
     for (int32_t t = 0; t < g.ntasks; t++)
         if (g.ndep[t] == 0) roots.push_back(t);
     std::stable_sort(roots.begin(), roots.end(), [&](int32_t x, int32_t y) { return g.prio[x] > g.prio[y]; });
     for (int32_t t : roots)
-        for (int p = 0; p < g.parts[t]; p++) g.ready_items.push_back((t << 2) | p);
+        for (int p = 0; p < g.parts[t]; p++) g.ready_items.push_back((t << 4) | p);
     for (int32_t t = 0; t < g.ntasks; t++) {
         g.total_items += g.parts[t];
         g.count[g.kind[t]]++;

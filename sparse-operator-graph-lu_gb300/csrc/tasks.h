@@ -42,6 +42,7 @@ struct TaskGraph {
     int64_t total_items = 0;                   // sum of parts
     int64_t gemm_pairs = 0;
     int64_t fused_subs = 0;
+    int64_t fused_inverses = 0;  // lowerInv tasks folded into their LU task
     int64_t count[5] = {0, 0, 0, 0, 0};
 };
 

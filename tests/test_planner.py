@@ -126,7 +126,9 @@ def test_task_graph(sg, wl, name):
     assert tg["lu"] == ops.get("lu", 0)
     assert tg["pairs"] == ops.get("mul", 0) + ops.get("mulneg", 0)
     assert tg["sub"] + tg["fused_subs"] == ops.get("sub", 0)
-    assert tg["linv"] + tg["uinv"] == ops.get("lowerInv", 0) + ops.get("upperInv", 0) + tg["added_inverses"]
+    assert tg["linv"] + tg["uinv"] + tg["fused_inverses"] == \
+        ops.get("lowerInv", 0) + ops.get("upperInv", 0) + tg["added_inverses"]
+    assert 0 < tg["fused_inverses"] <= tg["lu"]
     assert tg["levels"] <= info["stages"]
     assert tg["critical_path"] == tg["levels"]
     tg4 = p.task_graph_info(gemm_split=4)
