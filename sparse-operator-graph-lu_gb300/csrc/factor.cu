@@ -16,6 +16,7 @@
 
 #include "kernels.h"
 #include "tasks.h"
+#include "tc_gemm.cuh"
 
 namespace sog {
 
@@ -33,7 +34,8 @@ constexpr int LU_ELEMS = 32 * 64 + 3 * 64;          // 2 x 8 pivot rows of A and
 
 template <typename T>
 constexpr int smem_elems() {
-    constexpr int g = 2 * (sizeof(T) == 8 ? F64_STAGE : F32_STAGE);
+    // FP64: double-buffered DMMA stages; FP32: the tcgen05 operand area
+    constexpr int g = sizeof(T) == 8 ? 2 * F64_STAGE : tc::SMEM_BYTES / 4;
     constexpr int t = INV_ELEMS > LU_ELEMS ? INV_ELEMS : LU_ELEMS;
     return g > t ? g : t;
 }
@@ -422,8 +424,104 @@ __device__ void sub_task(const DevTasks& tk, T* __restrict__ tiles, int task) {
     }
 }
 
+// C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh). The
+// next pair's operands load from L2 into registers while the current pair's
+// MMAs run; `phase` is this CTA's mbarrier parity, carried across tasks.
+__device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm, tc::State& st,
+                            uint32_t& phase) {
+    unsigned char* smb = reinterpret_cast<unsigned char*>(sm);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
+    const unsigned long long lim = tk.wait_limit_ns;
+    float4 a4[4], b4[4];
+    auto operands = [&](int p) {
+        const int pbs = tk.pair_b[p];
+        tc::load_pair(tiles + (size_t)tk.pair_a[p] * 4096, tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096, a4, b4);
+    };
+    const int n = p1 - p0;
+    if (n > 0) operands(p0);
+    for (int i = 0; i < n; i++) {
+        const int s = i & 1;
+        unsigned char* stg = smb + s * tc::STAGE_BYTES;
+        if (i >= 2) {  // the MMAs of pair i-2 read this stage
+            if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
+            phase ^= 1u << s;
+        }
+        tc::stage_pair(stg, a4, b4, tk.pair_b[p0 + i] < 0 ? -1.f : 1.f);
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            tc::issue_pair(stg, st.tmem, i == 0);
+            tc::mma_commit(&st.bar[s]);
+        }
+        if (i + 1 < n) operands(p0 + i + 1);
+    }
+    for (int i = n > 2 ? n - 2 : 0; i < n; i++) {  // the commits not yet waited for
+        const int s = i & 1;
+        if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
+        phase ^= 1u << s;
+    }
+    tc::fence_after_sync();
+    // epilogue: C = init + D[0:64] + D[64:128] (warps 2,3,6,7 hold the lower half)
+    float* X = sm;  // [64][65], the operand area is free once the MMAs completed
+    const int quad = warp & 3, colh = (warp >> 2) * 32;
+    float v[32];
+    if (p0 < p1 && quad >= 2) {
+        tc::tmem_ld32(st.tmem + ((uint32_t)(32 * quad) << 16) + colh, v);
+        const int row = 32 * quad + lane - 64;
+#pragma unroll
+        for (int i = 0; i < 32; i++) X[row * 65 + colh + i] = v[i];
+    }
+    __syncthreads();
+    if (quad < 2) {
+        const int row = 32 * quad + lane;
+        if (p0 < p1) {
+            tc::tmem_ld32(st.tmem + ((uint32_t)(32 * quad) << 16) + colh, v);
+#pragma unroll
+            for (int i = 0; i < 32; i++) v[i] += X[row * 65 + colh + i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 32; i++) v[i] = 0.f;
+        }
+        const int init = tk.a[task];
+        if (init > 0) {
+            const float4* I = reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + row * 64 + colh);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float4 u = __ldcg(I + i);
+                v[4 * i] += u.x; v[4 * i + 1] += u.y; v[4 * i + 2] += u.z; v[4 * i + 3] += u.w;
+            }
+        }
+        float4* C = reinterpret_cast<float4*>(tiles + (size_t)tk.out[task] * 4096 + row * 64 + colh);
+#pragma unroll
+        for (int i = 0; i < 8; i++) C[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+}
+
+// Per-CTA tensor-memory set-up / tear-down for the mixed path.
+__device__ __forceinline__ void tc_setup(tc::State& st) {
+    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&st.tmem);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < tc::STAGES; s++) tc::mbar_init(&st.bar[s], 1);
+        st.fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+__device__ __forceinline__ void tc_teardown(tc::State& st, const DevTasks& tk) {
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0 && st.fail) atomicOr(&tk.status->flags, ST_TIMEOUT);
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(st.tmem);
+}
+
 template <typename T>
-__device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task, int part, T* sm) {
+__device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task, int part, T* sm, tc::State& st,
+                                         uint32_t& phase) {
     switch (tk.kind[task]) {
         case K_GEMM:
             if constexpr (sizeof(T) == 8) {
@@ -436,7 +534,7 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                     }
                 }
             } else {
-                gemm_f32_full(tk, tiles, task, sm);
+                gemm_f32_tc(tk, tiles, task, sm, st, phase);
             }
             break;
         case K_LU:
@@ -537,6 +635,9 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item, s_next, s_stop;
+    __shared__ tc::State st;
+    uint32_t phase = 0;
+    if constexpr (sizeof(T) == 4) tc_setup(st);
     if (threadIdx.x == 0) s_next = -1;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -578,7 +679,7 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T>(tk, tiles, item >> 4, item & 15, sm);
+        run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
@@ -592,14 +693,19 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
         __syncthreads();
         if (s_stop) break;
     }
+    if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles, const int32_t* items) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
+    __shared__ tc::State st;
+    uint32_t phase = 0;
+    if constexpr (sizeof(T) == 4) tc_setup(st);
     const int item = items[blockIdx.x];
-    run_item<T>(tk, tiles, item >> 4, item & 15, sm);
+    run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+    if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 
 template <typename T>

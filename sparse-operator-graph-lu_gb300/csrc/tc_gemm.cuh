@@ -1,0 +1,206 @@
+// Split-precision TF32 64x64 tile product on the 5th-generation tensor cores
+// (tcgen05, sm_100a family incl. sm_103a), accumulator in tensor memory.
+//
+//   C = init + sum_p s_p A_p B_p      (A_p, B_p, C: 64x64 FP32, row-major in HBM)
+//
+// Each operand is split into a TF32 head (rounded to nearest) and the FP32
+// remainder, staged into shared memory in the canonical no-swizzle K-major
+// layout (core matrices of 8 rows x 16 bytes): A as the 128-row stack
+// [A_hi; A_lo], B transposed as B_hi^T and B_lo^T. Per K=8 step two M=128,
+// N=64 MMAs run against the same A stack:
+//   D += [A_hi; A_lo] * B_hi        D += [A_hi; A_lo] * B_lo
+// so D rows 0..63 accumulate A_hi (B_hi + B_lo) and rows 64..127 accumulate
+// A_lo (B_hi + B_lo); the epilogue adds the halves, giving hi*hi + hi*lo +
+// lo*hi (+ the negligible lo*lo). The tensor core reads the TF32 part of each
+// FP32 word, so the remainder enters truncated to TF32 (relative error 2^-22
+// of the element). Two shared-memory stages alternate: pair p+1 is staged
+// while pair p's MMAs run. One thread issues the MMAs and commits them to the
+// stage's mbarrier; every wait is bounded.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sog {
+namespace tc {
+
+constexpr int ROW_GROUP_BYTES = 8 * 64 * 4;                 // 8 rows x K=64 fp32 = 2048
+constexpr int A_BYTES = 128 / 8 * ROW_GROUP_BYTES;         // [A_hi; A_lo] = 32768
+constexpr int B_BYTES = 64 / 8 * ROW_GROUP_BYTES;          // 16384 per part
+constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;         // 65536
+constexpr int STAGES = 2;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES;           // 131072
+constexpr uint32_t TMEM_COLS = 64;
+
+// byte offset of element (row, k) in the K-major core-matrix layout:
+// 8-row groups at ROW_GROUP_BYTES, K-adjacent core matrices at 128 bytes
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k) {
+    return (uint32_t)((row >> 3) * ROW_GROUP_BYTES + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// 64-bit shared-memory matrix descriptor, no swizzle: start address, leading
+// byte offset (K-adjacent core matrices) and stride byte offset (8-row groups)
+// in 16-byte units, version 1 at bit 46, swizzle mode 0 at bits 61-63
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor for kind::tf32: D f32, A/B tf32, K-major A and B,
+// N = 64 (bits 17-22 hold N >> 3), M = 128 (bits 24-28 hold M >> 4)
+__host__ __device__ constexpr uint32_t idesc_tf32_m128_n64() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// TF32 head of x, rounded to nearest (ties away from zero) on the magnitude
+__device__ __forceinline__ float tf32_head(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// bounded wait for the mbarrier phase `parity` to complete; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) return false;
+    }
+}
+
+// TMEM allocation by one full warp; the address lands in *slot (shared)
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS) : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 32 consecutive fp32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Per-CTA state of the tensor-core product (static shared memory). phase
+// holds, per stage s, the parity of that stage's next mbarrier phase (bit s);
+// pending, per stage, whether a commit on it is not yet waited for.
+struct State {
+    uint64_t bar[STAGES];
+    uint32_t tmem;
+    int32_t fail;
+};
+
+// Thread -> chunk mapping: warp w owns the 8-row group 8w..8w+7; in chunk j,
+// lane l handles row 8w + (l & 7) and K-quad 4j + (l >> 3). Eight consecutive
+// lanes then fill one 128-byte core matrix (conflict-free 16-byte stores) and
+// the global reads cover whole sectors.
+__device__ __forceinline__ void chunk_of(int j, int& row, int& k) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    row = 8 * warp + (lane & 7);
+    k = 4 * (4 * j + (lane >> 3));
+}
+
+// Load this thread's share of one pair from global (L2; produced by other
+// SMs): 4 chunks of A (4 consecutive k of one row) and of B^T (4 consecutive
+// k of one column of B).
+__device__ __forceinline__ void load_pair(const float* A, const float* B, float4 (&a4)[4], float4 (&b4)[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        int row, k;
+        chunk_of(j, row, k);
+        a4[j] = __ldcg(reinterpret_cast<const float4*>(A + row * 64 + k));
+        b4[j] = make_float4(__ldcg(B + (k + 0) * 64 + row), __ldcg(B + (k + 1) * 64 + row),
+                            __ldcg(B + (k + 2) * 64 + row), __ldcg(B + (k + 3) * 64 + row));
+    }
+}
+
+__device__ __forceinline__ void split4(const float4& x, float sgn, float4& hi, float4& lo) {
+    hi.x = tf32_head(sgn * x.x); lo.x = sgn * x.x - hi.x;
+    hi.y = tf32_head(sgn * x.y); lo.y = sgn * x.y - hi.y;
+    hi.z = tf32_head(sgn * x.z); lo.z = sgn * x.z - hi.z;
+    hi.w = tf32_head(sgn * x.w); lo.w = sgn * x.w - hi.w;
+}
+
+// Stage one pair into a stage buffer: A (x sgn) as [A_hi; A_lo], B as B_hi^T, B_lo^T.
+__device__ __forceinline__ void stage_pair(unsigned char* st, const float4 (&a4)[4], const float4 (&b4)[4],
+                                           float sgn) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        int row, k;
+        chunk_of(j, row, k);
+        float4 hi, lo;
+        split4(a4[j], sgn, hi, lo);
+        *reinterpret_cast<float4*>(st + kmajor_off(row, k)) = hi;
+        *reinterpret_cast<float4*>(st + kmajor_off(64 + row, k)) = lo;
+        split4(b4[j], 1.f, hi, lo);
+        *reinterpret_cast<float4*>(st + A_BYTES + kmajor_off(row, k)) = hi;
+        *reinterpret_cast<float4*>(st + A_BYTES + B_BYTES + kmajor_off(row, k)) = lo;
+    }
+}
+
+// Issue the 16 MMAs of one staged pair (8 K-steps x 2).
+__device__ __forceinline__ void issue_pair(const unsigned char* st, uint32_t tmem, bool first) {
+    const uint32_t base = smem_u32(st);
+    constexpr uint32_t idesc = idesc_tf32_m128_n64();
+#pragma unroll
+    for (int ks = 0; ks < 8; ks++) {
+        const uint32_t koff = ks * 256;  // K = 8 tf32 = two core matrices of 128 bytes
+        const uint64_t a = smem_desc(base + koff, 128, ROW_GROUP_BYTES);
+        const uint64_t bh = smem_desc(base + A_BYTES + koff, 128, ROW_GROUP_BYTES);
+        const uint64_t bl = smem_desc(base + A_BYTES + B_BYTES + koff, 128, ROW_GROUP_BYTES);
+        mma_tf32(tmem, a, bh, idesc, (first && ks == 0) ? 0u : 1u);
+        mma_tf32(tmem, a, bl, idesc, 1u);
+    }
+}
+
+}  // namespace tc
+}  // namespace sog
