@@ -35,6 +35,20 @@ __device__ __forceinline__ void st_release(int* p, int v) {
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// 16-byte read-only vector load of consecutive T (factor tiles are written by
+// an earlier kernel, so the non-coherent path is safe here)
+template <typename T>
+struct Vec16 {
+    T v[16 / sizeof(T)];
+};
+template <typename T>
+__device__ __forceinline__ Vec16<T> ldg16(const T* p) {
+    const int4 r = __ldg(reinterpret_cast<const int4*>(p));
+    Vec16<T> o;
+    memcpy(&o, &r, 16);
+    return o;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -55,6 +69,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                                                       int epoch, int lower) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NV = 64 * NR;
+    constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte load
     T* part = reinterpret_cast<T*>(smem_raw);
     T* ybuf = part + 8 * NV;
     T* acc = ybuf + 8 * NV;
@@ -103,15 +118,17 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             const T* vj = vec + (size_t)j * 64 * ld + c0;
             for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
             __syncwarp();
-#pragma unroll 8
-            for (int c = 0; c < 64; c++) {
-                const T b0 = __ldg(B + c), b1 = __ldg(B + 64 + c);
+#pragma unroll 4
+            for (int c = 0; c < 64; c += VW) {
+                const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
 #pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    const T y = yw[c * NR + r];
-                    pa[r] += b0 * y;
-                    pb[r] += b1 * y;
-                }
+                for (int v = 0; v < VW; v++)
+#pragma unroll
+                    for (int r = 0; r < NR; r++) {
+                        const T y = yw[(c + v) * NR + r];
+                        pa[r] += b0.v[v] * y;
+                        pb[r] += b1.v[v] * y;
+                    }
             }
             __syncwarp();
         }
@@ -137,10 +154,12 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
 #pragma unroll
             for (int r = 0; r < NR; r++) y[r] = T(0);
 #pragma unroll
-            for (int c = 0; c < 16; c++) {
-                const T d = __ldg(Dm + row * 64 + cb + c);
+            for (int c = 0; c < 16; c += VW) {
+                const Vec16<T> d = ldg16(Dm + row * 64 + cb + c);
 #pragma unroll
-                for (int r = 0; r < NR; r++) y[r] += d * acc[(cb + c) * NR + r];
+                for (int v = 0; v < VW; v++)
+#pragma unroll
+                    for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
             }
 #pragma unroll
             for (int r = 0; r < NR; r++) {
