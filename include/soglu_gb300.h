@@ -189,6 +189,27 @@ int sog_system_set_wait_limit(sog_system *sys, double ms);
 int sog_debug_poison_task(sog_system *sys, int32_t task);
 int sog_debug_unpoison(sog_system *sys);
 
+/* ---- allocation-free residual check (no counterpart in the reference) ------
+ * r = b - A x in FP64 for a CSR matrix on the device, and per right-hand side
+ * rel_resid[c] = ||r||_2 / ||b||_2 and backward_error[c] =
+ * ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf), the figures sog_solve
+ * reports. For callers that cannot call cudaMalloc: code whose device memory
+ * is owned by another allocator (a framework's caching allocator, a fixed
+ * serving budget) and latency-critical loops where an allocation would
+ * synchronise the device. It allocates nothing: its reduction scratch is a
+ * fixed 3 KB array of device memory that every GPU loading the library holds
+ * until exit, so nrhs is limited to 1..64 (SOG_EINVAL beyond). All calls
+ * share that array: calls that overlap on the GPU (different streams or host
+ * threads) race and must be serialised by the caller. The first call on a
+ * device looks up the array's device address (with that device current);
+ * make that first call before any stream capture. Arrays are device pointers;
+ * b, x, r are n x nrhs row-major; rel_resid and backward_error are host
+ * arrays of nrhs; stream is a cudaStream_t (NULL = default stream); returns
+ * after the results are on the host. */
+int sog_residual_noalloc(int32_t n, const int32_t *row_ptr, const int32_t *col, const double *val, int32_t nrhs,
+                         const double *b, const double *x, double *r, double *rel_resid, double *backward_error,
+                         void *stream);
+
 /* ---- outer drop-in --------------------------------------------------------------
  * SOGLU::solveLU (solver.cpp:121-184): plan, factor and solve one system on
  * device 0; x_out receives n values in the original ordering. */

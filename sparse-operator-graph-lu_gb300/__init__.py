@@ -67,7 +67,7 @@ EXPORTS = [
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
     "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
     "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
-    "sog_system_task_graph", "sog_plan_task_graph_info",
+    "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc",
 ]
 
 _lib = None
@@ -100,6 +100,7 @@ def lib() -> C.CDLL:
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
         "sog_system_task_graph": ([P, P, P, P], I32), "sog_plan_task_graph_info": ([P, I32, P], I32),
+        "sog_residual_noalloc": ([I32, P, P, P, I32, P, P, P, P, P, P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

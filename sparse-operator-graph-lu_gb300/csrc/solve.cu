@@ -12,6 +12,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "api_internal.h"
 #include "kernels.h"
 
 namespace sog {
@@ -354,4 +359,72 @@ int count_nonfinite_launch(const double* x, int64_t n, unsigned long long* count
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// ---------------------------------------------------------------- allocation-free residual check
+// The residual kernel's reduction buffer normally comes from the block pool.
+// This variant keeps it in a fixed array of device memory that exists for as
+// long as the library is loaded, for callers that must not allocate device
+// memory themselves: code whose device memory is owned by another allocator
+// (a framework's caching allocator, a fixed serving budget) and latency-
+// critical loops where cudaMalloc / cudaFree would synchronise the device.
+constexpr int NOALLOC_MAX_RHS = 64;  // 6 doubles per right-hand side: 3 KB
+static __device__ __align__(256) double g_noalloc_red[RED * NOALLOC_MAX_RHS];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};  // device address of g_noalloc_red, per device
+
+// Once per device, with that device current: the device address of the
+// array (in host code the array's name is only a host-side stand-in).
+int noalloc_scratch(int dev, double** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (dev < 0 || dev >= 256) return SOG_EINVAL;
+    if (!g_noalloc_addr[dev]) {
+        double* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_red);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return sog_internal::fail(SOG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return SOG_OK;
+}
+}  // namespace
+
 }  // namespace sog
+
+extern "C" int sog_residual_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* col, const double* val,
+                                    int32_t nrhs, const double* b, const double* x, double* r, double* rel_resid,
+                                    double* backward_error, void* stream) {
+    using namespace sog;
+    if (n <= 0 || !row_ptr || !col || !val || !b || !x || !r || !rel_resid || !backward_error)
+        return sog_internal::fail(SOG_EINVAL, "sog_residual_noalloc: bad argument");
+    if (nrhs < 1 || nrhs > NOALLOC_MAX_RHS)
+        return sog_internal::fail(SOG_EINVAL, "sog_residual_noalloc: nrhs must be 1.." +
+                                                  std::to_string(NOALLOC_MAX_RHS) + " (fixed scratch size)");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return sog_internal::fail(SOG_ENODEV, "sog_residual_noalloc: no current device");
+    }
+    double* red = nullptr;
+    int rc = noalloc_scratch(dev, &red);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevCSR A{n, row_ptr, col, val};
+    // the array keeps the previous call's sums: clear the part this call accumulates into
+    cudaMemsetAsync(red, 0, sizeof(double) * RED * nrhs, s);
+    residual_kernel<<<(n + 255) / 256, 256, 0, s>>>(A, b, x, r, nrhs, red, n);
+    double host[RED * NOALLOC_MAX_RHS];
+    cudaMemcpyAsync(host, red, sizeof(double) * RED * nrhs, cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return sog_internal::fail(SOG_ECUDA, std::string("sog_residual_noalloc: ") + cudaGetErrorString(e));
+    for (int c = 0; c < nrhs; c++) {
+        const double* q = host + RED * c;
+        rel_resid[c] = q[1] > 0 ? std::sqrt(q[0]) / std::sqrt(q[1]) : std::sqrt(q[0]);
+        const double den = q[5] * q[3] + q[4];
+        backward_error[c] = den > 0 ? q[2] / den : q[2];
+    }
+    return SOG_OK;
+}
