@@ -1,12 +1,17 @@
 #!/usr/bin/env python3
 """Benchmark of the factor-and-solve path on GB300.
 
-Workload: 3D 7-point variable-coefficient diffusion on a 48^3 grid
-(n = 110,592, 760,320 nnz, k = exp(N(0,1)) seed 1, harmonic-mean faces,
-diagonal shift 1e-3, x_true ~ U[-1,1] seed 0), seeded synthetic data.
-A step = numeric factorisation of the planned op DAG (1.08M unit ops) plus
-one solve to ||b - A x||_2 / ||b||_2 <= 1e-10. Host planning (ordering +
-DAG) happens once before timing, as the symbolic analysis does.
+Default workload (--workload var48): 3D 7-point variable-coefficient
+diffusion on a 48^3 grid (n = 110,592, 760,320 nnz, k = exp(N(0,1)) seed 1,
+harmonic-mean faces, diagonal shift 1e-3, x_true ~ U[-1,1] seed 0), seeded
+synthetic data. A step = numeric factorisation of the planned op DAG (1.08M
+unit ops) plus one solve to ||b - A x||_2 / ||b||_2 <= 1e-10 for every
+right-hand side. Host planning (ordering + DAG) happens once before timing,
+as the symbolic analysis does.
+
+Other workloads: lap64 = 3D 7-point Laplacian 64^3 (n = 262,144, 7.1M unit
+ops) with 64 right-hand sides (x_true ~ U[-1,1] seed 0); var24 = the var-coef
+system on 24^3, a small case of the same kernels for profiler captures.
 
   value   mixed precision (FP32 factors, 3xTF32 tile products, FP64
           refinement), inputs resident in HBM, solves/s over all ranks
@@ -36,7 +41,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG_DIR = os.path.join(ROOT, "sparse-operator-graph-lu_gb300")
 METRIC = "solves/s mixed+IR vs plain FP64 GPU LU at resid<=1e-10; p50/p99 latency"
-WORKLOAD = "3D 7-point var-coef diffusion 48^3 (n=110592, nnz=760320), 1 RHS, factor+solve to rel resid<=1e-10"
+WORKLOADS = {
+    "var48": "3D 7-point var-coef diffusion 48^3 (n=110592, nnz=760320), 1 RHS, factor+solve to rel resid<=1e-10",
+    "lap64": "3D 7-point Laplacian 64^3 (n=262144, nnz=1810432), 64 RHS, factor+solve to rel resid<=1e-10",
+    "var24": "3D 7-point var-coef diffusion 24^3 (n=13824, nnz=93312), 1 RHS, factor+solve to rel resid<=1e-10",
+}
 
 
 def load_package():
@@ -57,10 +66,12 @@ def build_native():
     b.build()
 
 
-def make_workload():
+def make_workload(name: str):
     load_package()
     import soglu_gb300.workloads as wl
-    return wl.varcoef3d(48)
+    if name == "lap64":
+        return wl.lap3d(64, nrhs=64)
+    return wl.varcoef3d(24 if name == "var24" else 48)
 
 
 def algorithmic_flops(op_count) -> float:
@@ -177,7 +188,11 @@ def run_reference(args):
         return 0
     build_native()
     sg = load_package()
-    s = make_workload()
+    if args.workload == "lap64":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU executor restatement keeps every 64^3 tile "
+                          "resident (50 GB of host memory, no free-after-last-use); run the default workload"}))
+        return 0
+    s = make_workload(args.workload)
     plan = sg.Plan(s.n, s.rows, s.cols, s.vals)
     perm, ops, L, U = plan.export()
     exp = (perm, ops, L, U, plan.info.block_rows, plan.info.storage_count, plan.input_tiles(s.vals))
@@ -194,11 +209,11 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": "fp64 CPU", "parallelism": "host cores"},
+            "config": {"workload": WORKLOADS[args.workload], "precision": "fp64 CPU", "parallelism": "host cores"},
             "rel_resid": rr,
             "p50_ms": 1e3 * statistics.median(times), "p99_ms": 1e3 * max(times),
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full factor+solve steps of the 48^3 system (the reference's "
+                             "sample": f"{args.steps} full factor+solve steps of the {args.workload} system (the reference's "
                                        "AVX-512 kernels do not compile on the aarch64 host; the C restatement "
                                        "of its executor path, pinned to the reference's outputs, is timed)"},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -216,7 +231,8 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     build_native()
     sg = load_package()
-    s = make_workload()
+    s = make_workload(args.workload)
+    nrhs = 1 if s.b.ndim == 1 else s.b.shape[0]
     t0 = time.perf_counter()
     plan = sg.Plan(s.n, s.rows, s.cols, s.vals)
     t_plan = time.perf_counter() - t0
@@ -257,7 +273,7 @@ def run_ours(args):
     def step(sysm, host):
         if host is None:
             sysm.factor_device(V.data_ptr())
-            return sysm.solve_device(1, b.data_ptr(), x.data_ptr())
+            return sysm.solve_device(nrhs, b.data_ptr(), x.data_ptr())
         hv, hb = host
         sysm.factor(hv)
         xs, st = sysm.solve(hb)
@@ -301,13 +317,13 @@ def run_ours(args):
                      "frac": flops / (f64m * 1e-3) / 1e12 / peaks["fp64_tflops"],
                      "peak_source": "cuBLAS DGEMM measured in this run", "avg_factor_ms": f64m}
         cpu = None
-        if world == 1 and not args.no_cpu_baseline:
+        if world == 1 and nrhs == 1 and not args.no_cpu_baseline:
             perm, ops, L, U = plan.export()
             exp = (perm, ops, L, U, info.block_rows, info.storage_count, plan.input_tiles(s.vals))
             cores = os.cpu_count() or 1
             dt, xc = cpu_oracle_step(exp, s, cores)
             cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-                   "sample": "one full factor+solve of the 48^3 system through the C restatement of the "
+                   "sample": f"one full factor+solve of the {args.workload} system through the C restatement of the "
                              "reference's executor path (the reference's AVX-512 build does not compile on aarch64)",
                    "seconds": dt}
         xt = s.x_true
@@ -315,8 +331,10 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": rm["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": "mixed: FP32 factors, 3xTF32 tile products, FP64 IR",
-                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (tiles 5.8 GB)",
+            "config": {"workload": WORKLOADS[args.workload], "rhs": nrhs,
+                       "precision": "mixed: FP32 factors, 3xTF32 tile products, FP64 IR",
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2 (FP32 tiles {info.storage_count * 16384 / 1e9:.2f} GB)",
                        "executor": "persistent queue"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),
@@ -330,8 +348,8 @@ def run_ours(args):
             "mixed_over_fp64": value / v64,
             "dominant": dominant,
             "roofline": roof,
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(s.nnz * 8 + s.n * 8),
-                    "d2h_bytes_per_step": int(s.n * 8), "ms_per_step": re2e["ms"] / args.steps},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(s.nnz * 8 + s.n * 8 * nrhs),
+                    "d2h_bytes_per_step": int(s.n * 8 * nrhs), "ms_per_step": re2e["ms"] / args.steps},
             "cpu_baseline": cpu,
             "clocks": rm["clocks"],
             "gpu_launches": int(rm["launches"]),
@@ -354,6 +372,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="var48")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -100,7 +100,9 @@ int sog_plan_build(int32_t n, int64_t nnz, int32_t symmetric, const int32_t *I, 
 int sog_plan_get_info(const sog_plan *plan, sog_plan_info *info);
 /* Copy out the plan: new_to_old[n] (GOrder::newOrder), ops[nops] in the
  * reference's stage order, lleaf/uleaf [n_*leaf][3] = {bi, bj, block id}. Any
- * pointer may be NULL to skip that array. */
+ * pointer may be NULL to skip that array. For a batch plan (sog_plan_merge)
+ * new_to_old has n_ext entries: per permuted row its row in its own system's
+ * original ordering, -1 for padding. */
 int sog_plan_export(const sog_plan *plan, int32_t *new_to_old, sog_op *ops, int32_t *lleaf, int32_t *uleaf);
 /* Dense input tiles (n_input x 64 x 64, row-major) for values V in the
  * triplet order given to sog_plan_build (BlockPlanner::iniBlockStorage,
@@ -112,6 +114,23 @@ int sog_plan_input_tiles(const sog_plan *plan, const double *V, double *tiles);
 int sog_plan_import(int32_t block_rows, int32_t storage_count, int32_t n_input, const sog_op *ops, int64_t nops,
                     const int32_t *lleaf, int64_t n_lleaf, const int32_t *uleaf, int64_t n_uleaf, sog_plan **out);
 void sog_plan_destroy(sog_plan *plan);
+
+/* ---- batches -----------------------------------------------------------------
+ * No counterpart in the reference, which factors one system per process
+ * (solver.cpp:121). A batch plan is the block-diagonal union of independent
+ * systems' plans: every op, stage and leaf of each system as its own planner
+ * made it, block ids and block rows shifted, so one executor launch factors
+ * all systems and merges ready tile operations of different systems into the
+ * same launch. A system built from it (sog_system_create) takes, in system
+ * order: V = the systems' triplet values concatenated (sog_factor*), and for
+ * solves b / x = per system nrhs_k x n_k values (rhs-major within the system),
+ * concatenated. Refinement (SOG_MIXED) stops per system: a system that has
+ * converged receives no further corrections while others refine, so its
+ * result is the one it gets alone. Imported plans cannot be batched. */
+int sog_plan_merge(const sog_plan *const *plans, int32_t count, sog_plan **out);
+/* Number of systems in a plan (1 for a plain plan) and, if n is not NULL,
+ * each system's dimension. */
+int sog_plan_segments(const sog_plan *plan, int32_t *count, int32_t *n);
 
 /* ---- device context ----------------------------------------------------------
  * The device block-pool arena that replaces memutil's per-thread block pools
@@ -146,6 +165,15 @@ int sog_factor_tiles(sog_system *sys, const double *tiles);
 int sog_solve(sog_system *sys, int32_t nrhs, const double *b, double *x, sog_solve_stats *stats);
 /* Same with device pointers. */
 int sog_solve_device(sog_system *sys, int32_t nrhs, const double *b_dev, double *x_dev, sog_solve_stats *stats);
+/* Batch solve with a right-hand-side count per system (nrhs[k] >= 0; a
+ * system with 0 right-hand sides is skipped): b / x = per system nrhs[k] x
+ * n_k values, concatenated in system order. stats, if not NULL, receives one
+ * entry per system (count from sog_plan_segments); the return value is the
+ * worst status. On a plain plan this is sog_solve with nrhs[0]. */
+int sog_solve_batch(sog_system *sys, const int32_t *nrhs, const double *b, double *x, sog_solve_stats *stats);
+/* Same with device pointers. */
+int sog_solve_batch_device(sog_system *sys, const int32_t *nrhs, const double *b_dev, double *x_dev,
+                           sog_solve_stats *stats);
 /* BlockPlanner::solve exactly: b_ext / x_ext are host arrays of length n_ext
  * in the planner's (permuted, padded) ordering; one right-hand side; no
  * refinement. */

@@ -67,7 +67,8 @@ EXPORTS = [
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
     "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
     "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
-    "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc",
+    "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
+    "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device",
 ]
 
 _lib = None
@@ -101,6 +102,8 @@ def lib() -> C.CDLL:
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
         "sog_system_task_graph": ([P, P, P, P], I32), "sog_plan_task_graph_info": ([P, I32, P], I32),
         "sog_residual_noalloc": ([I32, P, P, P, I32, P, P, P, P, P, P], I32),
+        "sog_plan_merge": ([P, I32, P], I32), "sog_plan_segments": ([P, P, P], I32),
+        "sog_solve_batch": ([P, P, P, P, P], I32), "sog_solve_batch_device": ([P, P, P, P, P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -149,20 +152,30 @@ class Plan:
                                      lleaf.shape[0], _p(uleaf), uleaf.shape[0], C.byref(h)))
         return cls(0, None, None, _handle=h)
 
+    def segments(self) -> list[int]:
+        """Dimensions of the systems in this plan (one entry for a plain plan)."""
+        cnt = C.c_int32()
+        _check(lib().sog_plan_segments(self._h, C.byref(cnt), None))
+        n = np.zeros(cnt.value, np.int32)
+        _check(lib().sog_plan_segments(self._h, C.byref(cnt), _p(n)))
+        return [int(v) for v in n]
+
     def info_dict(self) -> dict:
         d = {k: getattr(self.info, k) for k, _ in PlanInfo._fields_ if k != "op_count"}
         d["ops"] = {OP_NAMES[i]: int(self.info.op_count[i]) for i in range(13) if self.info.op_count[i]}
         return d
 
     def export(self):
-        """(new_to_old[n], ops[nops, 6] = op,src,src2,result,result2,stage, L[k,3], U[k,3])."""
+        """(new_to_old[n], ops[nops, 6] = op,src,src2,result,result2,stage, L[k,3], U[k,3]).
+        For a batch plan new_to_old has n_ext entries (row within its system, -1 = padding)."""
         i = self.info
-        perm = np.empty(max(i.n, 1), np.int32)
+        nperm = i.n_ext if getattr(self, "batch", False) else i.n
+        perm = np.empty(max(nperm, 1), np.int32)
         ops = np.empty((max(i.nops, 1), 6), np.int32)
         L = np.empty((max(i.n_lleaf, 1), 3), np.int32)
         U = np.empty((max(i.n_uleaf, 1), 3), np.int32)
         _check(lib().sog_plan_export(self._h, _p(perm), _p(ops), _p(L), _p(U)))
-        return perm[:i.n], ops[:i.nops], L[:i.n_lleaf], U[:i.n_uleaf]
+        return perm[:nperm], ops[:i.nops], L[:i.n_lleaf], U[:i.n_uleaf]
 
     def input_tiles(self, vals) -> np.ndarray:
         v = np.ascontiguousarray(vals, dtype=np.float64)
@@ -188,6 +201,21 @@ class Plan:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.sog_plan_destroy(self._h)
             self._h = None
+
+
+def merge_plans(plans) -> Plan:
+    """Batch plan: the block-diagonal union of independent systems' plans
+    (sog_plan_merge). A System on it factors every system in one executor
+    launch; values are the systems' triplet values concatenated, and solves go
+    through System.solve_batch."""
+    plans = list(plans)
+    arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
+    h = C.c_void_p()
+    _check(lib().sog_plan_merge(arr, len(plans), C.byref(h)))
+    m = Plan(0, None, None, _handle=h)
+    m.nnz = sum(p.nnz for p in plans)
+    m.batch = True
+    return m
 
 
 class Context:
@@ -250,6 +278,8 @@ class System:
         b = np.ascontiguousarray(b, dtype=np.float64)
         if b.ndim not in (1, 2) or b.shape[-1] != self.n:
             raise ValueError(f"right-hand side must have shape (n,) or (k, n) with n = {self.n}")
+        if b.ndim == 2 and len(self.plan.segments()) > 1:
+            raise ValueError("several right-hand sides of a batch: use solve_batch")
         k = 1 if b.ndim == 1 else b.shape[0]
         x = np.empty_like(b)
         st = SolveStats()
@@ -257,6 +287,38 @@ class System:
         if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
             _check(rc)
         return x, st.as_dict()
+
+    def solve_batch(self, bs, allow_noconv: bool = False):
+        """Per-system right-hand sides of a batch system: bs[k] of shape (n_k,)
+        or (r_k, n_k) (r_k may differ between systems, and may be 0). Returns
+        the per-system solutions (shaped as given) and statistics."""
+        ns = self.plan.segments()
+        if len(bs) != len(ns):
+            raise ValueError(f"expected {len(ns)} right-hand-side blocks, got {len(bs)}")
+        arrs, cnt = [], np.zeros(len(ns), np.int32)
+        for k, (bk, n) in enumerate(zip(bs, ns)):
+            a = np.ascontiguousarray(bk, dtype=np.float64)
+            if a.shape[-1] != n or a.ndim not in (1, 2):
+                raise ValueError(f"system {k}: right-hand side must have shape ({n},) or (r, {n})")
+            cnt[k] = 1 if a.ndim == 1 else a.shape[0]
+            arrs.append(a)
+        b = np.concatenate([a.ravel() for a in arrs]) if arrs else np.zeros(0)
+        x = np.empty_like(b)
+        st = (SolveStats * len(ns))()
+        rc = lib().sog_solve_batch(self._h, _p(cnt), _p(b) if b.size else None, _p(x) if x.size else None, st)
+        if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
+            _check(rc)
+        xs, o = [], 0
+        for a in arrs:
+            xs.append(x[o:o + a.size].reshape(a.shape))
+            o += a.size
+        return xs, [st[k].as_dict() for k in range(len(ns))]
+
+    def solve_batch_device(self, nrhs, b_ptr: int, x_ptr: int) -> list[dict]:
+        cnt = np.ascontiguousarray(nrhs, dtype=np.int32)
+        st = (SolveStats * cnt.size)()
+        _check(lib().sog_solve_batch_device(self._h, _p(cnt), C.c_void_p(b_ptr), C.c_void_p(x_ptr), st))
+        return [st[k].as_dict() for k in range(cnt.size)]
 
     def solve_device(self, nrhs: int, b_ptr: int, x_ptr: int) -> dict:
         st = SolveStats()

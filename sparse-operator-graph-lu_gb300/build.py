@@ -24,7 +24,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SRC = ["order.cpp", "planner.cpp", "mtx.cpp", "tasks.cpp", "plan_api.cpp", "runtime.cpp"]
+HOST_SRC = ["order.cpp", "planner.cpp", "mtx.cpp", "tasks.cpp", "batch.cpp", "plan_api.cpp", "runtime.cpp"]
 CUDA_SRC = ["factor.cu", "solve.cu"]
 HEADERS = ["plan.h", "tasks.h", "kernels.h", "api_internal.h"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function", f"-I{CUDA}/include",

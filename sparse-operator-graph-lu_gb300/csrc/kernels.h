@@ -102,11 +102,31 @@ void residual_launch(const DevCSR& A, const double* b, const double* x, double* 
 void scatter_csr_launch(const double* V, const int32_t* pos, int64_t nnz, double* csr_val, cudaStream_t s);
 void cast_f64_to_f32_launch(const double* src, float* dst, int64_t n, cudaStream_t s);
 void axpy_f32_to_f64_launch(const float* d, double* x, int64_t n, int assign, cudaStream_t s);
-// original-order rhs-major (nrhs x n) <-> permuted padded row-major (n_ext x nrhs)
-void gather_rhs_launch(const double* b, const int32_t* new_to_old, int n, int n_ext, int nrhs, double* out,
-                       cudaStream_t s);
-void scatter_solution_launch(const double* xe, const int32_t* old_to_new, int n, int nrhs, double* x,
-                             cudaStream_t s);
-int count_nonfinite_launch(const double* x, int64_t n, unsigned long long* counter, cudaStream_t s);
+// The systems of a solve. Permuted row i belongs to system of_brow[i >> 6]
+// and is row n2o[i] of that system's original ordering (-1 = padding). The
+// caller's b / x hold, per system k, nrhs[k] x n[k] values (rhs-major) at
+// offset voff[k]. A plain system is one such system with voff = 0.
+struct DevSegs {
+    int32_t nseg;
+    const int32_t* of_brow;  // per block row
+    const int32_t* n2o;      // per permuted row
+    const int32_t* n;        // per system
+    const int32_t* nrhs;     // per system, this solve
+    const int64_t* voff;     // per system, this solve
+    const int32_t* active;   // per system: 1 = takes the next refinement correction
+};
+// caller layout -> permuted padded row-major (n_ext x nc) for columns
+// [c0, c0+nc): padding rows get 1 (the reference's b for padded rows,
+// solver.cpp:159-161), columns past a system's nrhs get 0
+void gather_seg_launch(const double* b, const DevSegs& g, int n_ext, int c0, int nc, double* out, cudaStream_t s);
+// the inverse for real rows and columns; per-system non-finite counts into cnt[k]
+void scatter_seg_launch(const double* xe, const DevSegs& g, int n_ext, int c0, int nc, double* x,
+                        unsigned long long* cnt, cudaStream_t s);
+// r = b - A x (n_ext x nc); reductions per (system, column) over the system's
+// real rows and columns: red[(k*nc + c)*6 + {0..5}] as residual_launch
+void residual_seg_launch(const DevCSR& A, const double* b, const double* x, double* r, int c0, int nc,
+                         double* red, const DevSegs& g, cudaStream_t s);
+// dst = active[system of row] ? (float)src : 0 over n_ext x nc
+void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s);
 
 }  // namespace sog

@@ -56,6 +56,16 @@ struct Leaf {
     int32_t bi, bj, id;
 };
 
+// One system of a batch plan (merge_plans): its rows occupy permuted rows
+// [row0, row0 + 64*R) of the block-diagonal union, of which the first n are
+// real (the rest are its unit-diagonal padding); its original rows are
+// [noff, noff + n) of the concatenated original ordering, and its triplets
+// [trip_off, trip_off + ntrip) of the concatenated triplet values.
+struct Segment {
+    int32_t row0 = 0, n = 0, R = 0;
+    int64_t noff = 0, trip_off = 0, ntrip = 0;
+};
+
 // Everything the executor needs, in the reference's terms.
 struct Plan {
     Config cfg;
@@ -73,6 +83,10 @@ struct Plan {
     std::vector<int16_t> scatter_off;
     std::vector<int32_t> pad_tile;  // tile index of each padded row's diagonal
     std::vector<int16_t> pad_off;
+    // Batch plans only: the merged systems in order. Then ord.new_to_old has
+    // one entry per permuted row (n_ext): the row's index within its own
+    // system's original ordering, -1 for padding; ord.old_to_new is empty.
+    std::vector<Segment> segs;
     // statistics
     int64_t coarse_ops_emitted = 0, coarse_ops = 0, fine_ops_emitted = 0;
     double t_order = 0, t_plan = 0;
@@ -82,6 +96,14 @@ struct Plan {
 // two-level planning (solver.cpp:56-110). Throws std::runtime_error on bad input.
 Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I, const int32_t* J, const double* V,
                 int threads = 0);
+
+// Block-diagonal union of independent systems' plans (a batch): one DAG whose
+// ops from different systems never share a block, so one executor launch
+// factors all of them. Block ids are renumbered with every system's input
+// tiles first (ids 1..sum n_input, in system order), then every system's
+// other blocks; block rows are stacked in system order. Throws on plans that
+// cannot be merged (imported plans, batch plans, size overflow).
+Plan merge_plans(const std::vector<const Plan*>& ps);
 
 // Dense input tiles (n_input x 64 x 64, row-major) for values V of the same
 // triplets build_plan saw (after mirroring when symmetric).

@@ -2,6 +2,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "api_internal.h"
 
@@ -128,6 +129,43 @@ int sog_plan_import(int32_t block_rows, int32_t storage_count, int32_t n_input, 
     } catch (const std::exception& e) {
         return fail(SOG_EINVAL, e.what());
     }
+}
+
+int sog_plan_merge(const sog_plan* const* plans, int32_t count, sog_plan** out) {
+    if (!out) return fail(SOG_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (count <= 0 || !plans) return fail(SOG_EINVAL, "no plans to merge");
+    std::vector<const sog::Plan*> ps;
+    int64_t nnz = 0;
+    for (int32_t k = 0; k < count; k++) {
+        if (!plans[k]) return fail(SOG_EINVAL, "NULL plan in batch");
+        if (plans[k]->imported) return fail(SOG_EINVAL, "imported plans carry no triplet scatter: cannot batch");
+        ps.push_back(&plans[k]->p);
+        nnz += plans[k]->nnz;
+    }
+    try {
+        sog_plan* p = new sog_plan();
+        p->p = sog::merge_plans(ps);
+        p->nnz = nnz;
+        *out = p;
+        return SOG_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(SOG_ENOMEM, "host allocation failed while merging plans");
+    } catch (const std::exception& e) {
+        return fail(SOG_EINVAL, e.what());
+    }
+}
+
+int sog_plan_segments(const sog_plan* plan, int32_t* count, int32_t* n) {
+    if (!plan || !count) return fail(SOG_EINVAL, "NULL argument");
+    const sog::Plan& p = plan->p;
+    *count = p.segs.empty() ? 1 : (int32_t)p.segs.size();
+    if (n) {
+        if (p.segs.empty()) n[0] = p.cfg.n;
+        else
+            for (size_t k = 0; k < p.segs.size(); k++) n[k] = p.segs[k].n;
+    }
+    return SOG_OK;
 }
 
 void sog_plan_destroy(sog_plan* plan) { delete plan; }

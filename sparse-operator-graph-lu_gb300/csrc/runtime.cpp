@@ -116,7 +116,6 @@ struct sog_ctx {
     int num_sms = 0;
     Pool pool;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double* host_red = nullptr;  // pinned
 };
 
 struct sog_system {
@@ -147,13 +146,23 @@ struct sog_system {
     int32_t* d_csr_pos = nullptr;
     int32_t *d_sc_tile = nullptr, *d_pad_tile = nullptr;
     int16_t *d_sc_off = nullptr, *d_pad_off = nullptr;
-    int32_t *d_n2o = nullptr, *d_o2n = nullptr;
+    // systems of the plan (one for a plain plan; a batch plan's merged systems)
+    std::vector<Segment> segs;
+    int32_t *d_seg_brow = nullptr, *d_seg_n = nullptr, *d_n2o = nullptr;
     double* d_V = nullptr;
     // vectors (for up to vec_nrhs right-hand sides)
-    double *d_borig = nullptr, *d_xorig = nullptr, *d_bext = nullptr, *d_xext = nullptr, *d_r = nullptr,
-           *d_red = nullptr;
+    double *d_bext = nullptr, *d_xext = nullptr, *d_r = nullptr, *d_red = nullptr;
     float* d_v32 = nullptr;
-    unsigned long long* d_cnt = nullptr;
+    unsigned long long* d_cnt = nullptr;  // per system
+    int32_t *d_seg_nrhs = nullptr, *d_seg_active = nullptr;
+    int64_t* d_seg_voff = nullptr;
+    // pinned host mirrors: reductions (nseg x 64 x RED), per-system nrhs /
+    // active / offsets / non-finite counts
+    double* h_red = nullptr;
+    int32_t *h_nrhs = nullptr, *h_active = nullptr;
+    int64_t* h_voff = nullptr;
+    unsigned long long* h_cnt = nullptr;
+    std::vector<sog_solve_stats> seg_stats;
     int epoch = 2;
     bool factored = false;
     float t_factor = 0, t_solve = 0;
@@ -201,11 +210,11 @@ struct HostCSR {
 };
 HostCSR build_csr(const Plan& p) {
     HostCSR h;
-    const int n_ext = p.cfg.n_ext(), n = p.cfg.n;
+    const int n_ext = p.cfg.n_ext();
     const size_t nt = p.scatter_tile.size();
     std::vector<int64_t> key;
     std::vector<int32_t> trip;
-    key.reserve(nt + (n_ext - n));
+    key.reserve(nt + p.pad_tile.size());
     for (size_t k = 0; k < nt; k++) {
         int32_t t = p.scatter_tile[k];
         if (t < 0) continue;
@@ -214,8 +223,10 @@ HostCSR build_csr(const Plan& p) {
         key.push_back(row * n_ext + col);
         trip.push_back((int32_t)k);
     }
-    for (int i = n; i < n_ext; i++) {
-        key.push_back((int64_t)i * n_ext + i);
+    // padded rows: unit diagonal (one entry per padded row in the pad list)
+    for (size_t q = 0; q < p.pad_tile.size(); q++) {
+        const int64_t i = (int64_t)p.input_bi[p.pad_tile[q]] * 64 + p.pad_off[q] / 64;
+        key.push_back(i * n_ext + i);
         trip.push_back(-1);
     }
     std::vector<int64_t> order(key.size());
@@ -241,25 +252,40 @@ int ensure_vectors(sog_system* s, int nrhs) {
     if (nrhs <= s->vec_nrhs) return SOG_OK;
     if (s->vecs) s->ctx->pool.release(s->vecs, s->vec_bytes);
     s->vecs = nullptr;
+    s->vec_nrhs = 0;
     Layout L;
-    const size_t ne = (size_t)s->n_ext * nrhs, no = (size_t)s->n * nrhs;
-    uint64_t o_borig = L.add<double>(no), o_xorig = L.add<double>(no), o_bext = L.add<double>(ne),
-             o_xext = L.add<double>(ne), o_r = L.add<double>(ne), o_red = L.add<double>((size_t)RED * nrhs),
-             o_v32 = L.add<float>(ne), o_cnt = L.add<unsigned long long>(1);
+    const size_t ne = (size_t)s->n_ext * nrhs, ns = s->segs.size();
+    uint64_t o_bext = L.add<double>(ne), o_xext = L.add<double>(ne), o_r = L.add<double>(ne),
+             o_red = L.add<double>((size_t)RED * nrhs * ns), o_v32 = L.add<float>(ne),
+             o_cnt = L.add<unsigned long long>(ns), o_nrhs = L.add<int32_t>(ns), o_act = L.add<int32_t>(ns),
+             o_voff = L.add<int64_t>(ns);
     char* base = static_cast<char*>(s->ctx->pool.alloc(L.off));
     if (!base) return fail(SOG_ENOMEM, "block pool exhausted (solve vectors)");
     s->vecs = base;
     s->vec_bytes = L.off;
     s->vec_nrhs = nrhs;
-    s->d_borig = (double*)(base + o_borig);
-    s->d_xorig = (double*)(base + o_xorig);
     s->d_bext = (double*)(base + o_bext);
     s->d_xext = (double*)(base + o_xext);
     s->d_r = (double*)(base + o_r);
     s->d_red = (double*)(base + o_red);
     s->d_v32 = (float*)(base + o_v32);
     s->d_cnt = (unsigned long long*)(base + o_cnt);
+    s->d_seg_nrhs = (int32_t*)(base + o_nrhs);
+    s->d_seg_active = (int32_t*)(base + o_act);
+    s->d_seg_voff = (int64_t*)(base + o_voff);
     return SOG_OK;
+}
+
+DevSegs seg_view(const sog_system* s) {
+    DevSegs g;
+    g.nseg = (int32_t)s->segs.size();
+    g.of_brow = s->d_seg_brow;
+    g.n2o = s->d_n2o;
+    g.n = s->d_seg_n;
+    g.nrhs = s->d_seg_nrhs;
+    g.voff = s->d_seg_voff;
+    g.active = s->d_seg_active;
+    return g;
 }
 
 template <class T>
@@ -331,40 +357,55 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
     return SOG_OK;
 }
 
-struct Norms {
-    double rel = 0, bwd = 0;
-};
-int read_norms(sog_system* s, int nrhs, Norms& out) {
+// Per-system norms of this chunk's residual (columns [c0, c0+nc)), folded
+// into the systems' statistics; rel[k] = worst relative residual of system k
+// over the chunk's columns it has (0 if none).
+int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
     sog_ctx* c = s->ctx;
-    CK(cudaMemcpyAsync(c->host_red, s->d_red, sizeof(double) * RED * nrhs, cudaMemcpyDeviceToHost, c->stream));
+    const size_t ns = s->segs.size();
+    CK(cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED * nc * ns, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    out = Norms();
-    for (int k = 0; k < nrhs; k++) {
-        const double* r = c->host_red + RED * k;
-        double rel = r[1] > 0 ? std::sqrt(r[0]) / std::sqrt(r[1]) : std::sqrt(r[0]);
-        double den = r[5] * r[3] + r[4];
-        double bwd = den > 0 ? r[2] / den : r[2];
-        if (!(rel <= out.rel)) out.rel = rel;  // NaN propagates
-        if (!(bwd <= out.bwd)) out.bwd = bwd;
+    rel.assign(ns, 0.0);
+    for (size_t k = 0; k < ns; k++) {
+        sog_solve_stats& ss = s->seg_stats[k];
+        ss.rel_resid = ss.backward_error = 0;  // the latest iterate's norms
+        const int creal = std::min(nc, s->h_nrhs[k] - c0);
+        for (int j = 0; j < creal; j++) {
+            const double* r = s->h_red + ((size_t)k * nc + j) * RED;
+            const double rl = r[1] > 0 ? std::sqrt(r[0]) / std::sqrt(r[1]) : std::sqrt(r[0]);
+            const double den = r[5] * r[3] + r[4];
+            const double bw = den > 0 ? r[2] / den : r[2];
+            if (!(rl <= rel[k])) rel[k] = rl;  // NaN propagates
+            if (!(bw <= ss.backward_error)) ss.backward_error = bw;
+        }
+        ss.rel_resid = rel[k];
     }
     return SOG_OK;
 }
 
-// one chunk of <= 64 right-hand sides; b_ext already gathered into d_bext
-int solve_chunk(sog_system* s, int nc, sog_solve_stats* stats) {
+// One chunk of <= 64 right-hand-side columns [c0, c0+nc); b_ext already
+// gathered into d_bext. Refinement (mixed) corrects only the systems that
+// have not converged yet: the others' corrections are masked to zero, which
+// leaves their iterates bit for bit unchanged.
+int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chunk_stats) {
     sog_ctx* c = s->ctx;
     cudaStream_t st = c->stream;
     const int64_t ne = (int64_t)s->n_ext * nc;
+    const size_t ns = s->segs.size();
+    const DevSegs g = seg_view(s);
     int r;
-    Norms nm;
-    int iters = 0;
+    std::vector<double> rel;
+    std::vector<int> iters(ns, 0);
+    for (size_t k = 0; k < ns; k++) s->seg_stats[k].rel_resid = s->seg_stats[k].backward_error = 0;
+    bool have_norms = false;
     if (s->fp64) {
         CK(cudaMemcpyAsync(s->d_xext, s->d_bext, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st));
         if ((r = trisolve(s, s->d_xext, nc))) return r;
         if (s->csr.ptr) {
             s->launches++;
-            residual_launch(s->csr, s->d_bext, s->d_xext, s->d_r, nc, s->d_red, s->n, st);
-            if ((r = read_norms(s, nc, nm))) return r;
+            residual_seg_launch(s->csr, s->d_bext, s->d_xext, s->d_r, c0, nc, s->d_red, g, st);
+            if ((r = read_norms(s, c0, nc, rel))) return r;
+            have_norms = true;
         }
     } else {
         s->launches++;
@@ -375,64 +416,138 @@ int solve_chunk(sog_system* s, int nc, sog_solve_stats* stats) {
         if (s->csr.ptr) {
             for (;;) {
                 s->launches++;
-                residual_launch(s->csr, s->d_bext, s->d_xext, s->d_r, nc, s->d_red, s->n, st);
-                if ((r = read_norms(s, nc, nm))) return r;
-                if (nm.rel <= s->opt.tol || iters >= s->opt.max_refine || std::isnan(nm.rel)) break;
+                residual_seg_launch(s->csr, s->d_bext, s->d_xext, s->d_r, c0, nc, s->d_red, g, st);
+                if ((r = read_norms(s, c0, nc, rel))) return r;
+                have_norms = true;
+                bool any = false;
+                for (size_t k = 0; k < ns; k++) {
+                    const bool act = !(rel[k] <= s->opt.tol) && !std::isnan(rel[k]) && iters[k] < s->opt.max_refine;
+                    s->h_active[k] = act ? 1 : 0;
+                    any = any || act;
+                }
+                if (!any) break;
+                CK(cudaMemcpyAsync(s->d_seg_active, s->h_active, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, st));
                 s->launches++;
-                cast_f64_to_f32_launch(s->d_r, s->d_v32, ne, st);
+                cast_seg_launch(s->d_r, s->d_v32, s->n_ext, nc, g, st);
                 if ((r = trisolve(s, s->d_v32, nc))) return r;
                 s->launches++;
                 axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 0, st);
-                iters++;
+                for (size_t k = 0; k < ns; k++) iters[k] += s->h_active[k];
             }
         }
     }
     if ((r = check_status(s, false))) return r;
-    if (stats) {
-        stats->iterations = std::max(stats->iterations, iters);
-        if (!(nm.rel <= stats->rel_resid)) stats->rel_resid = nm.rel;
-        if (!(nm.bwd <= stats->backward_error)) stats->backward_error = nm.bwd;
+    for (size_t k = 0; k < ns; k++) {
+        if (c0 >= s->h_nrhs[k]) continue;
+        sog_solve_stats& cs = chunk_stats[k];
+        const sog_solve_stats& ss = s->seg_stats[k];
+        cs.iterations = std::max(cs.iterations, iters[k]);
+        if (have_norms) {
+            if (!(ss.rel_resid <= cs.rel_resid)) cs.rel_resid = ss.rel_resid;
+            if (!(ss.backward_error <= cs.backward_error)) cs.backward_error = ss.backward_error;
+            if (!s->fp64 && !(ss.rel_resid <= s->opt.tol)) cs.status = SOG_ENOCONV;
+        }
     }
-    if (!s->fp64 && s->csr.ptr && !(nm.rel <= s->opt.tol)) return SOG_ENOCONV;
     return SOG_OK;
 }
 
-int solve_device_impl(sog_system* s, int nrhs, const double* b_dev, double* x_dev, sog_solve_stats* stats) {
+// Solve for nrhs[k] right-hand sides of each system k (caller layout: per
+// system nrhs[k] x n_k, rhs-major, concatenated). Per-system statistics go to
+// s->seg_stats; agg (if not NULL) gets the worst over systems.
+int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, double* x_dev,
+                      sog_solve_stats* agg) {
     sog_ctx* c = s->ctx;
     cudaStream_t st = c->stream;
-    if (stats) {
-        std::memset(stats, 0, sizeof(*stats));
-        stats->min_pivot = bits_to_double(s->last.min_pivot_bits);
-        stats->clamped_pivots = s->last.clamped;
+    const size_t ns = s->segs.size();
+    int maxr = 0;
+    int64_t off = 0;
+    for (size_t k = 0; k < ns; k++) {
+        if (nrhs[k] < 0) return fail(SOG_EINVAL, "negative right-hand-side count");
+        s->h_nrhs[k] = nrhs[k];
+        s->h_voff[k] = off;
+        off += (int64_t)nrhs[k] * s->segs[k].n;
+        maxr = std::max(maxr, nrhs[k]);
     }
-    int r = ensure_vectors(s, std::min(nrhs, 64));
+    sog_solve_stats base;
+    std::memset(&base, 0, sizeof(base));
+    base.min_pivot = bits_to_double(s->last.min_pivot_bits);
+    base.clamped_pivots = s->last.clamped;
+    std::vector<sog_solve_stats> out(ns, base);
+    s->seg_stats.assign(ns, base);
+    if (agg) *agg = base;
+    if (maxr == 0) return SOG_OK;
+    int r = ensure_vectors(s, std::min(maxr, 64));
     if (r) return r;
+    CK(cudaMemcpyAsync(s->d_seg_nrhs, s->h_nrhs, sizeof(int32_t) * ns, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->d_seg_voff, s->h_voff, sizeof(int64_t) * ns, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s->d_cnt, 0, sizeof(unsigned long long) * ns, st));
+    const DevSegs g = seg_view(s);
     CK(cudaEventRecord(c->e0, st));
-    int worst = SOG_OK;
-    for (int c0 = 0; c0 < nrhs; c0 += 64) {
-        const int nc = std::min(64, nrhs - c0);
+    for (int c0 = 0; c0 < maxr; c0 += 64) {
+        const int nc = std::min(64, maxr - c0);
         s->launches++;
-        gather_rhs_launch(b_dev + (size_t)c0 * s->n, s->d_n2o, s->n, s->n_ext, nc, s->d_bext, st);
-        r = solve_chunk(s, nc, stats);
-        if (r && r != SOG_ENOCONV) return r;
-        if (r) worst = r;
+        gather_seg_launch(b_dev, g, s->n_ext, c0, nc, s->d_bext, st);
+        r = solve_chunk(s, c0, nc, out);
+        if (r) return r;
         s->launches++;
-        scatter_solution_launch(s->d_xext, s->d_o2n, s->n, nc, x_dev + (size_t)c0 * s->n, st);
+        scatter_seg_launch(s->d_xext, g, s->n_ext, c0, nc, x_dev, s->d_cnt, st);
     }
     CK(cudaEventRecord(c->e1, st));
-    s->launches++;
-    count_nonfinite_launch(x_dev, (int64_t)s->n * nrhs, s->d_cnt, st);
-    unsigned long long bad = 0;
-    CK(cudaMemcpyAsync(&bad, s->d_cnt, sizeof(bad), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaEventElapsedTime(&s->t_solve, c->e0, c->e1));
-    if (stats) {
-        stats->nan_count = (int64_t)bad;
-        stats->status = worst;
+    int worst = SOG_OK;
+    for (size_t k = 0; k < ns; k++) {
+        out[k].nan_count = (int64_t)s->h_cnt[k];
+        if (out[k].nan_count) out[k].status = SOG_ENAN;
+        if (out[k].status == SOG_ENAN) worst = SOG_ENAN;
+        else if (out[k].status && !worst) worst = out[k].status;
+        if (agg) {
+            agg->iterations = std::max(agg->iterations, out[k].iterations);
+            if (!(out[k].rel_resid <= agg->rel_resid)) agg->rel_resid = out[k].rel_resid;
+            if (!(out[k].backward_error <= agg->backward_error)) agg->backward_error = out[k].backward_error;
+            agg->nan_count += out[k].nan_count;
+        }
     }
-    if (bad) return fail(SOG_ENAN, "non-finite values in the solution");
+    s->seg_stats = out;
+    if (agg) agg->status = worst;
+    if (worst == SOG_ENAN) return fail(SOG_ENAN, "non-finite values in the solution");
     if (worst) return fail(worst, "iterative refinement did not reach the tolerance");
     return SOG_OK;
+}
+
+int64_t solve_values(const sog_system* s, const int32_t* nrhs) {
+    int64_t t = 0;
+    for (size_t k = 0; k < s->segs.size(); k++) t += (int64_t)nrhs[k] * s->segs[k].n;
+    return t;
+}
+
+// host b / x through pool staging buffers
+int solve_host(sog_system* s, const int32_t* nrhs, const double* b, double* x, sog_solve_stats* agg) {
+    sog_ctx* c = s->ctx;
+    const uint64_t bytes = sizeof(double) * (uint64_t)solve_values(s, nrhs);
+    if (bytes == 0) return solve_device_impl(s, nrhs, nullptr, nullptr, agg);
+    double* db = static_cast<double*>(c->pool.alloc(bytes));
+    double* dx = static_cast<double*>(c->pool.alloc(bytes));
+    if (!db || !dx) {
+        c->pool.release(db, bytes);
+        c->pool.release(dx, bytes);
+        return fail(SOG_ENOMEM, "block pool exhausted (rhs)");
+    }
+    int r = SOG_OK;
+    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        r = fail(SOG_ECUDA, "rhs upload failed");
+    if (!r) {
+        r = solve_device_impl(s, nrhs, db, dx, agg);
+        if (!r || r == SOG_ENOCONV || r == SOG_ENAN) {
+            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)
+                r = fail(SOG_ECUDA, "download failed");
+        }
+    }
+    c->pool.release(db, bytes);
+    c->pool.release(dx, bytes);
+    return r;
 }
 
 }  // namespace
@@ -452,8 +567,7 @@ int sog_ctx_create(int32_t device, uint64_t pool_bytes, sog_ctx** out) {
     sog_ctx* c = new sog_ctx();
     c->device = device;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess ||
-        cudaMallocHost(&c->host_red, sizeof(double) * RED * 64) != cudaSuccess) {
+        cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess) {
         delete c;
         return fail(SOG_ECUDA, "context set-up failed");
     }
@@ -470,7 +584,6 @@ void sog_ctx_destroy(sog_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     c->pool.destroy();
-    if (c->host_red) cudaFreeHost(c->host_red);
     if (c->e0) cudaEventDestroy(c->e0);
     if (c->e1) cudaEventDestroy(c->e1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -570,6 +683,27 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (int i = 0; i < s->R; i++) { lptr[i + 1] += lptr[i]; uptr[i + 1] += uptr[i]; }
     HostCSR hc;
     if (!plan->imported) hc = build_csr(p);
+    // systems: a plain plan is one system over all block rows
+    if (p.segs.empty()) {
+        Segment sg;
+        sg.n = p.cfg.n;
+        sg.R = p.cfg.block_rows;
+        sg.ntrip = (int64_t)p.scatter_tile.size();
+        s->segs.push_back(sg);
+    } else {
+        s->segs = p.segs;
+    }
+    const size_t ns = s->segs.size();
+    std::vector<int32_t> seg_brow(s->R), seg_n(ns), n2o(s->n_ext, -1);
+    for (size_t k = 0; k < ns; k++) {
+        const Segment& sg = s->segs[k];
+        seg_n[k] = sg.n;
+        for (int r = 0; r < sg.R; r++) seg_brow[sg.row0 / 64 + r] = (int32_t)k;
+    }
+    if (p.segs.empty())
+        for (int i = 0; i < p.cfg.n; i++) n2o[i] = p.ord.new_to_old[i];
+    else
+        n2o = p.ord.new_to_old;
     // task arrays
     std::vector<int32_t> parts32(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) parts32[t] = g.parts[t];
@@ -594,8 +728,9 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_ccol = L.add<int32_t>(hc.col.size()), o_cval = L.add<double>(hc.val.size()),
              o_cpos = L.add<int32_t>(hc.pos.size()), o_sct = L.add<int32_t>(p.scatter_tile.size()),
              o_sco = L.add<int16_t>(p.scatter_off.size()), o_pdt = L.add<int32_t>(p.pad_tile.size()),
-             o_pdo = L.add<int16_t>(p.pad_off.size()), o_n2o = L.add<int32_t>(p.ord.new_to_old.size()),
-             o_o2n = L.add<int32_t>(p.ord.old_to_new.size()), o_V = L.add<double>(s->ntrip);
+             o_pdo = L.add<int16_t>(p.pad_off.size()), o_n2o = L.add<int32_t>(n2o.size()),
+             o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
+             o_V = L.add<double>(s->ntrip);
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
     if (!s->tiles) {
@@ -669,8 +804,18 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         s->d_pad_tile = put(A, o_pdt, p.pad_tile, st);
         s->d_pad_off = put(A, o_pdo, p.pad_off, st);
     }
-    s->d_n2o = put(A, o_n2o, p.ord.new_to_old, st);
-    s->d_o2n = put(A, o_o2n, p.ord.old_to_new, st);
+    s->d_n2o = put(A, o_n2o, n2o, st);
+    s->d_seg_brow = put(A, o_sbr, seg_brow, st);
+    s->d_seg_n = put(A, o_sn, seg_n, st);
+    if (cudaMallocHost(&s->h_red, sizeof(double) * RED * 64 * ns) != cudaSuccess ||
+        cudaMallocHost(&s->h_nrhs, sizeof(int32_t) * ns) != cudaSuccess ||
+        cudaMallocHost(&s->h_active, sizeof(int32_t) * ns) != cudaSuccess ||
+        cudaMallocHost(&s->h_voff, sizeof(int64_t) * ns) != cudaSuccess ||
+        cudaMallocHost(&s->h_cnt, sizeof(unsigned long long) * ns) != cudaSuccess) {
+        cudaGetLastError();
+        sog_system_destroy(s);
+        return fail(SOG_ENOMEM, "pinned host buffers");
+    }
     s->d_V = reinterpret_cast<double*>(A + o_V);
     s->grid_factor = factor_persistent_grid(s->fp64, c->num_sms);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
@@ -691,6 +836,11 @@ void sog_system_destroy(sog_system* s) {
     c->pool.release(s->aux, s->aux_bytes);
     c->pool.release(s->vecs, s->vec_bytes);
     c->pool.release(s->trace, s->trace_bytes);
+    if (s->h_red) cudaFreeHost(s->h_red);
+    if (s->h_nrhs) cudaFreeHost(s->h_nrhs);
+    if (s->h_active) cudaFreeHost(s->h_active);
+    if (s->h_voff) cudaFreeHost(s->h_voff);
+    if (s->h_cnt) cudaFreeHost(s->h_cnt);
     delete s;
 }
 
@@ -746,35 +896,38 @@ int sog_solve_device(sog_system* s, int32_t nrhs, const double* b_dev, double* x
     if (!s || nrhs <= 0 || !b_dev || !x_dev) return fail(SOG_EINVAL, "bad argument");
     if (!s->factored) return fail(SOG_ESTATE, "solve before factor");
     CK(cudaSetDevice(s->ctx->device));
-    return solve_device_impl(s, nrhs, b_dev, x_dev, stats);
+    std::vector<int32_t> k(s->segs.size(), nrhs);
+    return solve_device_impl(s, k.data(), b_dev, x_dev, stats);
 }
 
 int sog_solve(sog_system* s, int32_t nrhs, const double* b, double* x, sog_solve_stats* stats) {
     if (!s || nrhs <= 0 || !b || !x) return fail(SOG_EINVAL, "bad argument");
     if (!s->factored) return fail(SOG_ESTATE, "solve before factor");
-    sog_ctx* c = s->ctx;
-    CK(cudaSetDevice(c->device));
-    const uint64_t bytes = sizeof(double) * (uint64_t)s->n * nrhs;
-    double* db = static_cast<double*>(c->pool.alloc(bytes));
-    double* dx = static_cast<double*>(c->pool.alloc(bytes));
-    if (!db || !dx) {
-        c->pool.release(db, bytes);
-        c->pool.release(dx, bytes);
-        return fail(SOG_ENOMEM, "block pool exhausted (rhs)");
-    }
-    int r = SOG_OK;
-    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
-        r = fail(SOG_ECUDA, "rhs upload failed");
-    if (!r || r == SOG_ENOCONV) {
-        r = solve_device_impl(s, nrhs, db, dx, stats);
-        if (!r || r == SOG_ENOCONV || r == SOG_ENAN) {
-            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-                cudaStreamSynchronize(c->stream) != cudaSuccess)
-                r = fail(SOG_ECUDA, "download failed");
-        }
-    }
-    c->pool.release(db, bytes);
-    c->pool.release(dx, bytes);
+    CK(cudaSetDevice(s->ctx->device));
+    std::vector<int32_t> k(s->segs.size(), nrhs);
+    return solve_host(s, k.data(), b, x, stats);
+}
+
+int sog_solve_batch(sog_system* s, const int32_t* nrhs, const double* b, double* x, sog_solve_stats* stats) {
+    if (!s || !nrhs) return fail(SOG_EINVAL, "bad argument");
+    if (!s->factored) return fail(SOG_ESTATE, "solve before factor");
+    if (solve_values(s, nrhs) > 0 && (!b || !x)) return fail(SOG_EINVAL, "NULL b or x");
+    CK(cudaSetDevice(s->ctx->device));
+    const int r = solve_host(s, nrhs, b, x, nullptr);
+    if (stats && s->seg_stats.size() == s->segs.size())
+        std::memcpy(stats, s->seg_stats.data(), sizeof(sog_solve_stats) * s->segs.size());
+    return r;
+}
+
+int sog_solve_batch_device(sog_system* s, const int32_t* nrhs, const double* b_dev, double* x_dev,
+                           sog_solve_stats* stats) {
+    if (!s || !nrhs) return fail(SOG_EINVAL, "bad argument");
+    if (!s->factored) return fail(SOG_ESTATE, "solve before factor");
+    if (solve_values(s, nrhs) > 0 && (!b_dev || !x_dev)) return fail(SOG_EINVAL, "NULL b or x");
+    CK(cudaSetDevice(s->ctx->device));
+    const int r = solve_device_impl(s, nrhs, b_dev, x_dev, nullptr);
+    if (stats && s->seg_stats.size() == s->segs.size())
+        std::memcpy(stats, s->seg_stats.data(), sizeof(sog_solve_stats) * s->segs.size());
     return r;
 }
 

@@ -280,25 +280,79 @@ __global__ void axpy_kernel(const float* __restrict__ d, double* __restrict__ x,
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = assign ? (double)d[i] : x[i] + (double)d[i];
 }
-__global__ void gather_kernel(const double* __restrict__ b, const int32_t* __restrict__ n2o, int n, int n_ext,
-                              int nrhs, double* __restrict__ out) {
+// one thread per (permuted row, column) of the chunk; systems are whole
+// 64-row block rows, so the system lookup is one load per row
+__global__ void gather_seg_kernel(const double* __restrict__ b, DevSegs g, int n_ext, int c0, int nc,
+                                  double* __restrict__ out) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (int64_t)n_ext * nrhs) return;
-    const int i = (int)(e / nrhs), c = (int)(e - (int64_t)i * nrhs);
-    out[e] = i < n ? b[(size_t)c * n + n2o[i]] : 1.0;
+    if (e >= (int64_t)n_ext * nc) return;
+    const int i = (int)(e / nc), c = (int)(e - (int64_t)i * nc), col = c0 + c;
+    const int k = g.of_brow[i >> 6], o = g.n2o[i];
+    double v = 1.0;
+    if (o >= 0) v = col < g.nrhs[k] ? b[g.voff[k] + (int64_t)col * g.n[k] + o] : 0.0;
+    out[e] = v;
 }
-__global__ void scatter_kernel(const double* __restrict__ xe, const int32_t* __restrict__ o2n, int n, int nrhs,
-                               double* __restrict__ x) {
+__global__ void scatter_seg_kernel(const double* __restrict__ xe, DevSegs g, int n_ext, int c0, int nc,
+                                   double* __restrict__ x, unsigned long long* cnt) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (int64_t)n * nrhs) return;
-    const int c = (int)(e / n), i = (int)(e - (int64_t)c * n);
-    x[e] = xe[(size_t)o2n[i] * nrhs + c];
+    if (e >= (int64_t)n_ext * nc) return;
+    const int i = (int)(e / nc), c = (int)(e - (int64_t)i * nc), col = c0 + c;
+    const int k = g.of_brow[i >> 6], o = g.n2o[i];
+    if (o < 0 || col >= g.nrhs[k]) return;
+    const double v = xe[e];
+    x[g.voff[k] + (int64_t)col * g.n[k] + o] = v;
+    if (!isfinite(v)) atomicAdd(cnt + k, 1ull);
 }
-__global__ void nonfinite_kernel(const double* __restrict__ x, int64_t n, unsigned long long* cnt) {
-    unsigned long long local = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        if (!isfinite(x[i])) local++;
-    if (local) atomicAdd(cnt, local);
+// as residual_kernel, reductions per (system, column): a warp's 32 rows lie
+// in one 64-row block row, so each warp reduces into one system's slots
+__global__ void residual_seg_kernel(DevCSR A, const double* __restrict__ b, const double* __restrict__ x,
+                                    double* __restrict__ r, int c0, int nc, double* red, DevSegs g) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row - (threadIdx.x & 31) >= A.n) return;  // whole warp past the end (A.n is a multiple of 64)
+    const int lane = threadIdx.x & 31;
+    const int k = g.of_brow[row >> 6];
+    const bool real = g.n2o[row] >= 0;
+    double rowabs = 0;
+    if (real)
+        for (int q = A.ptr[row]; q < A.ptr[row + 1]; q++) rowabs += fabs(A.val[q]);
+    for (int o = 16; o > 0; o >>= 1) rowabs = fmax(rowabs, __shfl_xor_sync(0xffffffffu, rowabs, o));
+    const int creal = min(nc, g.nrhs[k] - c0);  // columns of this chunk that system k has
+    for (int c = 0; c < nc; c++) {
+        double acc = 0;
+        for (int q = A.ptr[row]; q < A.ptr[row + 1]; q++) acc += A.val[q] * x[(size_t)A.col[q] * nc + c];
+        const double bv = b[(size_t)row * nc + c];
+        const double rv = bv - acc;
+        r[(size_t)row * nc + c] = rv;
+        if (c >= creal) continue;  // warp-uniform
+        double rr = 0, bb = 0, ar = 0, ax = 0, ab = 0;
+        if (real) {
+            rr = rv * rv; bb = bv * bv; ar = fabs(rv); ax = fabs(x[(size_t)row * nc + c]); ab = fabs(bv);
+        }
+        rr = warp_sum(rr);
+        bb = warp_sum(bb);
+        for (int o = 16; o > 0; o >>= 1) {
+            ar = fmax(ar, __shfl_xor_sync(0xffffffffu, ar, o));
+            ax = fmax(ax, __shfl_xor_sync(0xffffffffu, ax, o));
+            ab = fmax(ab, __shfl_xor_sync(0xffffffffu, ab, o));
+        }
+        if (lane == 0) {
+            double* rd = red + ((size_t)k * nc + c) * RED;
+            atomicAdd(rd + 0, rr);
+            atomicAdd(rd + 1, bb);
+            atomic_max_nonneg(rd + 2, ar);
+            atomic_max_nonneg(rd + 3, ax);
+            atomic_max_nonneg(rd + 4, ab);
+            atomic_max_nonneg(rd + 5, rowabs);
+        }
+    }
+}
+__global__ void cast_seg_kernel(const double* __restrict__ src, float* __restrict__ dst, int n_ext, int nc,
+                                DevSegs g) {
+    const int64_t tot = (int64_t)n_ext * nc;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / nc);
+        dst[e] = g.active[g.of_brow[i >> 6]] ? (float)src[e] : 0.0f;
+    }
 }
 
 }  // namespace
@@ -343,20 +397,22 @@ void cast_f64_to_f32_launch(const double* src, float* dst, int64_t n, cudaStream
 void axpy_f32_to_f64_launch(const float* d, double* x, int64_t n, int assign, cudaStream_t s) {
     if (n > 0) axpy_kernel<<<608, 256, 0, s>>>(d, x, n, assign);
 }
-void gather_rhs_launch(const double* b, const int32_t* new_to_old, int n, int n_ext, int nrhs, double* out,
-                       cudaStream_t s) {
-    const int64_t tot = (int64_t)n_ext * nrhs;
-    gather_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(b, new_to_old, n, n_ext, nrhs, out);
+void gather_seg_launch(const double* b, const DevSegs& g, int n_ext, int c0, int nc, double* out, cudaStream_t s) {
+    const int64_t tot = (int64_t)n_ext * nc;
+    if (tot > 0) gather_seg_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(b, g, n_ext, c0, nc, out);
 }
-void scatter_solution_launch(const double* xe, const int32_t* old_to_new, int n, int nrhs, double* x,
-                             cudaStream_t s) {
-    const int64_t tot = (int64_t)n * nrhs;
-    scatter_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(xe, old_to_new, n, nrhs, x);
+void scatter_seg_launch(const double* xe, const DevSegs& g, int n_ext, int c0, int nc, double* x,
+                        unsigned long long* cnt, cudaStream_t s) {
+    const int64_t tot = (int64_t)n_ext * nc;
+    if (tot > 0) scatter_seg_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(xe, g, n_ext, c0, nc, x, cnt);
 }
-int count_nonfinite_launch(const double* x, int64_t n, unsigned long long* counter, cudaStream_t s) {
-    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
-    if (n > 0) nonfinite_kernel<<<304, 256, 0, s>>>(x, n, counter);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+void residual_seg_launch(const DevCSR& A, const double* b, const double* x, double* r, int c0, int nc,
+                         double* red, const DevSegs& g, cudaStream_t s) {
+    cudaMemsetAsync(red, 0, sizeof(double) * RED * nc * g.nseg, s);
+    residual_seg_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A, b, x, r, c0, nc, red, g);
+}
+void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s) {
+    if ((int64_t)n_ext * nc > 0) cast_seg_kernel<<<608, 256, 0, s>>>(src, dst, n_ext, nc, g);
 }
 
 // ---------------------------------------------------------------- allocation-free residual check

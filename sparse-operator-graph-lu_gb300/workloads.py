@@ -34,7 +34,9 @@ class System:
             y = np.zeros(self.n)
             np.add.at(y, self.rows, self.vals * x[self.cols])
             return y
-        return np.stack([self.matvec(xi) for xi in x])
+        import scipy.sparse as sp
+        a = sp.csr_matrix((self.vals, (self.rows, self.cols)), shape=(self.n, self.n))
+        return np.ascontiguousarray((a @ x.T).T)
 
     def to_scipy(self):
         import scipy.sparse as sp
@@ -66,9 +68,10 @@ def lap2d(side: int = 128, diag: float = 4.01, seed: int = 0) -> System:
     return _finish(n, np.concatenate(r), np.concatenate(c), np.concatenate(v), x_true, f"lap2d_{side}")
 
 
-def lap3d(side: int = 64, diag: float = 6.01, seed: int = 0) -> System:
+def lap3d(side: int = 64, diag: float = 6.01, seed: int = 0, nrhs: int = 1) -> System:
     """3D 7-point Laplacian on side^3; diagonal `diag`, off-diagonals -1;
-    x_true ~ U[-1, 1] from default_rng(seed)."""
+    x_true ~ U[-1, 1] from default_rng(seed): shape (n,) for one right-hand
+    side, (nrhs, n) otherwise; b = A x_true column by column."""
     n = side ** 3
     idx = np.arange(n).reshape(side, side, side)
     r = [idx.ravel()]
@@ -81,7 +84,8 @@ def lap3d(side: int = 64, diag: float = 6.01, seed: int = 0) -> System:
         hi[ax] = slice(1, side)
         a, b_ = idx[tuple(lo)].ravel(), idx[tuple(hi)].ravel()
         r += [a, b_]; c += [b_, a]; v += [np.full(a.size, -1.0)] * 2
-    x_true = np.random.default_rng(seed).uniform(-1.0, 1.0, n)
+    shape = n if nrhs == 1 else (nrhs, n)
+    x_true = np.random.default_rng(seed).uniform(-1.0, 1.0, shape)
     return _finish(n, np.concatenate(r), np.concatenate(c), np.concatenate(v), x_true, f"lap3d_{side}")
 
 
