@@ -10,8 +10,13 @@ right-hand side. Host planning (ordering + DAG) happens once before timing,
 as the symbolic analysis does.
 
 Other workloads: lap64 = 3D 7-point Laplacian 64^3 (n = 262,144, 7.1M unit
-ops) with 64 right-hand sides (x_true ~ U[-1,1] seed 0); var24 = the var-coef
-system on 24^3, a small case of the same kernels for profiler captures.
+ops) with 64 right-hand sides (x_true ~ U[-1,1] seed 0); batch1024 = 1,024
+independent 2D convection-diffusion systems (side ~ U{16..96}, cell Peclet ~
+U[0,10], angle ~ U[0,2pi), 5-point upwind, 4 N(0,1) right-hand sides each),
+merged into one batch plan and factored in one executor launch per step;
+var24 = the var-coef system on 24^3, a small case of the same kernels for
+profiler captures. A "solve" is one system factored and solved for all its
+right-hand sides.
 
   value   mixed precision (FP32 factors, 3xTF32 tile products, FP64
           refinement), inputs resident in HBM, solves/s over all ranks
@@ -45,7 +50,43 @@ WORKLOADS = {
     "var48": "3D 7-point var-coef diffusion 48^3 (n=110592, nnz=760320), 1 RHS, factor+solve to rel resid<=1e-10",
     "lap64": "3D 7-point Laplacian 64^3 (n=262144, nnz=1810432), 64 RHS, factor+solve to rel resid<=1e-10",
     "var24": "3D 7-point var-coef diffusion 24^3 (n=13824, nnz=93312), 1 RHS, factor+solve to rel resid<=1e-10",
+    "serving": "serving stream: Poisson arrivals, random band systems n log-uniform [2000, 200000], 3-27 nnz/row "
+               "within half-band 0.02n, diag 1.1 x row abs sum, 1-16 RHS; continuous batching, pool admission",
+    "batch1024": "1,024 nonsymmetric 2D conv-diff systems (side U{16..96}, n 256-9216, Pe U[0,10]), 4 RHS each, "
+                 "one batch plan, one factor launch per step, factor+solve to rel resid<=1e-10 per system",
 }
+
+
+class Work:
+    """A benchmark workload: its systems, the plan the executor runs (a batch
+    plan for several systems) and the flat value / right-hand-side arrays in
+    the C-ABI layout (per system, rhs-major, concatenated)."""
+
+    def __init__(self, name: str, sg):
+        self.name = name
+        self.desc = WORKLOADS[name]
+        self.systems = make_workload(name)
+        t0 = time.perf_counter()
+        self.plans = [sg.Plan(s.n, s.rows, s.cols, s.vals) for s in self.systems]
+        self.plan = self.plans[0] if len(self.plans) == 1 else sg.merge_plans(self.plans)
+        self.t_plan = time.perf_counter() - t0
+        s0 = self.systems[0]
+        self.nrhs = 1 if s0.b.ndim == 1 else s0.b.shape[0]
+        self.vals = np.concatenate([s.vals for s in self.systems])
+        self.b = np.concatenate([s.b.ravel() for s in self.systems])
+        self.count = len(self.systems)
+        self.nnz = int(self.vals.size)
+        self.n = int(sum(s.n for s in self.systems))
+        self.flops = sum(algorithmic_flops(p.info.op_count) for p in self.plans)
+
+    def split(self, x):
+        out, o = [], 0
+        for s in self.systems:
+            m = s.n * self.nrhs
+            out.append(x[o:o + m].reshape(s.b.shape))
+            o += m
+        return out
+
 
 
 def load_package():
@@ -70,8 +111,16 @@ def make_workload(name: str):
     load_package()
     import soglu_gb300.workloads as wl
     if name == "lap64":
-        return wl.lap3d(64, nrhs=64)
-    return wl.varcoef3d(24 if name == "var24" else 48)
+        return [wl.lap3d(64, nrhs=64)]
+    if name == "batch1024":
+        return wl.convdiff_batch(1024)
+    return [wl.varcoef3d(24 if name == "var24" else 48)]
+
+
+# DRAM bytes (read + write) of one mixed factor launch, from a one-pass ncu
+# capture of the full-size launch (dram__bytes_read.sum + dram__bytes_write.sum:
+# 421.45 MB + 3.83 GB at var48); None where no capture covers the workload
+TRAFFIC: dict = {"var48": 421.45e6 + 3.83e9}
 
 
 def algorithmic_flops(op_count) -> float:
@@ -173,13 +222,104 @@ def measure_peaks(torch, device) -> dict:
     return out
 
 
-def cpu_oracle_step(plan_export, s, threads: int):
+def cpu_sample(work, sg, threads: int, budget_s: float = 15.0):
+    """The oracle (C restatement of the reference's calculate + solve) on the
+    host cores: whole systems in order, each factored once and solved for its
+    right-hand sides, until about budget_s seconds of work. Returns (systems
+    done, seconds, worst relative residual)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    perm, ops, L, U, block_rows, storage, tiles_in = plan_export
+    done, t_tot, worst = 0, 0.0, 0.0
+    for s, p in zip(work.systems, work.plans):
+        perm, ops, L, U = p.export()
+        tiles_in = p.input_tiles(s.vals)
+        t0 = time.perf_counter()
+        X = oracle.solve_system_multi(perm, s.n, p.info.block_rows, ops, p.info.storage_count, tiles_in, L, U,
+                                      s.b, threads=threads)
+        t_tot += time.perf_counter() - t0
+        done += 1
+        B = np.atleast_2d(s.b)
+        worst = max(worst, float(np.linalg.norm(B - np.atleast_2d(s.matvec(X))) / np.linalg.norm(B)))
+        if t_tot >= budget_s:
+            break
+    return done, t_tot, worst
+
+
+def run_serving(args):
+    """Serving stream (sog_server_*): requests arrive as a Poisson process at
+    each rate of the sweep; each is planned on host threads, admitted by free
+    pool memory, merged with whatever else is ready into shared launches,
+    answered and released. Latency = submit -> answer (host clock);
+    throughput = requests answered / (last answer - first arrival)."""
+    import threading
+    import torch
+    torch.cuda.set_device(0)
+    build_native()
+    sg = load_package()
+    import soglu_gb300.workloads as wl
+    rng = np.random.default_rng(17)
+    spec = wl.serving_requests(args.requests, seed=3)
     t0 = time.perf_counter()
-    x, _, _ = oracle.solve_system(perm, s.n, block_rows, ops, storage, tiles_in, L, U, s.b, threads=threads)
-    return time.perf_counter() - t0, x
+    systems = [wl.random_band(n, seed=sd, nrhs=k) for n, sd, k in spec]
+    t_gen = time.perf_counter() - t0
+    ctx = sg.Context(0)
+    rates = [float(r) for r in args.rates.split(",")]
+    sweep = []
+    for prec_name, prec in (("mixed", sg.MIXED), ("fp64", sg.FP64)):
+        if prec_name == "fp64" and not args.serving_fp64:
+            continue
+        for lam in (rates if prec_name == "mixed" else rates[-1:]):
+            srv = sg.Server(ctx, precision=prec, planners=args.planners, omp_threads=max(1, (os.cpu_count() or 2)
+                                                                                        // args.planners))
+            gaps = rng.exponential(1.0 / lam, len(systems))
+            arrivals = np.cumsum(gaps) - gaps[0]
+            ids = [None] * len(systems)
+            t_start = time.perf_counter()
+
+            def submitter():
+                for k, s in enumerate(systems):
+                    d = t_start + arrivals[k] - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    ids[k] = srv.submit(s.n, s.rows, s.cols, s.vals, s.b)
+
+            th = threading.Thread(target=submitter)
+            th.start()
+            lat, worst, stat_bad, t_last, infos = [], 0.0, 0, t_start, []
+            for k, s in enumerate(systems):
+                while ids[k] is None:
+                    time.sleep(0.001)
+                x, info = srv.wait(ids[k], allow_noconv=True)
+                t_last = max(t_last, time.perf_counter())
+                srv.release(ids[k])
+                lat.append(info["total_ms"])
+                infos.append(info)
+                if info["status"] != sg.SOG_OK:
+                    stat_bad += 1
+                worst = max(worst, info["rel_resid"])
+            th.join()
+            wall = t_last - t_start
+            c = srv.counters()
+            srv.close()
+            sweep.append({"precision": prec_name, "rate_per_s": lam, "requests": len(systems),
+                          "throughput_per_s": len(systems) / wall, "wall_s": wall,
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                          "mean_plan_ms": float(np.mean([i["plan_ms"] for i in infos])),
+                          "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])),
+                          "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i in infos])),
+                          "batches": c["batches"], "largest_batch": c["max_batch"],
+                          "worst_rel_resid": worst, "not_ok": stat_bad})
+    ctx.close()
+    top = [r for r in sweep if r["precision"] == "mixed"][-1]
+    line = {"metric": METRIC, "value": top["throughput_per_s"], "unit": "requests/s", "n_gpus": 1,
+            "steps": len(systems), "warmup": 0, "ms_per_step": 1e3 * top["wall_s"] / len(systems),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic", "config": {"workload": WORKLOADS["serving"], "requests": len(systems),
+                                            "rates_per_s": rates, "planner_threads": args.planners,
+                                            "n": [int(s.n) for s in systems]},
+            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep, "generate_s": t_gen}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def run_reference(args):
@@ -192,36 +332,45 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU executor restatement keeps every 64^3 tile "
                           "resident (50 GB of host memory, no free-after-last-use); run the default workload"}))
         return 0
-    s = make_workload(args.workload)
-    plan = sg.Plan(s.n, s.rows, s.cols, s.vals)
-    perm, ops, L, U = plan.export()
-    exp = (perm, ops, L, U, plan.info.block_rows, plan.info.storage_count, plan.input_tiles(s.vals))
+    if args.workload == "serving":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference solves one system per process and has "
+                          "no request loop; its per-system CPU rate is the default workload's reference line"}))
+        return 0
+    work = Work(args.workload, sg)
     cores = os.cpu_count() or 1
+    # each step a bounded sample: the whole system (single-system workloads)
+    # or as many of the batch's systems as fit in the budget
+    budget = 1e9 if work.count == 1 else 6.0
     for _ in range(args.warmup):
-        cpu_oracle_step(exp, s, cores)
-    times = []
+        cpu_sample(work, sg, cores, budget)
+    times, worst, done = [], 0.0, 0
     for _ in range(args.steps):
-        dt, x = cpu_oracle_step(exp, s, cores)
-        times.append(dt)
+        d, dt, w = cpu_sample(work, sg, cores, budget)
+        times.append(dt / d * work.count)  # seconds for the whole workload at the sampled rate
+        worst = max(worst, w)
+        done = d
     tot = sum(times)
-    v = args.steps / tot
-    rr = float(np.linalg.norm(s.b - s.matvec(x)) / np.linalg.norm(s.b))
+    v = args.steps * work.count / tot
+    sample = (f"{args.steps} full factor+solve steps of the {args.workload} system" if work.count == 1 else
+              f"per step the first {done} of the {work.count} systems, factor + {work.nrhs} solves each, "
+              f"rate scaled to the whole batch")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "precision": "fp64 CPU", "parallelism": "host cores"},
-            "rel_resid": rr,
+            "config": {"workload": work.desc, "precision": "fp64 CPU", "parallelism": "host cores"},
+            "rel_resid": worst,
             "p50_ms": 1e3 * statistics.median(times), "p99_ms": 1e3 * max(times),
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full factor+solve steps of the {args.workload} system (the reference's "
-                                       "AVX-512 kernels do not compile on the aarch64 host; the C restatement "
-                                       "of its executor path, pinned to the reference's outputs, is timed)"},
+                             "sample": sample + " (the reference's AVX-512 kernels do not compile on the aarch64 "
+                                       "host; the C restatement of its executor path, pinned to the reference's "
+                                       "outputs, is timed)"},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 def run_ours(args):
+    import ctypes
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -231,21 +380,34 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     build_native()
     sg = load_package()
-    s = make_workload(args.workload)
-    nrhs = 1 if s.b.ndim == 1 else s.b.shape[0]
-    t0 = time.perf_counter()
-    plan = sg.Plan(s.n, s.rows, s.cols, s.vals)
-    t_plan = time.perf_counter() - t0
+    work = Work(args.workload, sg)
+    plan = work.plan
     info = plan.info
-    flops = algorithmic_flops(info.op_count)
+    flops = work.flops
+    nrhs = work.nrhs
     ctx = sg.Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream())
-    V = torch.from_numpy(s.vals).to(dev)
-    b = torch.from_numpy(s.b).to(dev)
+    V = torch.from_numpy(work.vals).to(dev)
+    b = torch.from_numpy(work.b).to(dev)
     x = torch.empty_like(b)
     torch.cuda.synchronize()
+    L = sg.lib()
+    # host buffers for the end-to-end leg: pinned, C-ABI calls with host pointers
+    hv = torch.from_numpy(work.vals).pin_memory()
+    hb = torch.from_numpy(work.b).pin_memory()
+    hx = torch.empty_like(hb).pin_memory()
 
-    def timed(sysm, steps, warmup, host=None):
+    def step(sysm, host):
+        if not host:
+            sysm.factor_device(V.data_ptr())
+            return sysm.solve_device(nrhs, b.data_ptr(), x.data_ptr())
+        st = sg.SolveStats()
+        sg._check(L.sog_factor(sysm._h, ctypes.c_void_p(hv.data_ptr())))
+        sg._check(L.sog_solve(sysm._h, nrhs, ctypes.c_void_p(hb.data_ptr()), ctypes.c_void_p(hx.data_ptr()),
+                              ctypes.byref(st)))
+        return st.as_dict()
+
+    def timed(sysm, steps, warmup, host=False):
         lat, fms, sms, iters, st = [], [], [], [], None
         for _ in range(warmup):
             step(sysm, host)
@@ -270,22 +432,11 @@ def run_ours(args):
         return {"ms": max_over_ranks(ms, world, dev), "lat": lat, "factor_ms": fms, "solve_ms": sms,
                 "iters": iters, "stats": st, "clocks": clocks, "launches": sysm.task_info()["launches"] - l0}
 
-    def step(sysm, host):
-        if host is None:
-            sysm.factor_device(V.data_ptr())
-            return sysm.solve_device(nrhs, b.data_ptr(), x.data_ptr())
-        hv, hb = host
-        sysm.factor(hv)
-        xs, st = sysm.solve(hb)
-        return st
-
     mixed = sg.System(ctx, plan, precision=sg.MIXED, max_refine=20, tol=1e-10)
     rm = timed(mixed, args.steps, args.warmup)
     x_mixed = x.cpu().numpy()
-    # end to end through the C ABI with host buffers (pinned)
-    hv = torch.from_numpy(s.vals).pin_memory().numpy()
-    hb = torch.from_numpy(s.b).pin_memory().numpy()
-    re2e = timed(mixed, args.steps, args.warmup, host=(hv, hb))
+    re2e = timed(mixed, args.steps, args.warmup, host=True)
+    x_e2e = hx.numpy().copy()
     mixed.close()
     fp64 = sg.System(ctx, plan, precision=sg.FP64)
     k64 = max(3, args.steps // 3)
@@ -294,11 +445,10 @@ def run_ours(args):
     ti = fp64.task_info()
     fp64.close()
 
-    total = args.steps * world
+    total = args.steps * work.count * world
     value = total / (rm["ms"] * 1e-3)
     e2e_value = total / (re2e["ms"] * 1e-3)
-    v64 = k64 * world / (r64["ms"] * 1e-3)
-    line = None
+    v64 = k64 * work.count * world / (r64["ms"] * 1e-3)
     if rank == 0:
         peaks = measure_peaks(torch, dev)
         fm = statistics.mean(rm["factor_ms"])
@@ -310,50 +460,59 @@ def run_ours(args):
         ach = flops / (fm * 1e-3) / 1e12
         roof = {"bound": "tensor", "kernel": "factor_persistent_kernel<float> (3xTF32 tile products + LU/inverse "
                                                 "tasks, one launch per factorisation)",
-                "achieved": ach, "peak": eff_peak, "unit": "TFLOP/s", "frac": ach / eff_peak, "traffic": None,
+                "achieved": ach, "peak": eff_peak, "unit": "TFLOP/s", "frac": ach / eff_peak,
+                "traffic": TRAFFIC.get(args.workload),
                 "peak_source": f"cuBLAS TF32 GEMM measured in this run ({peaks['tf32_tflops']:.1f} TFLOP/s) / 3",
                 "algorithmic_flop_per_launch": flops, "avg_launch_ms": fm}
         fp64_roof = {"achieved": flops / (f64m * 1e-3) / 1e12, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                      "frac": flops / (f64m * 1e-3) / 1e12 / peaks["fp64_tflops"],
                      "peak_source": "cuBLAS DGEMM measured in this run", "avg_factor_ms": f64m}
         cpu = None
-        if world == 1 and nrhs == 1 and not args.no_cpu_baseline:
-            perm, ops, L, U = plan.export()
-            exp = (perm, ops, L, U, info.block_rows, info.storage_count, plan.input_tiles(s.vals))
+        if world == 1 and args.workload != "lap64" and not args.no_cpu_baseline:
             cores = os.cpu_count() or 1
-            dt, xc = cpu_oracle_step(exp, s, cores)
-            cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-                   "sample": f"one full factor+solve of the {args.workload} system through the C restatement of the "
-                             "reference's executor path (the reference's AVX-512 build does not compile on aarch64)",
+            d, dt, _ = cpu_sample(work, sg, cores, 15.0)
+            cpu = {"value": d / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+                   "sample": (f"one full factor+solve of the {args.workload} system" if work.count == 1 else
+                              f"the first {d} of the {work.count} systems, factor + {nrhs} solves each") +
+                             " through the C restatement of the reference's executor path (the reference's "
+                             "AVX-512 build does not compile on aarch64)",
                    "seconds": dt}
-        xt = s.x_true
+        fwd = {}
+        xt = [s.x_true for s in work.systems]
+        if all(t is not None for t in xt):
+            def ferr(xx):
+                parts = work.split(xx)
+                return max(float(np.linalg.norm(p - t) / np.linalg.norm(t)) for p, t in zip(parts, xt))
+            fwd = {"fwd_err_vs_x_true": ferr(x_mixed)}
+        e2e_match = bool(np.array_equal(x_e2e, x_mixed))
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": rm["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "rhs": nrhs,
+            "config": {"workload": work.desc, "systems_per_step": work.count, "rhs": nrhs,
                        "precision": "mixed: FP32 factors, 3xTF32 tile products, FP64 IR",
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (FP32 tiles {info.storage_count * 16384 / 1e9:.2f} GB)",
                        "executor": "persistent queue"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),
-            "rel_resid": rm["stats"]["rel_resid"], "backward_error": rm["stats"]["backward_error"],
-            "fwd_err_vs_x_true": float(np.linalg.norm(x_mixed - xt) / np.linalg.norm(xt)),
+            "rel_resid": rm["stats"]["rel_resid"], "backward_error": rm["stats"]["backward_error"], **fwd,
             "fp64_plain": {"value": v64, "unit": "solves/s", "steps": k64, "ms_per_step": r64["ms"] / k64,
                            "factor_ms": f64m, "solve_ms": statistics.mean(r64["solve_ms"]),
                            "rel_resid": r64["stats"]["rel_resid"],
-                           "fwd_err_vs_x_true": float(np.linalg.norm(x_fp64 - xt) / np.linalg.norm(xt)),
+                           **({"fwd_err_vs_x_true": max(float(np.linalg.norm(p - t) / np.linalg.norm(t))
+                                                        for p, t in zip(work.split(x_fp64), xt))} if fwd else {}),
                            "roofline": fp64_roof},
             "mixed_over_fp64": value / v64,
             "dominant": dominant,
             "roofline": roof,
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(s.nnz * 8 + s.n * 8 * nrhs),
-                    "d2h_bytes_per_step": int(s.n * 8 * nrhs), "ms_per_step": re2e["ms"] / args.steps},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(work.nnz * 8 + work.b.size * 8),
+                    "d2h_bytes_per_step": int(work.b.size * 8), "ms_per_step": re2e["ms"] / args.steps,
+                    "path": "sog_factor + sog_solve with pinned host buffers", "x_equals_device_path": e2e_match},
             "cpu_baseline": cpu,
             "clocks": rm["clocks"],
             "gpu_launches": int(rm["launches"]),
-            "plan": {"host_plan_s": t_plan, "ops": int(info.nops), "stages": int(info.stages),
+            "plan": {"host_plan_s": work.t_plan, "ops": int(info.nops), "stages": int(info.stages),
                      "tasks": ti["tasks"], "levels": ti["levels"], "algorithmic_gflop": flops / 1e9},
         }
         print(json.dumps(line), flush=True)
@@ -373,10 +532,18 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="var48")
+    ap.add_argument("--requests", type=int, default=32, help="serving: requests per rate")
+    ap.add_argument("--rates", default="0.5,2,8", help="serving: Poisson arrival rates (requests/s)")
+    ap.add_argument("--planners", type=int, default=4, help="serving: host planning threads")
+    ap.add_argument("--serving-fp64", action="store_true", help="serving: also run the plain FP64 path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    return run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
+    return run_ours(args)
 
 
 if __name__ == "__main__":

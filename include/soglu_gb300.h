@@ -68,7 +68,10 @@ typedef struct {
     int32_t max_refine;  /* iterative-refinement steps allowed (SOG_MIXED) */
     double tol;          /* target ||b - A x||_2 / ||b||_2 (SOG_MIXED), e.g. 1e-10 */
     int32_t gemm_split;  /* 0 = auto; FP64 tile products split into 1 or 4 output quadrants */
-    int32_t reserved[7];
+    int32_t solve_lookahead; /* 0 = on, -1 = off: the factor also forms Dinv_i * L_{i,i-1} (and the U
+                                counterpart) so each substitution row waits on its neighbour for one
+                                64x64 product only */
+    int32_t reserved[6];
 } sog_options;
 
 typedef struct {
@@ -143,6 +146,9 @@ int sog_ctx_pool_usage(const sog_ctx *ctx, uint64_t *used, uint64_t *total);
  * on this context is launched on it, so callers can order and time work
  * against it with their own events. */
 int sog_ctx_stream(const sog_ctx *ctx, void **stream);
+/* Return pool chunks that hold no allocation to the device (after many
+ * systems of different sizes came and went). */
+int sog_ctx_trim(sog_ctx *ctx);
 
 /* ---- one system --------------------------------------------------------------
  * Upload the plan's DAG and allocate its tiles in the pool (admission: returns
@@ -243,6 +249,57 @@ int sog_residual_noalloc(int32_t n, const int32_t *row_ptr, const int32_t *col, 
  * device 0; x_out receives n values in the original ordering. */
 int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_t *index_i, const int32_t *index_j,
                   const double *vals, const double *b, double *x_out, int32_t precision);
+
+/* ---- serving -----------------------------------------------------------------
+ * No counterpart in the reference (one system per process, main.cpp). A
+ * request loop with continuous batching: sog_server_submit copies a request
+ * (COO system as for sog_plan_build, nrhs right-hand sides rhs-major) and
+ * returns at once; host worker threads plan it; one scheduler thread owns the
+ * context and, whenever the GPU is free, admits every planned request that
+ * the block pool can hold (first come, first served, sog_system_bytes as the
+ * estimate), merges them into one batch plan, factors them in one executor
+ * launch and solves all their right-hand sides together. Requests that arrive
+ * while a batch runs join the next one. A request larger than the whole pool
+ * fails with SOG_ENOMEM; one that fits once others are released waits.
+ * Factors stay resident after the answer (sog_server_solve for further
+ * right-hand sides) until sog_server_release. The context must not be used
+ * directly while a server runs on it. */
+typedef struct sog_server sog_server;
+typedef struct {
+    int32_t planner_threads;      /* host planning workers (0 = 2) */
+    int32_t planner_omp_threads;  /* OpenMP threads per plan (0 = default) */
+    int32_t max_batch;            /* requests merged into one launch at most (0 = 256) */
+    int32_t reserved0;
+    double batch_window_ms;       /* once a request is planned, wait up to this long for requests
+                                     still being planned to join its launch (0 = launch at once) */
+    int32_t reserved[2];
+} sog_server_options;
+typedef struct {
+    int32_t status;       /* SOG_OK, SOG_ENOCONV, SOG_ENAN, or the request's error */
+    int32_t batch_size;   /* requests factored in the same launch */
+    int64_t batch_id;
+    double plan_ms;       /* host planning */
+    double queue_ms;      /* planned -> admitted */
+    double gpu_ms;        /* the batch's factor + solve, host clock */
+    double total_ms;      /* submit -> answer */
+    sog_solve_stats stats;
+} sog_request_info;
+/* opt: the systems' options (NULL = SOG_MIXED, 10 refinement steps, 1e-10) */
+int sog_server_create(sog_ctx *ctx, const sog_options *opt, const sog_server_options *sopt, sog_server **out);
+int sog_server_submit(sog_server *srv, int32_t n, int64_t nnz, const int32_t *I, const int32_t *J, const double *V,
+                      int32_t nrhs, const double *b, int64_t *id);
+/* Wait for the answer (timeout_ms < 0: no limit; SOG_ETIMEOUT if still
+ * running). x (if not NULL) receives nrhs x n values. */
+int sog_server_wait(sog_server *srv, int64_t id, double timeout_ms, double *x, sog_request_info *info);
+/* Further right-hand sides on a request's resident factors (blocks the caller). */
+int sog_server_solve(sog_server *srv, int64_t id, int32_t nrhs, const double *b, double *x, sog_solve_stats *stats);
+/* Drop a finished request; its batch's pool memory returns when all of the
+ * batch's requests are released. */
+int sog_server_release(sog_server *srv, int64_t id);
+/* counts[8] = {batches launched, requests admitted, completed, rejected,
+ * largest batch, requests resident, planned and waiting, waiting to plan} */
+int sog_server_counters(sog_server *srv, int64_t *counts);
+void sog_server_destroy(sog_server *srv);
 
 #ifdef __cplusplus
 }

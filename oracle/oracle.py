@@ -76,3 +76,18 @@ def solve_system(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, stor
     x = np.empty(n)
     x[perm_new_to_old] = x_ext[:n]
     return x, tiles, nan
+
+
+def solve_system_multi(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, storage_count, input_tiles, L, U,
+                       B: np.ndarray, threads: int = 0) -> np.ndarray:
+    """One calculate, then one substitution per right-hand side (rows of B,
+    original ordering): the reference's factor-once, solve-each path."""
+    tiles = calculate(ops, storage_count, input_tiles, threads)
+    B = np.atleast_2d(np.asarray(B, dtype=np.float64))
+    X = np.empty_like(B)
+    for r in range(B.shape[0]):
+        b_ext = np.ones(block_rows * 64)
+        b_ext[:n] = B[r][perm_new_to_old]
+        x_ext, _ = solve(block_rows, L, U, tiles, b_ext)
+        X[r][perm_new_to_old] = x_ext[:n]
+    return X

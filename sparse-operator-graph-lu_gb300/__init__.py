@@ -47,7 +47,7 @@ class PlanInfo(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
-                ("gemm_split", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class SolveStats(C.Structure):
@@ -59,6 +59,22 @@ class SolveStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("planner_threads", C.c_int32), ("planner_omp_threads", C.c_int32), ("max_batch", C.c_int32),
+                ("reserved0", C.c_int32), ("batch_window_ms", C.c_double), ("reserved", C.c_int32 * 2)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_int32), ("batch_id", C.c_int64), ("plan_ms", C.c_double),
+                ("queue_ms", C.c_double), ("gpu_ms", C.c_double), ("total_ms", C.c_double), ("stats", SolveStats)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stats"}
+        d.update(self.stats.as_dict())
+        d["status"] = self.status
+        return d
+
+
 # every symbol declared in include/soglu_gb300.h
 EXPORTS = [
     "sog_last_error", "sog_version", "sog_plan_build", "sog_plan_get_info", "sog_plan_export", "sog_plan_input_tiles",
@@ -68,7 +84,9 @@ EXPORTS = [
     "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
     "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
     "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
-    "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device",
+    "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
+    "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
+    "sog_server_destroy",
 ]
 
 _lib = None
@@ -104,6 +122,11 @@ def lib() -> C.CDLL:
         "sog_residual_noalloc": ([I32, P, P, P, I32, P, P, P, P, P, P], I32),
         "sog_plan_merge": ([P, I32, P], I32), "sog_plan_segments": ([P, P, P], I32),
         "sog_solve_batch": ([P, P, P, P, P], I32), "sog_solve_batch_device": ([P, P, P, P, P], I32),
+        "sog_ctx_trim": ([P], I32), "sog_server_create": ([P, P, P, P], I32),
+        "sog_server_submit": ([P, I32, I64, P, P, P, I32, P, P], I32),
+        "sog_server_wait": ([P, I64, D, P, P], I32), "sog_server_solve": ([P, I64, I32, P, P, P], I32),
+        "sog_server_release": ([P, I64], I32), "sog_server_counters": ([P, P], I32),
+        "sog_server_destroy": ([P], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -250,12 +273,12 @@ class System:
     """One system resident in the device pool: factor once, solve many."""
 
     def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
-                 max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0):
+                 max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0):
         self.ctx, self.plan = ctx, plan
         self.n = plan.info.n
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
-                           gemm_split=gemm_split)
+                           gemm_split=gemm_split, solve_lookahead=solve_lookahead)
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
 
     def factor(self, vals) -> None:
@@ -380,6 +403,79 @@ class System:
     def close(self):
         if getattr(self, "_h", None):
             lib().sog_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+
+class Server:
+    """Request loop with continuous batching on one context (sog_server_*):
+    submit returns at once; requests are planned on host threads and merged
+    into shared launches as the GPU and the block pool allow; factors stay
+    resident until release."""
+
+    def __init__(self, ctx: Context, precision: int = MIXED, max_refine: int = 10, tol: float = 1e-10,
+                 planners: int = 2, omp_threads: int = 0, max_batch: int = 0, batch_window_ms: float = 0.0):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        self.opt = Options(precision=precision, executor=EXEC_PERSISTENT, max_refine=max_refine, tol=tol)
+        self.sopt = ServerOptions(planner_threads=planners, planner_omp_threads=omp_threads, max_batch=max_batch,
+                                  batch_window_ms=batch_window_ms)
+        self._n = {}
+        _check(lib().sog_server_create(ctx._h, C.byref(self.opt), C.byref(self.sopt), C.byref(self._h)))
+
+    def submit(self, n: int, rows, cols, vals, b) -> int:
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        c = np.ascontiguousarray(cols, dtype=np.int32)
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        k = 1 if bb.ndim == 1 else bb.shape[0]
+        if bb.size != k * n:
+            raise ValueError(f"right-hand sides must have shape ({n},) or (k, {n})")
+        rid = C.c_int64()
+        _check(lib().sog_server_submit(self._h, int(n), r.size, _p(r), _p(c), _p(v), k, _p(bb), C.byref(rid)))
+        self._n[rid.value] = (n, bb.shape)
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: float = -1.0, allow_noconv: bool = False):
+        """(x shaped like the submitted b, info dict)."""
+        if rid not in self._n:
+            raise SOGError(SOG_EINVAL, f"unknown or released request {rid}")
+        n, shape = self._n[rid]
+        x = np.empty(shape, np.float64)
+        info = RequestInfo()
+        rc = lib().sog_server_wait(self._h, rid, timeout_ms, _p(x), C.byref(info))
+        if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
+            _check(rc)
+        return x, info.as_dict()
+
+    def solve(self, rid: int, b):
+        if rid not in self._n:
+            raise SOGError(SOG_EINVAL, f"unknown or released request {rid}")
+        n, _ = self._n[rid]
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        k = 1 if bb.ndim == 1 else bb.shape[0]
+        x = np.empty_like(bb)
+        st = SolveStats()
+        _check(lib().sog_server_solve(self._h, rid, k, _p(bb), _p(x), C.byref(st)))
+        return x, st.as_dict()
+
+    def release(self, rid: int) -> None:
+        _check(lib().sog_server_release(self._h, rid))
+        self._n.pop(rid, None)
+
+    def counters(self) -> dict:
+        c = np.zeros(8, np.int64)
+        _check(lib().sog_server_counters(self._h, _p(c)))
+        keys = ["batches", "admitted", "completed", "rejected", "max_batch", "resident", "planned_waiting",
+                "to_plan"]
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sog_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -24,7 +24,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SRC = ["order.cpp", "planner.cpp", "mtx.cpp", "tasks.cpp", "batch.cpp", "plan_api.cpp", "runtime.cpp"]
+HOST_SRC = ["order.cpp", "planner.cpp", "mtx.cpp", "tasks.cpp", "batch.cpp", "plan_api.cpp", "runtime.cpp", "server.cpp"]
 CUDA_SRC = ["factor.cu", "solve.cu"]
 HEADERS = ["plan.h", "tasks.h", "kernels.h", "api_internal.h"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function", f"-I{CUDA}/include",
@@ -78,7 +78,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         list(ex.map(_run, steps))
     libdir = _cuda_libdir()
     if _stale(LIB, objs):
-        _run(["g++", "-shared", "-o", LIB, *objs, f"-L{libdir}", "-lcudart", "-fopenmp",
+        _run(["g++", "-shared", "-o", LIB, *objs, f"-L{libdir}", "-lcudart", "-fopenmp", "-pthread",
               f"-Wl,-rpath,{libdir}"])
     cli_src = os.path.join(CSRC, "solve_main.cpp")
     if _stale(CLI, [cli_src, LIB] + hdrs):

@@ -554,6 +554,11 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 __device__ __forceinline__ void red_release_add(int* p, int v) {
     asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ int atom_add_acquire(int* p, int v) {
+    int old;
+    asm volatile("atom.acquire.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
 
 // Called by warp 0 once the CTA's writes for an item are complete. The last
 // part of a task releases its successors; of those that become ready, the one
@@ -563,10 +568,10 @@ __device__ __forceinline__ void red_release_add(int* p, int v) {
 __device__ int complete_item(const DevTasks& tk, int task) {
     const int lane = threadIdx.x & 31;
     int last = 0;
-    if (lane == 0) {
-        __threadfence();
-        last = (tk.parts[task] == 1) || (atomicSub(&tk.parts_left[task], 1) == 1);
-    }
+    // release: the CTA's writes for this item (ordered before this warp by the
+    // CTA barrier) become visible before any counter below moves
+    __threadfence();
+    if (lane == 0) last = (tk.parts[task] == 1) || (atom_add_acquire(&tk.parts_left[task], -1) == 1);
     last = __shfl_sync(FULL, last, 0);
     int keep = -1, keep_prio = -1;  // warp-uniform
     if (last) {
@@ -576,7 +581,9 @@ __device__ int complete_item(const DevTasks& tk, int task) {
             int s = -1;
             if (k < s1) {
                 s = tk.succ[k];
-                if (atomicSub(&tk.dep[s], 1) != 1) s = -1;
+                // acquire: the lane that sees the count reach zero synchronises
+                // with every producer's release of this successor's inputs
+                if (atom_add_acquire(&tk.dep[s], -1) != 1) s = -1;
                 else if (tk.trace) tk.trace[4 * (size_t)s] = globaltimer_ns();
             }
             if (!__any_sync(FULL, s >= 0)) continue;
@@ -613,7 +620,8 @@ __device__ int complete_item(const DevTasks& tk, int task) {
             }
         }
         if (keep >= 0) {
-            __threadfence();  // the kept task's inputs, released by their producers, are visible here
+            // the kept task's inputs were acquired by the lane that released it;
+            // the CTA barrier before the task passes that on to every thread
             const int np = tk.parts[keep];
             if (np > 1) {
                 int base_pos = 0;
@@ -638,7 +646,11 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
     __shared__ tc::State st;
     uint32_t phase = 0;
     if constexpr (sizeof(T) == 4) tc_setup(st);
-    if (threadIdx.x == 0) s_next = -1;
+    if (threadIdx.x == 0) {
+        s_next = -1;
+        s_stop = 0;
+    }
+    unsigned done_here = 0;  // items this CTA completed (thread 0)
     for (;;) {
         if (threadIdx.x == 0) {
             int item = s_next;
@@ -651,6 +663,7 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
                     while ((item = ld_acquire(tk.queue + slot)) < 0) {
                         if ((++spins & 15) == 0) {
                             if (ld_acquire(tk.done) >= tk.total_items) { item = -1; break; }
+                            if (ld_acquire(&tk.status->flags) & ST_TIMEOUT) { item = -1; break; }
                             if (globaltimer_ns() - t0 > tk.wait_limit_ns) {
                                 atomicOr(&tk.status->flags, ST_TIMEOUT);
                                 tk.status->timeout_where = slot;
@@ -673,7 +686,8 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
                 atomicMax(tr + 1, ~globaltimer_ns());  // start = min over parts, stored inverted
                 tr[3] = smid;
             }
-            __threadfence();
+            // a claimed item was acquired from its queue slot, a kept one by
+            // complete_item; the barrier below extends either to the CTA
             s_item = item;
         }
         __syncthreads();
@@ -686,8 +700,9 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
             const int keep = complete_item(tk, item >> 4);
             if (threadIdx.x == 0) {
                 s_next = keep;
-                // a timeout anywhere stops every CTA at its next claim
-                s_stop = (ld_acquire(&tk.status->flags) & ST_TIMEOUT) ? 1 : 0;
+                // a timeout anywhere stops every CTA: spinning ones in the claim
+                // loop, busy ones here every 8th item (an L2 round trip each)
+                if ((++done_here & 7) == 0) s_stop = (ld_acquire(&tk.status->flags) & ST_TIMEOUT) ? 1 : 0;
             }
         }
         __syncthreads();

@@ -72,15 +72,27 @@ struct DevSolve {
     const int32_t *u_ptr, *u_col, *u_id;
     const int32_t *l_diag, *u_diag;  // diagonal block id per block row
     const int32_t *l_dinv, *u_dinv;  // block id of the inverse of each diagonal block
-    int32_t* flags;                  // per block row readiness epoch
+    int32_t* flags;                  // readiness epoch per (column chunk, block row): R x TRISOLVE_MAX_CHUNKS
     DevStatus* status;
     unsigned long long wait_limit_ns;
     // optional trace (4 x u64 per block row: lower start/end, upper start/end), NULL = off
     unsigned long long* trace;
+    // optional dealing order of block rows to CTAs (position -> block row) for
+    // the lower / upper solve; NULL = ascending / descending rows. Every row's
+    // dependencies must come at earlier positions. Batches interleave their
+    // systems so that consecutive positions are independent rows.
+    const int32_t *order_l, *order_u;
+    // optional look-ahead products per block row (block id of Dinv_i L_{i,i-1}
+    // / Dinv_i U_{i,i+1}, 0 = none); NULL = none
+    const int32_t *l_la, *u_la;
 };
+// Column chunks of 8 right-hand sides solved together in one launch pair
+constexpr int TRISOLVE_MAX_CHUNKS = 8;
 // In-place block substitution on vec (n_ext x nrhs, row-major), lower then
-// upper, in chunks of up to 8 columns. epoch: readiness tag, advanced by 2 per
-// chunk (lower publishes epoch, upper epoch+1); launches counts kernels.
+// upper: full 8-column chunks together in one launch per triangle (their rows
+// interleaved), the remaining columns in chunks of 4, 2, 1. epoch: readiness
+// tag, advanced by 2 per launch pair (lower publishes epoch, upper epoch+1);
+// launches counts kernels.
 int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrhs, int& epoch, int grid,
                     cudaStream_t st, int& launches);
 int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int& epoch, int grid,

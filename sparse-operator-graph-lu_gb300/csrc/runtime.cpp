@@ -90,6 +90,19 @@ struct Pool {
             return;
         }
     }
+    // give chunks without allocations back to the device
+    void trim() {
+        std::vector<Chunk> keep;
+        for (auto& c : chunks) {
+            if (c.free_.size() == 1 && c.free_.begin()->first == 0 && c.free_.begin()->second == c.size) {
+                cudaFree(c.base);
+                reserved -= c.size;
+            } else {
+                keep.push_back(std::move(c));
+            }
+        }
+        chunks.swap(keep);
+    }
     void destroy() {
         for (auto& c : chunks) cudaFree(c.base);
         chunks.clear();
@@ -348,7 +361,8 @@ int run_factor(sog_system* s) {
 
 int trisolve(sog_system* s, void* vec, int nrhs) {
     sog_ctx* c = s->ctx;
-    const int grid = std::min(s->R, trisolve_grid(s->fp64, nrhs, c->num_sms));
+    const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));  // positions per row
+    const int grid = std::min(s->R * nch, trisolve_grid(s->fp64, nrhs, c->num_sms));
     int nl = 0;
     int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, c->stream, nl)
                      : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, c->stream, nl);
@@ -596,6 +610,14 @@ int sog_ctx_stream(const sog_ctx* c, void** stream) {
     return SOG_OK;
 }
 
+int sog_ctx_trim(sog_ctx* c) {
+    if (!c) return fail(SOG_EINVAL, "NULL context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    c->pool.trim();
+    return SOG_OK;
+}
+
 int sog_ctx_pool_usage(const sog_ctx* c, uint64_t* used, uint64_t* total) {
     if (!c) return fail(SOG_EINVAL, "NULL context");
     if (used) *used = c->pool.used;
@@ -607,7 +629,8 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     if (!plan || !bytes) return fail(SOG_EINVAL, "NULL argument");
     sog_options o = opt ? *opt : default_options();
     const Plan& p = plan->p;
-    uint64_t tiles = (uint64_t)p.storage_count * 4096 * elem_bytes(o);
+    // + diagonal inverses and look-ahead products added for the substitution
+    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows) * 4096 * elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
     *bytes = tiles + aux;
@@ -646,12 +669,16 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     int32_t storage2 = p.storage_count;
     std::vector<int32_t> ldinv, udinv;
     add_diag_inverses(ops2, storage2, s->R, p.L, p.U, ldinv, udinv);
+    std::vector<int32_t> lla, ula;
+    if (o.solve_lookahead >= 0) add_lookahead_products(ops2, storage2, s->R, p.L, p.U, ldinv, udinv, lla, ula);
     s->storage = storage2;
     std::vector<int32_t> outputs;
     for (const Leaf& lf : p.L) outputs.push_back(lf.id);
     for (const Leaf& lf : p.U) outputs.push_back(lf.id);
     for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
+    for (int32_t id : lla) if (id > 0) outputs.push_back(id);
+    for (int32_t id : ula) if (id > 0) outputs.push_back(id);
     try {
         s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts);
     } catch (const std::exception& e) {
@@ -704,6 +731,21 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         for (int i = 0; i < p.cfg.n; i++) n2o[i] = p.ord.new_to_old[i];
     else
         n2o = p.ord.new_to_old;
+    // substitution dealing order of a batch: by row within its system (from
+    // the top for L, from the bottom for U), then by system
+    std::vector<int32_t> ord_l, ord_u;
+    if (ns > 1) {
+        int maxR = 0;
+        for (const Segment& sg : s->segs) maxR = std::max(maxR, sg.R);
+        ord_l.reserve(s->R);
+        ord_u.reserve(s->R);
+        for (int r = 0; r < maxR; r++)
+            for (const Segment& sg : s->segs)
+                if (r < sg.R) {
+                    ord_l.push_back(sg.row0 / 64 + r);
+                    ord_u.push_back(sg.row0 / 64 + sg.R - 1 - r);
+                }
+    }
     // task arrays
     std::vector<int32_t> parts32(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) parts32[t] = g.parts[t];
@@ -724,12 +766,14 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_lid = L.add<int32_t>(lid.size()), o_uptr = L.add<int32_t>(uptr.size()),
              o_ucol = L.add<int32_t>(ucol.size()), o_uid = L.add<int32_t>(uid.size()),
              o_ldiag = L.add<int32_t>(ldiag.size()), o_udiag = L.add<int32_t>(udiag.size()),
-             o_flags = L.add<int32_t>(s->R), o_cptr = L.add<int32_t>(hc.ptr.size()),
+             o_flags = L.add<int32_t>((size_t)s->R * TRISOLVE_MAX_CHUNKS), o_cptr = L.add<int32_t>(hc.ptr.size()),
              o_ccol = L.add<int32_t>(hc.col.size()), o_cval = L.add<double>(hc.val.size()),
              o_cpos = L.add<int32_t>(hc.pos.size()), o_sct = L.add<int32_t>(p.scatter_tile.size()),
              o_sco = L.add<int16_t>(p.scatter_off.size()), o_pdt = L.add<int32_t>(p.pad_tile.size()),
              o_pdo = L.add<int16_t>(p.pad_off.size()), o_n2o = L.add<int32_t>(n2o.size()),
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
+             o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
+             o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()),
              o_V = L.add<double>(s->ntrip);
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
@@ -789,7 +833,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     ds.l_dinv = put(A, o_ldinv, ldinv, st);
     ds.u_dinv = put(A, o_udinv, udinv, st);
     ds.flags = reinterpret_cast<int32_t*>(A + o_flags);
-    cudaMemsetAsync(ds.flags, 0, sizeof(int32_t) * s->R, st);
+    cudaMemsetAsync(ds.flags, 0, sizeof(int32_t) * s->R * TRISOLVE_MAX_CHUNKS, st);
     ds.status = dt.status;
     ds.wait_limit_ns = dt.wait_limit_ns;
     if (!plan->imported) {
@@ -807,6 +851,10 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->d_n2o = put(A, o_n2o, n2o, st);
     s->d_seg_brow = put(A, o_sbr, seg_brow, st);
     s->d_seg_n = put(A, o_sn, seg_n, st);
+    ds.order_l = ord_l.empty() ? nullptr : put(A, o_ordl, ord_l, st);
+    ds.order_u = ord_u.empty() ? nullptr : put(A, o_ordu, ord_u, st);
+    ds.l_la = lla.empty() ? nullptr : put(A, o_lla, lla, st);
+    ds.u_la = ula.empty() ? nullptr : put(A, o_ula, ula, st);
     if (cudaMallocHost(&s->h_red, sizeof(double) * RED * 64 * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_nrhs, sizeof(int32_t) * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_active, sizeof(int32_t) * ns) != cudaSuccess ||

@@ -8,10 +8,13 @@
 // block as soon as the block row it multiplies is published (a per-row
 // readiness flag), then solves its diagonal block and publishes its own row.
 // Rows only wait on rows dealt earlier, so the smallest unfinished row can
-// always proceed; every wait is bounded and reports a timeout status.
+// always proceed; every wait is bounded and reports a timeout status. A batch
+// of independent systems deals its rows interleaved (row 0 of every system,
+// then row 1, ...), so that neighbouring CTAs work on different systems.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -66,12 +69,16 @@ __device__ __forceinline__ T warp_sum(T v) {
 // its off-diagonal blocks: each warp waits (bounded) only for the row its
 // block multiplies, stages that row's NR-column slice in shared memory and
 // accumulates block * slice in registers (lane l: rows 2l, 2l+1). The warp
-// partials and b_i are combined, multiplied by the precomputed inverse of the
-// diagonal block, and the row is published with a release store.
+// partials and b_i are combined and multiplied by the precomputed inverse of
+// the diagonal block. With a look-ahead product M = Dinv_i * B_{i,j} for the
+// neighbouring row j (i-1 for L, i+1 for U), block B_{i,j} is left out of the
+// sum and y_i = Dinv_i (b_i - sum) - M y_j is finished after row j is
+// published: the row's critical path is one 64x64 product. The row is then
+// published with a release store.
 // smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR]
 template <typename T, int NR>
-__global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld, int c0,
-                                                      int epoch, int lower) {
+__global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
+                                                      int cbase, int nch, int epoch, int lower) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NV = 64 * NR;
     constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte load
@@ -85,38 +92,52 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     const int* col = lower ? s.l_col : s.u_col;
     const int* ids = lower ? s.l_id : s.u_id;
     const int* dinv = lower ? s.l_dinv : s.u_dinv;
+    const int* lookahead = lower ? s.l_la : s.u_la;
+    const int* order = lower ? s.order_l : s.order_u;
     if (tid == 0) s_stop = 0;
     __syncthreads();
     T* yw = ybuf + warp * NV;
-    for (int k = blockIdx.x; k < R; k += gridDim.x) {
-        const int i = lower ? k : R - 1 - k;
+    // bounded wait of lane 0 for row j's flag; the warp's later reads of row j
+    // are ordered after lane 0's acquire by the __syncwarp that follows
+    const int* fl = nullptr;  // this position's chunk of the flags
+    auto wait_row = [&](int j) -> bool {
+        if (lane == 0) {
+            const unsigned long long t0 = globaltimer_ns();
+            while (ld_acquire(fl + j) != epoch) {
+                if (globaltimer_ns() - t0 > s.wait_limit_ns) {
+                    atomicOr(&s.status->flags, ST_SOLVE_TIMEOUT);
+                    s_stop = 1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __syncwarp();
+        return !*(volatile int*)&s_stop;
+    };
+    // positions: nch column chunks of each row in turn, rows in dealing order
+    for (int k = blockIdx.x; k < R * nch; k += gridDim.x) {
+        const int kk = k / nch, ch = k - kk * nch, c0 = cbase + ch * NR;
+        const int i = order ? order[kk] : (lower ? kk : R - 1 - kk);
+        fl = s.flags + (size_t)ch * R;
         if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
         const T* Dm = tiles + (size_t)dinv[i] * 4096;
+        const int la = lookahead ? lookahead[i] : 0;
         // warm L1 with this lane's slice of the diagonal inverse
         asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
         T pa[NR], pb[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
         bool stop = false;
-        for (int q = ptr[i] + warp; q < ptr[i + 1]; q += 8) {
+        // with a look-ahead product the last block (the neighbouring row) is left out
+        const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0);
+        for (int q = ptr[i] + warp; q < q1; q += 8) {
             const int j = col[q];
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
             // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
 #pragma unroll
             for (int o = 0; o < 128; o += 128 / (int)sizeof(T)) asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
-            if (lane == 0) {
-                const unsigned long long t0 = globaltimer_ns();
-                while (ld_acquire(s.flags + j) != epoch) {
-                    if (globaltimer_ns() - t0 > s.wait_limit_ns) {
-                        atomicOr(&s.status->flags, ST_SOLVE_TIMEOUT);
-                        s_stop = 1;
-                        break;
-                    }
-                    __nanosleep(32);
-                }
-            }
-            __syncwarp();  // lane 0's acquire orders the warp's reads of row j after it
-            if (*(volatile int*)&s_stop) {
+            if (!wait_row(j)) {
                 stop = true;
                 break;
             }
@@ -152,9 +173,16 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             acc[e] = v;
         }
         __syncthreads();
-        // y_i = inv(D_ii) * acc: warp w rows 8w..8w+7, four lanes per row
+        // y_i = inv(D_ii) * acc [- M * y_j]: warp w rows 8w..8w+7, four lanes
+        // per row, each lane 16 columns; partial sums reduced over the four lanes
         {
             const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
+            Vec16<T> m[16 / VW];
+            if (la > 0) {  // the look-ahead slice, loaded before the wait
+                const T* M = tiles + (size_t)la * 4096 + row * 64 + cb;
+#pragma unroll
+                for (int c = 0; c < 16 / VW; c++) m[c] = ldg16(M + c * VW);
+            }
             T y[NR];
 #pragma unroll
             for (int r = 0; r < NR; r++) y[r] = T(0);
@@ -165,6 +193,17 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 for (int v = 0; v < VW; v++)
 #pragma unroll
                     for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
+            }
+            if (la > 0) {
+                const int j = lower ? i - 1 : i + 1;
+                if (!wait_row(j)) return;  // s_stop is set: every warp leaves at this same point
+                const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
+#pragma unroll
+                for (int c = 0; c < 16 / VW; c++)
+#pragma unroll
+                    for (int v = 0; v < VW; v++)
+#pragma unroll
+                        for (int r = 0; r < NR; r++) y[r] -= m[c].v[v] * __ldcg(vj + (size_t)(c * VW + v) * ld + r);
             }
 #pragma unroll
             for (int r = 0; r < NR; r++) {
@@ -179,7 +218,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         __syncthreads();
         if (tid == 0) {
             __threadfence();  // the row written by all threads (ordered by the barrier) before the flag
-            st_release(s.flags + i, epoch);
+            st_release(s.flags + (size_t)ch * R + i, epoch);
             if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
         }
     }
@@ -191,11 +230,12 @@ size_t trisolve_smem() {
 }
 
 template <typename T, int NR>
-int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int& epoch, int grid, cudaStream_t st) {
+int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int nch, int& epoch, int grid,
+                   cudaStream_t st) {
     const size_t smem = trisolve_smem<T, NR>();
     cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, epoch, 1);
-    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, epoch + 1, 0);
+    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch, 1);
+    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch + 1, 0);
     epoch += 2;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -206,10 +246,13 @@ int trisolve_impl(const DevSolve& s, const T* tiles, T* vec, int nrhs, int& epoc
     int rc = 0;
     for (int c0 = 0; c0 < nrhs && rc == 0;) {
         const int left = nrhs - c0;
-        if (left >= 8) { rc = trisolve_chunk<T, 8>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 8; }
-        else if (left >= 4) { rc = trisolve_chunk<T, 4>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 4; }
-        else if (left >= 2) { rc = trisolve_chunk<T, 2>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 2; }
-        else { rc = trisolve_chunk<T, 1>(s, tiles, vec, nrhs, c0, epoch, grid, st); c0 += 1; }
+        if (left >= 8) {
+            const int nch = std::min(left / 8, TRISOLVE_MAX_CHUNKS);
+            rc = trisolve_chunk<T, 8>(s, tiles, vec, nrhs, c0, nch, epoch, grid, st);
+            c0 += 8 * nch;
+        } else if (left >= 4) { rc = trisolve_chunk<T, 4>(s, tiles, vec, nrhs, c0, 1, epoch, grid, st); c0 += 4; }
+        else if (left >= 2) { rc = trisolve_chunk<T, 2>(s, tiles, vec, nrhs, c0, 1, epoch, grid, st); c0 += 2; }
+        else { rc = trisolve_chunk<T, 1>(s, tiles, vec, nrhs, c0, 1, epoch, grid, st); c0 += 1; }
         launches += 2;
     }
     return rc;

@@ -58,5 +58,13 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
 // diagonal L and U blocks. storage_count grows by the number of new blocks.
 void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv);
+// Look-ahead products for the substitution: for every block row i with an L
+// block at (i, i-1), lla[i] = id of a new block Linv_ii * L_{i,i-1}; for every
+// U block at (i, i+1), ula[i] = id of Uinv_ii * U_{i,i+1} (0 = none). The
+// substitution then forms y_i = Linv_ii (b_i - sum_{j<i-1} L_ij y_j) - lla_i
+// y_{i-1}: everything but one 64x64 product is done before row i-1 is ready.
+void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+                            const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
+                            const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula);
 
 }  // namespace sog
