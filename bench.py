@@ -117,6 +117,16 @@ def make_workload(name: str):
     return [wl.varcoef3d(24 if name == "var24" else 48)]
 
 
+def _measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+MEASURED = _measured_peaks()
+
 # DRAM bytes (read + write) of one mixed factor launch, from a one-pass ncu
 # capture of the full-size launch (dram__bytes_read.sum + dram__bytes_write.sum:
 # 421.45 MB + 3.83 GB at var48); None where no capture covers the workload
@@ -464,6 +474,19 @@ def run_ours(args):
                 "traffic": TRAFFIC.get(args.workload),
                 "peak_source": f"cuBLAS TF32 GEMM measured in this run ({peaks['tf32_tflops']:.1f} TFLOP/s) / 3",
                 "algorithmic_flop_per_launch": flops, "avg_launch_ms": fm}
+        # substitution: HBM-bound by its algorithmic bytes per pass (every factor
+        # tile it reads once, FP32: off-diagonal L/U leaves, diagonal inverses,
+        # look-ahead products; the vectors), passes = 1 + refinement steps
+        R = info.block_rows
+        tiles_read = (info.n_lleaf + info.n_uleaf - 2 * R) + 2 * R + 2 * R
+        pass_bytes = tiles_read * 4096 * 4 + 3 * info.n_ext * 4 * nrhs
+        passes = 1 + statistics.mean(rm["iters"])
+        s_ach = pass_bytes / (sm_ * 1e-3 / passes) / 1e9
+        hbm_peak, hbm_src = (MEASURED.get("hbm_gbs"), "MEASURED_PEAKS.json hbm_gbs (measured copy)") \
+            if MEASURED.get("hbm_gbs") else (6800.0, "fallback 6.8 TB/s")
+        solve_roof = {"bound": "hbm", "kernel": "trisolve_kernel<float> (L and U passes)", "achieved": s_ach,
+                      "peak": hbm_peak, "unit": "GB/s", "frac": s_ach / hbm_peak, "peak_source": hbm_src,
+                      "algorithmic_bytes_per_pass": pass_bytes, "passes_per_solve": passes}
         fp64_roof = {"achieved": flops / (f64m * 1e-3) / 1e12, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                      "frac": flops / (f64m * 1e-3) / 1e12 / peaks["fp64_tflops"],
                      "peak_source": "cuBLAS DGEMM measured in this run", "avg_factor_ms": f64m}
@@ -506,6 +529,7 @@ def run_ours(args):
             "mixed_over_fp64": value / v64,
             "dominant": dominant,
             "roofline": roof,
+            "solve_roofline": solve_roof,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(work.nnz * 8 + work.b.size * 8),
                     "d2h_bytes_per_step": int(work.b.size * 8), "ms_per_step": re2e["ms"] / args.steps,
                     "path": "sog_factor + sog_solve with pinned host buffers", "x_equals_device_path": e2e_match},

@@ -191,9 +191,11 @@ int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
 int sog_system_last_times(const sog_system *sys, double *factor_ms, double *solve_ms);
 void sog_system_destroy(sog_system *sys);
 /* Build the device task graph of a plan on the host only (no device):
- * counts[13] = {tasks, dependency levels, queue items, tile-product pairs,
+ * counts[15] = {tasks, dependency levels, queue items, tile-product pairs,
  * GEMM, LU, LINV, UINV, SUB tasks, fused Schur subs, added diagonal-inverse
- * blocks, critical-path length in tasks, lower inverses fused into LU}. */
+ * blocks, critical-path length in tasks, lower inverses fused into LU, copies
+ * replaced by aliasing (a copy's readers read its source's tile), repeated
+ * inverses of one block replaced by aliasing}. */
 int sog_plan_task_graph_info(const sog_plan *plan, int32_t gemm_split, int64_t *counts);
 /* Task-graph summary: counts[11] = {tasks, dependency levels, queue items,
  * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid,

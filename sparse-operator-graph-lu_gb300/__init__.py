@@ -208,10 +208,10 @@ class Plan:
 
     def task_graph_info(self, gemm_split: int = 1) -> dict:
         """Device task graph built on the host (no GPU needed)."""
-        c = np.zeros(13, np.int64)
+        c = np.zeros(15, np.int64)
         _check(lib().sog_plan_task_graph_info(self._h, gemm_split, _p(c)))
         keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "fused_subs",
-                "added_inverses", "critical_path", "fused_inverses"]
+                "added_inverses", "critical_path", "fused_inverses", "aliased_copies", "aliased_inverses"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def bytes_needed(self, precision: int = FP64) -> int:

@@ -7,6 +7,8 @@
 //
 // Block matrices are quadtrees over a power-of-two grid of blocks; absent
 // children are zero blocks and generate no ops.
+#include <omp.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -274,7 +276,7 @@ struct OpOrder {
 // Liveness, dead-op elimination, stage assignment and ordering
 // (BlockPlanner.cpp:103-374). `inputs` / `outputs` are block ids.
 void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>& inputs,
-              const std::vector<int32_t>& outputs, bool always_prune) {
+              const std::vector<int32_t>& outputs, bool always_prune, int threads) {
     std::vector<int32_t> lastuse(storage, 0), stage(storage, 0);
     stage[0] = 1;
     for (int32_t id : inputs) { stage[id] = 1; lastuse[id] = 0; }
@@ -328,7 +330,23 @@ void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>&
         if (o.res2 > 0) continue;
         if (o.res > 0 && stage[o.res] > o.stage) o.stage = stage[o.res];
     }
-    std::sort(ops.begin(), ops.end(), OpOrder());
+    // sort by OpOrder: bucket by stage (its first key), then order each
+    // stage's ops by the remaining keys, stages in parallel. OpOrder is a
+    // total order (seq is unique), so the result is the single sorted order.
+    {
+        int32_t maxst = 0;
+        for (const Op& o : ops) maxst = std::max(maxst, o.stage);
+        std::vector<int64_t> start(maxst + 2, 0);
+        for (const Op& o : ops) start[o.stage + 1]++;
+        for (int32_t st = 0; st <= maxst; st++) start[st + 1] += start[st];
+        std::vector<Op> sorted(ops.size());
+        std::vector<int64_t> pos(start.begin(), start.end() - 1);
+        for (const Op& o : ops) sorted[pos[o.stage]++] = o;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : omp_get_max_threads())
+        for (int32_t st = 0; st <= maxst; st++)
+            std::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
+        ops.swap(sorted);
+    }
     // stages of more than 8000 ops are split (BlockPlanner.cpp:335-354)
     int32_t jump = 0, band = 0, cur = 0;
     for (Op& o : ops) {
@@ -395,7 +413,7 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
         std::vector<int32_t> outs;
         for (auto& lf : cL) outs.push_back(lf.id);
         for (auto& lf : cU) outs.push_back(lf.id);
-        schedule(cz.ops, cz.storage, cinputs, outs, true);
+        schedule(cz.ops, cz.storage, cinputs, outs, true, threads);
     }
     p.coarse_ops = (int64_t)cz.ops.size();
 
@@ -508,7 +526,7 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
         std::vector<int32_t> outs;
         for (auto& lf : p.L) outs.push_back(lf.id);
         for (auto& lf : p.U) outs.push_back(lf.id);
-        schedule(fz.ops, fz.storage, finputs, outs, false);
+        schedule(fz.ops, fz.storage, finputs, outs, false, threads);
     }
     p.ops = std::move(fz.ops);
     p.storage_count = fz.storage;

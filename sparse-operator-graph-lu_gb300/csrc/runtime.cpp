@@ -686,14 +686,21 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
     }
     const TaskGraph& g = s->tg;
+    // leaves and substitution tiles through the copy aliases: a copied block's
+    // value lives in its source's tile
+    for (Leaf& lf : s->L) lf.id = g.alias[lf.id];
+    for (Leaf& lf : s->U) lf.id = g.alias[lf.id];
+    for (auto* v : {&ldinv, &udinv, &lla, &ula})
+        for (int32_t& id : *v)
+            if (id > 0) id = g.alias[id];
     // solve structure
     std::vector<int32_t> lptr(s->R + 1, 0), uptr(s->R + 1, 0), ldiag(s->R, 0), udiag(s->R, 0);
     std::vector<Leaf> loff, uoff;
-    for (const Leaf& lf : p.L) {
+    for (const Leaf& lf : s->L) {
         if (lf.bi == lf.bj) ldiag[lf.bi] = lf.id;
         else if (lf.bj < lf.bi) loff.push_back(lf);
     }
-    for (const Leaf& lf : p.U) {
+    for (const Leaf& lf : s->U) {
         if (lf.bi == lf.bj) udiag[lf.bi] = lf.id;
         else if (lf.bj > lf.bi) uoff.push_back(lf);
     }
@@ -1124,6 +1131,8 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
         counts[10] = storage2 - p.storage_count;
         counts[11] = g.ntasks ? *std::max_element(g.prio.begin(), g.prio.end()) + 1 : 0;
         counts[12] = g.fused_inverses;
+        counts[13] = g.aliased_copies;
+        counts[14] = g.aliased_inverses;
     } catch (const std::exception& e) {
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
     }

@@ -6,9 +6,74 @@
 
 namespace sog {
 
-TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input,
-                      const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs) {
+// Redundant ops become aliases (every block is written once, so equal inputs
+// give equal values): a copy (sub with src = 0: res = src2) reads src2's tile,
+// and a second lowerInv / upperInv of the same block reads the first one's
+// result (the planner's two levels invert some diagonal blocks twice). Chains
+// resolve to the first non-redundant block.
+static std::vector<Op> alias_copies(const std::vector<Op>& in, int32_t storage_count, std::vector<int32_t>& alias,
+                                    int64_t& ncopies, int64_t& ndup) {
+    alias.resize(storage_count);
+    for (int32_t b = 0; b < storage_count; b++) alias[b] = b;
+    ncopies = ndup = 0;
+    auto find = [&](int32_t b) {
+        int32_t r = b;
+        while (alias[r] != r) r = alias[r];
+        while (alias[b] != r) {
+            const int32_t nx = alias[b];
+            alias[b] = r;
+            b = nx;
+        }
+        return r;
+    };
+    auto valid = [&](int32_t b) { return b > 0 && b < storage_count; };
+    std::vector<char> skip(in.size(), 0);
+    std::unordered_map<int64_t, int32_t> first_inv;  // (kind, source root) -> result
+    for (size_t i = 0; i < in.size(); i++) {
+        const Op& o = in[i];
+        if (o.op == OP_SUB && o.src == 0 && valid(o.src2) && valid(o.res) && alias[o.res] == o.res) {
+            alias[o.res] = o.src2;
+            skip[i] = 1;
+            ncopies++;
+        } else if ((o.op == OP_LOWERINV || o.op == OP_UPPERINV) && valid(o.src) && valid(o.res) &&
+                   alias[o.res] == o.res) {
+            const int64_t key = ((int64_t)find(o.src) << 1) | (o.op == OP_UPPERINV ? 1 : 0);
+            auto it = first_inv.find(key);
+            if (it == first_inv.end()) {
+                first_inv.emplace(key, o.res);
+            } else {
+                alias[o.res] = it->second;
+                skip[i] = 1;
+                ndup++;
+            }
+        }
+    }
+    for (int32_t b = 0; b < storage_count; b++) find(b);
+    std::vector<Op> out;
+    out.reserve(in.size() - ncopies - ndup);
+    for (size_t i = 0; i < in.size(); i++) {
+        const Op& o = in[i];
+        if (skip[i]) continue;
+        if ((o.res > 0 && o.res < storage_count && alias[o.res] != o.res) ||
+            (o.res2 > 0 && o.res2 < storage_count && alias[o.res2] != o.res2))
+            throw std::runtime_error("block written by a copy and by another op");
+        Op q = o;
+        if (q.src > 0 && q.src < storage_count) q.src = alias[q.src];
+        if (q.src2 > 0 && q.src2 < storage_count) q.src2 = alias[q.src2];
+        out.push_back(q);
+    }
+    return out;
+}
+
+TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int32_t n_input,
+                      const std::vector<int32_t>& outputs_in, int gemm_parts, bool fuse_subs) {
     if (gemm_parts != 1 && gemm_parts != 4) throw std::runtime_error("gemm_parts must be 1 or 4");
+    std::vector<int32_t> alias;
+    int64_t ncopies = 0, ndup = 0;
+    const std::vector<Op> ops = alias_copies(ops_in, storage_count, alias, ncopies, ndup);
+    std::vector<int32_t> outputs;
+    outputs.reserve(outputs_in.size());
+    for (int32_t id : outputs_in) outputs.push_back(id > 0 && id < storage_count ? alias[id] : id);
     const int64_t nops = (int64_t)ops.size();
     std::vector<int32_t> producer(storage_count, -1);  // block -> task
     std::vector<int32_t> readers(storage_count, 0);
@@ -106,6 +171,9 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
     g.storage_count = storage_count;
     g.fused_subs = fused;
     g.fused_inverses = fused_inv;
+    g.aliased_copies = ncopies;
+    g.aliased_inverses = ndup;
+    g.alias = std::move(alias);
     for (size_t t = 0; t < tl.size(); t++)
         if (!tl[t].dead) newid[t] = g.ntasks++;
     g.pair_ptr.assign(g.ntasks + 1, 0);

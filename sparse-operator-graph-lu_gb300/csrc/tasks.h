@@ -43,10 +43,17 @@ struct TaskGraph {
     int64_t gemm_pairs = 0;
     int64_t fused_subs = 0;
     int64_t fused_inverses = 0;  // lowerInv tasks folded into their LU task
+    int64_t aliased_copies = 0;  // copy ops (sub with src = 0) replaced by aliasing
+    int64_t aliased_inverses = 0;  // repeated lowerInv / upperInv of one block replaced by aliasing
     int64_t count[5] = {0, 0, 0, 0, 0};
+    // block -> block whose tile holds its value: identity except the result of
+    // a copy, which reads its source's tile (every block is written once, so
+    // a copy's source never changes after the copy would have run)
+    std::vector<int32_t> alias;
 };
 
-// outputs: block ids that must be materialised (the L/U leaves). Throws
+// outputs: block ids that must be materialised (the L/U leaves; a copied
+// output is materialised in its source's tile, see TaskGraph::alias). Throws
 // std::runtime_error on a block written by ops of different kinds, a read of a
 // block nobody produces (and not an input), an id out of range, or a cycle.
 // gemm_parts: parts per GEMM task (1 or 4).

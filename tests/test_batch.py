@@ -92,7 +92,7 @@ def test_merge_plans_task_graph(sg, wl):
     m = sg.merge_plans(plans)
     g = m.task_graph_info()
     parts = [p.task_graph_info() for p in plans]
-    for key in ("tasks", "pairs", "gemm", "lu", "linv", "uinv", "sub", "fused_subs"):
+    for key in ("tasks", "pairs", "gemm", "lu", "linv", "uinv", "sub", "fused_subs", "aliased_copies"):
         assert g[key] == sum(q[key] for q in parts), key
     assert g["critical_path"] == max(q["critical_path"] for q in parts)
 

@@ -125,8 +125,8 @@ def test_task_graph(sg, wl, name):
     ops = info["ops"]
     assert tg["lu"] == ops.get("lu", 0)
     assert tg["pairs"] == ops.get("mul", 0) + ops.get("mulneg", 0)
-    assert tg["sub"] + tg["fused_subs"] == ops.get("sub", 0)
-    assert tg["linv"] + tg["uinv"] + tg["fused_inverses"] == \
+    assert tg["sub"] + tg["fused_subs"] + tg["aliased_copies"] == ops.get("sub", 0)
+    assert tg["linv"] + tg["uinv"] + tg["fused_inverses"] + tg["aliased_inverses"] == \
         ops.get("lowerInv", 0) + ops.get("upperInv", 0) + tg["added_inverses"]
     assert 0 < tg["fused_inverses"] <= tg["lu"]
     assert tg["levels"] <= info["stages"]
