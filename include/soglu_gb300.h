@@ -37,8 +37,11 @@ extern "C" {
 #define SOG_FP64 0      /* plain FP64 factor + solve (DMMA tile products) */
 #define SOG_MIXED 1     /* FP32 factors, 3xTF32 tile products, FP64 iterative refinement */
 
-#define SOG_EXEC_PERSISTENT 0 /* one persistent launch pulling ready tasks from a device queue */
+#define SOG_EXEC_PERSISTENT 0 /* one persistent launch claiming tasks in a static order (estimated start
+                                 time), each claimant waiting for its task's dependency count to reach zero */
 #define SOG_EXEC_LEVELS 1     /* one launch per dependency level (stage-synchronous, like calculate()) */
+#define SOG_EXEC_QUEUE 2      /* one persistent launch pulling ready tasks from a device queue, each CTA
+                                 keeping the most urgent successor it readied */
 
 /* One unit operation: the fields of the reference's struct operation
  * (operation.h:37-48); op numbering follows enum blockOp (operation.h:20):
@@ -64,7 +67,7 @@ typedef struct {
 
 typedef struct {
     int32_t precision;   /* SOG_FP64 or SOG_MIXED */
-    int32_t executor;    /* SOG_EXEC_PERSISTENT or SOG_EXEC_LEVELS */
+    int32_t executor;    /* SOG_EXEC_PERSISTENT, SOG_EXEC_LEVELS or SOG_EXEC_QUEUE */
     int32_t max_refine;  /* iterative-refinement steps allowed (SOG_MIXED) */
     double tol;          /* target ||b - A x||_2 / ||b||_2 (SOG_MIXED), e.g. 1e-10 */
     int32_t gemm_split;  /* 0 = auto; FP64 tile products split into 1 or 4 output quadrants */

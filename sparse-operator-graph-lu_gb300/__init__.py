@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(_PKG, "lib", "libsoglu_gb300.so")
 
 SOG_OK, SOG_EINVAL, SOG_ENOMEM, SOG_EPIVOT, SOG_ENAN, SOG_ETIMEOUT, SOG_ECUDA, SOG_ENOCONV, SOG_ESTATE, SOG_ENODEV = range(10)
 FP64, MIXED = 0, 1
-EXEC_PERSISTENT, EXEC_LEVELS = 0, 1
+EXEC_PERSISTENT, EXEC_LEVELS, EXEC_QUEUE = 0, 1, 2
 OP_NAMES = ["inv", "lu", "lowerInv", "upperInv", "sub", "add", "neg", "copy", "mul", "mulneg", "llt", "mult", "noop"]
 _CODES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "EPIVOT", 4: "ENAN", 5: "ETIMEOUT", 6: "ECUDA", 7: "ENOCONV",
           8: "ESTATE", 9: "ENODEV"}

@@ -1,8 +1,16 @@
 // Factor-phase kernels for sm_103a: the unit ops of the reference's DAG
-// (MatrixStdDouble.cpp) as CTA-wide tile tasks, and two executors that run the
-// task graph: a persistent kernel that pulls ready tasks from a device queue
-// with atomic dependency counters, and a per-level launch (stage-synchronous,
-// as BlockPlanner::calculate runs stages, BlockPlanner.cpp:376-651).
+// (MatrixStdDouble.cpp) as CTA-wide tile tasks, and three executors that run
+// the task graph with atomic dependency counters: a persistent kernel whose
+// CTAs claim tasks in a static order and wait for each to become ready (the
+// default), a persistent kernel that pulls ready tasks from a device queue,
+// and a per-level launch (stage-synchronous, as BlockPlanner::calculate runs
+// stages, BlockPlanner.cpp:376-651).
+//
+// Hardware notes for sm_103a: the mixed path's tile products use tcgen05 MMAs
+// with TMEM accumulators (tc_gemm.cuh); LU and triangular inverses run on the
+// CUDA cores with rows in registers; FP64 scalar and DMMA throughput on this
+// part are about 1.2 TFLOP/s, so the FP64 path is compute-bound and the mixed
+// path latency-bound on the DAG's critical path.
 //
 // Tiles are dense 64x64 row-major; block id k lives at tiles + k*4096.
 // FP64 path: tile products on the FP64 tensor pipe (DMMA, mma.sync m8n8k4).
@@ -12,6 +20,8 @@
 // produced by other SMs during the same launch), double-buffered over the
 // operand pairs of a product so the next pair loads while this one computes.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include "kernels.h"
@@ -635,11 +645,12 @@ __device__ int complete_item(const DevTasks& tk, int task) {
     return keep >= 0 ? (keep << 4) : -1;
 }
 
-// Each CTA runs the item it kept from its last completion, else claims the
-// next queue slot and waits (bounded) until a producer fills it. The launch
-// ends when every item has completed; no CTA ever waits inside a task.
+// Ready-queue executor: each CTA runs the item it kept from its last
+// completion, else claims the next queue slot and waits (bounded) until a
+// producer fills it. The launch ends when every item has completed; no CTA
+// ever waits inside a task.
 template <typename T>
-__global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* tiles) {
+__global__ void __launch_bounds__(NT) factor_queue_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item, s_next, s_stop;
@@ -711,6 +722,89 @@ __global__ void __launch_bounds__(NT) factor_persistent_kernel(DevTasks tk, T* t
     if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 
+// Warp 0 after the CTA's writes for an item are complete: the last part of a
+// task releases its successors with fire-and-forget reductions (no round
+// trip): a claimant spinning on a successor's count sees it reach zero.
+__device__ void release_item(const DevTasks& tk, int task) {
+    const int lane = threadIdx.x & 31;
+    __threadfence();  // release: the CTA's writes (ordered before this warp by the barrier)
+    int last = 1;
+    if (tk.parts[task] > 1) {
+        if (lane == 0) last = atom_add_acquire(&tk.parts_left[task], -1) == 1;
+        last = __shfl_sync(FULL, last, 0);
+        if (last) __threadfence();  // the other parts' writes, acquired above, released with ours
+    }
+    if (last)
+        for (int k = tk.succ_ptr[task] + lane; k < tk.succ_ptr[task + 1]; k += 32)
+            red_release_add(&tk.dep[tk.succ[k]], -1);
+}
+
+// Static list scheduling. Every CTA claims the next position of a fixed item
+// order (estimated start time, then longest remaining path) and waits,
+// bounded, until that item's task has no unfinished predecessor; then runs it
+// and releases its successors. Predecessors always come earlier in the order,
+// so the smallest unfinished position can always run: with every CTA
+// co-resident the launch cannot deadlock. A critical task is usually claimed
+// before it is ready, so its claimant starts as soon as the count drops.
+template <typename T>
+__global__ void __launch_bounds__(NT) factor_ordered_kernel(DevTasks tk, T* tiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    __shared__ int s_item;
+    __shared__ tc::State st;
+    uint32_t phase = 0;
+    if constexpr (sizeof(T) == 4) tc_setup(st);
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int item = -1;
+            const int pos = atomicAdd(tk.head, 1);
+            if (pos < tk.total_items) {
+                item = tk.order[pos];
+                const int task = item >> 4;
+                if (task < 0 || task >= tk.ntasks) {
+                    atomicOr(&tk.status->flags, ST_BAD_ITEM);
+                    item = -1;
+                } else {
+                    const unsigned long long t0 = globaltimer_ns();
+                    unsigned spins = 0;
+                    while (ld_acquire(tk.dep + task) > 0) {
+                        if ((++spins & 15) == 0) {
+                            if (ld_acquire(&tk.status->flags) & (ST_TIMEOUT | ST_BAD_ITEM)) { item = -1; break; }
+                            if (globaltimer_ns() - t0 > tk.wait_limit_ns) {
+                                atomicOr(&tk.status->flags, ST_TIMEOUT);
+                                tk.status->timeout_where = pos;
+                                item = -1;
+                                break;
+                            }
+                        }
+                        __nanosleep(32);
+                    }
+                    if (item >= 0 && tk.trace) {
+                        unsigned smid;
+                        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+                        unsigned long long* tr = tk.trace + 4 * (size_t)task;
+                        const unsigned long long now = globaltimer_ns();
+                        atomicMax(tr + 0, now);   // ready: seen by the (last) claimant
+                        atomicMax(tr + 1, ~now);  // start = min over parts, stored inverted
+                        tr[3] = smid;
+                    }
+                }
+            }
+            s_item = item;  // the claimant's acquire passes to the CTA at the barrier
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item < 0) break;
+        run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
+            release_item(tk, item >> 4);
+        }
+    }
+    if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles, const int32_t* items) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -724,10 +818,18 @@ __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles,
 }
 
 template <typename T>
-int persistent_launch(const DevTasks& t, T* tiles, int grid, cudaStream_t s) {
+int queue_launch(const DevTasks& t, T* tiles, int grid, cudaStream_t s) {
     const size_t smem = smem_elems<T>() * sizeof(T);
-    cudaFuncSetAttribute(factor_persistent_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    factor_persistent_kernel<T><<<grid, NT, smem, s>>>(t, tiles);
+    cudaFuncSetAttribute(factor_queue_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    factor_queue_kernel<T><<<grid, NT, smem, s>>>(t, tiles);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename T>
+int ordered_launch(const DevTasks& t, T* tiles, int grid, cudaStream_t s) {
+    const size_t smem = smem_elems<T>() * sizeof(T);
+    cudaFuncSetAttribute(factor_ordered_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    factor_ordered_kernel<T><<<grid, NT, smem, s>>>(t, tiles);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -770,11 +872,17 @@ __global__ void widen_kernel(const float* __restrict__ s, double* __restrict__ d
 
 }  // namespace
 
-int factor_persistent_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s) {
-    return persistent_launch<double>(t, tiles, grid, s);
+int factor_queue_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s) {
+    return queue_launch<double>(t, tiles, grid, s);
 }
-int factor_persistent_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s) {
-    return persistent_launch<float>(t, tiles, grid, s);
+int factor_queue_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s) {
+    return queue_launch<float>(t, tiles, grid, s);
+}
+int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s) {
+    return ordered_launch<double>(t, tiles, grid, s);
+}
+int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s) {
+    return ordered_launch<float>(t, tiles, grid, s);
 }
 int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, cudaStream_t s) {
     return level_launch<double>(t, tiles, items, nitems, s);
@@ -787,17 +895,21 @@ size_t factor_smem_bytes(bool fp64) {
     return fp64 ? smem_elems<double>() * sizeof(double) : smem_elems<float>() * sizeof(float);
 }
 
-int factor_persistent_grid(bool fp64, int num_sms) {
+template <typename K>
+int resident_per_sm(K kernel, size_t smem) {
     int per_sm = 0;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, smem);
+    return per_sm < 1 ? 1 : per_sm;
+}
+
+int factor_persistent_grid(bool fp64, int num_sms) {
+    // both persistent executors launch this many CTAs: the smaller residency of the two
     const size_t smem = factor_smem_bytes(fp64);
-    if (fp64) {
-        cudaFuncSetAttribute(factor_persistent_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, factor_persistent_kernel<double>, NT, smem);
-    } else {
-        cudaFuncSetAttribute(factor_persistent_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, factor_persistent_kernel<float>, NT, smem);
-    }
-    if (per_sm < 1) per_sm = 1;
+    int per_sm = fp64 ? std::min(resident_per_sm(factor_queue_kernel<double>, smem),
+                                 resident_per_sm(factor_ordered_kernel<double>, smem))
+                      : std::min(resident_per_sm(factor_queue_kernel<float>, smem),
+                                 resident_per_sm(factor_ordered_kernel<float>, smem));
     return per_sm * num_sms;
 }
 

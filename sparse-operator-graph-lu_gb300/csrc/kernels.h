@@ -39,6 +39,9 @@ struct DevTasks {
     int32_t* head;        // next slot to claim
     int32_t* tail;        // next slot to fill
     int32_t* done;        // completed items
+    // static claim order of items (the ordered executor): estimated start
+    // time, then longest remaining path
+    const int32_t* order;
     DevStatus* status;
     unsigned long long wait_limit_ns;  // bound on any single queue wait
     // optional per-task trace (4 x u64 per task: ready, start, end, sm id), NULL = off
@@ -47,8 +50,11 @@ struct DevTasks {
 
 // ---- factor (factor.cu) ----
 // tiles: block id -> tiles + id*4096 elements. double => SOG_FP64, float => SOG_MIXED.
-int factor_persistent_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
-int factor_persistent_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
+int factor_queue_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
+int factor_queue_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
+// ordered executor: one persistent launch claiming items in the static order
+int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
+int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
 int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, cudaStream_t s);
 int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, cudaStream_t s);
 // persistent grid size (CTAs co-resident on the device)

@@ -344,9 +344,13 @@ int run_factor(sog_system* s) {
                          : factor_level_launch(s->dt, (float*)s->tiles, s->d_level_items + a, b - a, st);
             s->launches++;
         }
+    } else if (s->opt.executor == SOG_EXEC_QUEUE) {
+        rc = s->fp64 ? factor_queue_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
+                     : factor_queue_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
+        s->launches++;
     } else {
-        rc = s->fp64 ? factor_persistent_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
-                     : factor_persistent_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
+        rc = s->fp64 ? factor_ordered_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
+                     : factor_ordered_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
         s->launches++;
     }
     if (rc) return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -642,7 +646,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     *out = nullptr;
     sog_options o = opt ? *opt : default_options();
     if (o.precision != SOG_FP64 && o.precision != SOG_MIXED) return fail(SOG_EINVAL, "bad precision");
-    if (o.executor != SOG_EXEC_PERSISTENT && o.executor != SOG_EXEC_LEVELS) return fail(SOG_EINVAL, "bad executor");
+    if (o.executor != SOG_EXEC_PERSISTENT && o.executor != SOG_EXEC_LEVELS && o.executor != SOG_EXEC_QUEUE)
+        return fail(SOG_EINVAL, "bad executor");
     if (o.tol <= 0) o.tol = 1e-10;
     if (o.max_refine < 0) o.max_refine = 0;
     CK(cudaSetDevice(c->device));
@@ -715,6 +720,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (const Leaf& lf : loff) { lptr[lf.bi + 1]++; lcol.push_back(lf.bj); lid.push_back(lf.id); }
     for (const Leaf& lf : uoff) { uptr[lf.bi + 1]++; ucol.push_back(lf.bj); uid.push_back(lf.id); }
     for (int i = 0; i < s->R; i++) { lptr[i + 1] += lptr[i]; uptr[i + 1] += uptr[i]; }
+    const std::vector<int32_t> order = static_order(g, s->fp64);
     HostCSR hc;
     if (!plan->imported) hc = build_csr(p);
     // systems: a plain plan is one system over all block rows
@@ -781,6 +787,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()),
+             o_order = L.add<int32_t>(order.size()),
              o_V = L.add<double>(s->ntrip);
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
@@ -824,6 +831,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.tail = dt.head + 1;
     dt.done = dt.head + 2;
     s->d_level_items = put(A, o_levels, g.level_items, st);
+    dt.order = put(A, o_order, order, st);
     s->d_status0 = put(A, o_st0, st0, st);
     dt.status = reinterpret_cast<DevStatus*>(A + o_st);
     dt.wait_limit_ns = 10ull * 1000 * 1000 * 1000;

@@ -8,7 +8,8 @@
 // right-hand side there, main.cpp:61; this writes x.)
 //
 // options: --mixed (FP32 factors + FP64 refinement) | --fp64 (default)
-//          --levels (stage-synchronous executor) --device N --threads N
+//          --levels (stage-synchronous executor) --queue (ready-queue executor)
+//          --device N --threads N
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -27,7 +28,7 @@ static double now_s() {
 
 int main(int argc, char** argv) {
     if (argc <= 1 || std::string(argv[1]).find(".mtx") == std::string::npos) {
-        std::printf("usage: ./solve filename.mtx [--fp64|--mixed] [--levels] [--device N] [--threads N]\n");
+        std::printf("usage: ./solve filename.mtx [--fp64|--mixed] [--levels|--queue] [--device N] [--threads N]\n");
         return 0;
     }
     std::string fname = argv[1];
@@ -37,6 +38,7 @@ int main(int argc, char** argv) {
         if (a == "--mixed") precision = SOG_MIXED;
         else if (a == "--fp64") precision = SOG_FP64;
         else if (a == "--levels") executor = SOG_EXEC_LEVELS;
+        else if (a == "--queue") executor = SOG_EXEC_QUEUE;
         else if (a == "--device" && i + 1 < argc) device = std::atoi(argv[++i]);
         else if (a == "--threads" && i + 1 < argc) threads = std::atoi(argv[++i]);
     }

@@ -295,6 +295,41 @@ void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_r
     }
 }
 
+std::vector<int32_t> static_order(const TaskGraph& g, bool fp64) {
+    // single-CTA task latencies on GB300 (us), enough to rank start times
+    auto cost = [&](int32_t t) -> double {
+        const int np = g.pair_ptr[t + 1] - g.pair_ptr[t];
+        switch (g.kind[t]) {
+            case K_GEMM: return fp64 ? 5.0 + 20.0 * np / g.parts[t] : 1.5 + 2.0 * np;
+            case K_LU: return fp64 ? 140.0 : 24.0;
+            case K_LINV:
+            case K_UINV: return fp64 ? 95.0 : 14.0;
+            default: return fp64 ? 6.0 : 3.0;
+        }
+    };
+    const double hop = 2.0;
+    std::vector<int32_t> by_level(g.ntasks);
+    for (int32_t t = 0; t < g.ntasks; t++) by_level[t] = t;
+    std::stable_sort(by_level.begin(), by_level.end(), [&](int32_t a, int32_t b) { return g.level[a] < g.level[b]; });
+    std::vector<double> est(g.ntasks, 0.0);
+    for (int32_t t : by_level) {
+        const double fin = est[t] + cost(t) + hop;
+        for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++) est[g.succ[k]] = std::max(est[g.succ[k]], fin);
+    }
+    std::vector<int32_t> tasks(g.ntasks);
+    for (int32_t t = 0; t < g.ntasks; t++) tasks[t] = t;
+    std::stable_sort(tasks.begin(), tasks.end(), [&](int32_t a, int32_t b) {
+        if (est[a] != est[b]) return est[a] < est[b];
+        if (g.prio[a] != g.prio[b]) return g.prio[a] > g.prio[b];
+        return a < b;
+    });
+    std::vector<int32_t> items;
+    items.reserve(g.total_items);
+    for (int32_t t : tasks)
+        for (int p = 0; p < g.parts[t]; p++) items.push_back((t << 4) | p);
+    return items;
+}
+
 void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula) {

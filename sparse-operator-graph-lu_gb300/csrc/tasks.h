@@ -65,6 +65,11 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
 // diagonal L and U blocks. storage_count grows by the number of new blocks.
 void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv);
+// Claim order of the ordered executor: items by estimated start time (longest
+// weighted path from a source, single-CTA task latencies as weights), ties by
+// longest remaining path. Every task comes after its predecessors.
+std::vector<int32_t> static_order(const TaskGraph& g, bool fp64);
+
 // Look-ahead products for the substitution: for every block row i with an L
 // block at (i, i-1), lla[i] = id of a new block Linv_ii * L_{i,i-1}; for every
 // U block at (i, i+1), ula[i] = id of Uinv_ii * U_{i,i+1} (0 = none). The

@@ -8,11 +8,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_poisoned_dependency_times_out_then_recovers(sg, wl):
+@pytest.mark.parametrize("executor", [0, 2], ids=["persistent", "queue"])
+def test_poisoned_dependency_times_out_then_recovers(sg, wl, executor):
     ctx = sg.Context()
     s = wl.lap2d(32)
     p = sg.Plan(s.n, s.rows, s.cols, s.vals)
-    sys_ = sg.System(ctx, p, precision=sg.FP64)
+    sys_ = sg.System(ctx, p, precision=sg.FP64, executor=executor)
     sys_.set_wait_limit(200.0)
     ntasks = sys_.task_info()["tasks"]
     assert sg.lib().sog_debug_poison_task(sys_._h, ntasks // 2) == 0

@@ -27,7 +27,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("executor", [0, 1], ids=["persistent", "levels"])
+@pytest.mark.parametrize("executor", [0, 1, 2], ids=["persistent", "levels", "queue"])
 @pytest.mark.parametrize("name", SMALL)
 def test_fp64_solution_matches_reference(sg, wl, ctx, name, executor):
     s = golden_cases(wl)[name]()
@@ -59,12 +59,13 @@ def test_fp64_factors_match_oracle(sg, wl, ctx, oracle, name, split):
     sys_.close()
 
 
+@pytest.mark.parametrize("executor", [0, 2], ids=["persistent", "queue"])
 @pytest.mark.parametrize("name", SMALL)
-def test_mixed_refinement_reaches_tolerance(sg, wl, ctx, name):
+def test_mixed_refinement_reaches_tolerance(sg, wl, ctx, name, executor):
     s = golden_cases(wl)[name]()
     g = golden(name)
     p = sg.Plan(s.n, s.rows, s.cols, s.vals)
-    sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10)
+    sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=executor)
     sys_.factor(s.vals)
     x, st = sys_.solve(rhs_of(s))
     assert st["rel_resid"] <= 1e-10
