@@ -442,8 +442,10 @@ def run_ours(args):
         return {"ms": max_over_ranks(ms, world, dev), "lat": lat, "factor_ms": fms, "solve_ms": sms,
                 "iters": iters, "stats": st, "clocks": clocks, "launches": sysm.task_info()["launches"] - l0}
 
-    mixed = sg.System(ctx, plan, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=args.executor)
+    mixed = sg.System(ctx, plan, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=args.executor,
+                      pipeline_stages=args.stages)
     rm = timed(mixed, args.steps, args.warmup)
+    grid_mixed = mixed.task_info()["grid"]
     x_mixed = x.cpu().numpy()
     re2e = timed(mixed, args.steps, args.warmup, host=True)
     x_e2e = hx.numpy().copy()
@@ -516,7 +518,9 @@ def run_ours(args):
                        "precision": "mixed: FP32 factors, 3xTF32 tile products, FP64 IR",
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (FP32 tiles {info.storage_count * 16384 / 1e9:.2f} GB)",
-                       "executor": ["persistent, static order", "per level", "persistent, ready queue"][args.executor]},
+                       "executor": ["persistent, static order", "per level", "persistent, ready queue",
+                                    "autotuned"][args.executor],
+                       "factor_ctas": grid_mixed, "pipeline_stages": args.stages or "tuned"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),
             "rel_resid": rm["stats"]["rel_resid"], "backward_error": rm["stats"]["backward_error"], **fwd,
@@ -556,7 +560,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="var48")
-    ap.add_argument("--executor", type=int, default=0, help="0 persistent (static order), 1 per level, 2 ready queue")
+    ap.add_argument("--executor", type=int, default=0,
+                    help="0 persistent (static order), 1 per level, 2 ready queue, 3 autotuned")
+    ap.add_argument("--stages", type=int, default=0, help="mixed path operand stages: 1, 2, or 0 = tuned")
     ap.add_argument("--requests", type=int, default=32, help="serving: requests per rate")
     ap.add_argument("--rates", default="0.5,2,8", help="serving: Poisson arrival rates (requests/s)")
     ap.add_argument("--planners", type=int, default=4, help="serving: host planning threads")

@@ -42,6 +42,10 @@ extern "C" {
 #define SOG_EXEC_LEVELS 1     /* one launch per dependency level (stage-synchronous, like calculate()) */
 #define SOG_EXEC_QUEUE 2      /* one persistent launch pulling ready tasks from a device queue, each CTA
                                  keeping the most urgent successor it readied */
+#define SOG_EXEC_AUTO 3       /* tuned: the first factorisation times the persistent executors (and, for
+                                 SOG_MIXED with pipeline_stages = 0, both stage counts where two CTAs fit
+                                 per SM) and keeps the fastest, remembered for task graphs of the same
+                                 size and parallelism */
 
 /* One unit operation: the fields of the reference's struct operation
  * (operation.h:37-48); op numbering follows enum blockOp (operation.h:20):
@@ -67,14 +71,17 @@ typedef struct {
 
 typedef struct {
     int32_t precision;   /* SOG_FP64 or SOG_MIXED */
-    int32_t executor;    /* SOG_EXEC_PERSISTENT, SOG_EXEC_LEVELS or SOG_EXEC_QUEUE */
+    int32_t executor;    /* SOG_EXEC_PERSISTENT, SOG_EXEC_LEVELS, SOG_EXEC_QUEUE or SOG_EXEC_AUTO */
     int32_t max_refine;  /* iterative-refinement steps allowed (SOG_MIXED) */
     double tol;          /* target ||b - A x||_2 / ||b||_2 (SOG_MIXED), e.g. 1e-10 */
     int32_t gemm_split;  /* 0 = auto; FP64 tile products split into 1 or 4 output quadrants */
     int32_t solve_lookahead; /* 0 = on, -1 = off: the factor also forms Dinv_i * L_{i,i-1} (and the U
                                 counterpart) so each substitution row waits on its neighbour for one
                                 64x64 product only */
-    int32_t reserved[6];
+    int32_t pipeline_stages; /* SOG_MIXED tensor-core operand stages: 2 (the next product stages while
+                                one computes; 128 KB of shared memory), 1 (64 KB), or 0 = 2, tuned with
+                                SOG_EXEC_AUTO */
+    int32_t reserved[5];
 } sog_options;
 
 typedef struct {

@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(_PKG, "lib", "libsoglu_gb300.so")
 
 SOG_OK, SOG_EINVAL, SOG_ENOMEM, SOG_EPIVOT, SOG_ENAN, SOG_ETIMEOUT, SOG_ECUDA, SOG_ENOCONV, SOG_ESTATE, SOG_ENODEV = range(10)
 FP64, MIXED = 0, 1
-EXEC_PERSISTENT, EXEC_LEVELS, EXEC_QUEUE = 0, 1, 2
+EXEC_PERSISTENT, EXEC_LEVELS, EXEC_QUEUE, EXEC_AUTO = 0, 1, 2, 3
 OP_NAMES = ["inv", "lu", "lowerInv", "upperInv", "sub", "add", "neg", "copy", "mul", "mulneg", "llt", "mult", "noop"]
 _CODES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "EPIVOT", 4: "ENAN", 5: "ETIMEOUT", 6: "ECUDA", 7: "ENOCONV",
           8: "ESTATE", 9: "ENODEV"}
@@ -47,7 +47,8 @@ class PlanInfo(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
-                ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("pipeline_stages", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class SolveStats(C.Structure):
@@ -273,12 +274,14 @@ class System:
     """One system resident in the device pool: factor once, solve many."""
 
     def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
-                 max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0):
+                 max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0,
+                 pipeline_stages: int = 0):
         self.ctx, self.plan = ctx, plan
         self.n = plan.info.n
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
-                           gemm_split=gemm_split, solve_lookahead=solve_lookahead)
+                           gemm_split=gemm_split, solve_lookahead=solve_lookahead,
+                           pipeline_stages=pipeline_stages)
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
 
     def factor(self, vals) -> None:

@@ -42,10 +42,10 @@ constexpr int F32_STAGE = 64 * 68 + 64 * 72;  // full A and B tiles
 constexpr int INV_ELEMS = 64 * LD + 16 * 64 + 64;  // source tile + 2 x 8 finished rows + reciprocals
 constexpr int LU_ELEMS = 32 * 64 + 3 * 64;          // 2 x 8 pivot rows of A and of L^-1 + pivot data
 
-template <typename T>
+template <typename T, int S>
 constexpr int smem_elems() {
     // FP64: double-buffered DMMA stages; FP32: the tcgen05 operand area
-    constexpr int g = sizeof(T) == 8 ? 2 * F64_STAGE : tc::SMEM_BYTES / 4;
+    constexpr int g = sizeof(T) == 8 ? 2 * F64_STAGE : S * tc::STAGE_BYTES / 4;
     constexpr int t = INV_ELEMS > LU_ELEMS ? INV_ELEMS : LU_ELEMS;
     return g > t ? g : t;
 }
@@ -437,6 +437,7 @@ __device__ void sub_task(const DevTasks& tk, T* __restrict__ tiles, int task) {
 // C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh). The
 // next pair's operands load from L2 into registers while the current pair's
 // MMAs run; `phase` is this CTA's mbarrier parity, carried across tasks.
+template <int S>
 __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm, tc::State& st,
                             uint32_t& phase) {
     unsigned char* smb = reinterpret_cast<unsigned char*>(sm);
@@ -449,11 +450,20 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
         tc::load_pair(tiles + (size_t)tk.pair_a[p] * 4096, tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096, a4, b4);
     };
     const int n = p1 - p0;
+    // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
+    // under the operand loads and the MMAs
+    const int quad = warp & 3, colh = (warp >> 2) * 32, init = tk.a[task];
+    float4 u[8];
+    if (quad < 2 && init > 0) {
+        const float4* I = reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + (32 * quad + lane) * 64 + colh);
+#pragma unroll
+        for (int i = 0; i < 8; i++) u[i] = __ldcg(I + i);
+    }
     if (n > 0) operands(p0);
     for (int i = 0; i < n; i++) {
-        const int s = i & 1;
+        const int s = i % S;
         unsigned char* stg = smb + s * tc::STAGE_BYTES;
-        if (i >= 2) {  // the MMAs of pair i-2 read this stage
+        if (i >= S) {  // the MMAs of pair i-S read this stage
             if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
             phase ^= 1u << s;
         }
@@ -467,15 +477,14 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
         }
         if (i + 1 < n) operands(p0 + i + 1);
     }
-    for (int i = n > 2 ? n - 2 : 0; i < n; i++) {  // the commits not yet waited for
-        const int s = i & 1;
+    for (int i = n > S ? n - S : 0; i < n; i++) {  // the commits not yet waited for
+        const int s = i % S;
         if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
         phase ^= 1u << s;
     }
     tc::fence_after_sync();
     // epilogue: C = init + D[0:64] + D[64:128] (warps 2,3,6,7 hold the lower half)
     float* X = sm;  // [64][65], the operand area is free once the MMAs completed
-    const int quad = warp & 3, colh = (warp >> 2) * 32;
     float v[32];
     if (p0 < p1 && quad >= 2) {
         tc::tmem_ld32(st.tmem + ((uint32_t)(32 * quad) << 16) + colh, v);
@@ -494,13 +503,10 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
 #pragma unroll
             for (int i = 0; i < 32; i++) v[i] = 0.f;
         }
-        const int init = tk.a[task];
         if (init > 0) {
-            const float4* I = reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + row * 64 + colh);
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                const float4 u = __ldcg(I + i);
-                v[4 * i] += u.x; v[4 * i + 1] += u.y; v[4 * i + 2] += u.z; v[4 * i + 3] += u.w;
+                v[4 * i] += u[i].x; v[4 * i + 1] += u[i].y; v[4 * i + 2] += u[i].z; v[4 * i + 3] += u[i].w;
             }
         }
         float4* C = reinterpret_cast<float4*>(tiles + (size_t)tk.out[task] * 4096 + row * 64 + colh);
@@ -515,7 +521,7 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
 __device__ __forceinline__ void tc_setup(tc::State& st) {
     if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&st.tmem);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < tc::STAGES; s++) tc::mbar_init(&st.bar[s], 1);
+        for (int s = 0; s < tc::MAX_STAGES; s++) tc::mbar_init(&st.bar[s], 1);
         st.fail = 0;
     }
     tc::fence_before_sync();
@@ -529,7 +535,7 @@ __device__ __forceinline__ void tc_teardown(tc::State& st, const DevTasks& tk) {
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(st.tmem);
 }
 
-template <typename T>
+template <typename T, int S>
 __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task, int part, T* sm, tc::State& st,
                                          uint32_t& phase) {
     switch (tk.kind[task]) {
@@ -544,7 +550,7 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                     }
                 }
             } else {
-                gemm_f32_tc(tk, tiles, task, sm, st, phase);
+                gemm_f32_tc<S>(tk, tiles, task, sm, st, phase);
             }
             break;
         case K_LU:
@@ -649,7 +655,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
 // completion, else claims the next queue slot and waits (bounded) until a
 // producer fills it. The launch ends when every item has completed; no CTA
 // ever waits inside a task.
-template <typename T>
+template <typename T, int S>
 __global__ void __launch_bounds__(NT) factor_queue_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
@@ -704,7 +710,7 @@ __global__ void __launch_bounds__(NT) factor_queue_kernel(DevTasks tk, T* tiles)
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+        run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
@@ -746,7 +752,7 @@ __device__ void release_item(const DevTasks& tk, int task) {
 // so the smallest unfinished position can always run: with every CTA
 // co-resident the launch cannot deadlock. A critical task is usually claimed
 // before it is ready, so its claimant starts as soon as the count drops.
-template <typename T>
+template <typename T, int S>
 __global__ void __launch_bounds__(NT) factor_ordered_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
@@ -795,7 +801,7 @@ __global__ void __launch_bounds__(NT) factor_ordered_kernel(DevTasks tk, T* tile
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+        run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
@@ -805,7 +811,7 @@ __global__ void __launch_bounds__(NT) factor_ordered_kernel(DevTasks tk, T* tile
     if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 
-template <typename T>
+template <typename T, int S>
 __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles, const int32_t* items) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
@@ -813,32 +819,32 @@ __global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles,
     uint32_t phase = 0;
     if constexpr (sizeof(T) == 4) tc_setup(st);
     const int item = items[blockIdx.x];
-    run_item<T>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+    run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
     if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 
-template <typename T>
+template <typename T, int S>
 int queue_launch(const DevTasks& t, T* tiles, int grid, cudaStream_t s) {
-    const size_t smem = smem_elems<T>() * sizeof(T);
-    cudaFuncSetAttribute(factor_queue_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    factor_queue_kernel<T><<<grid, NT, smem, s>>>(t, tiles);
+    const size_t smem = smem_elems<T, S>() * sizeof(T);
+    cudaFuncSetAttribute(factor_queue_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    factor_queue_kernel<T, S><<<grid, NT, smem, s>>>(t, tiles);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <typename T>
+template <typename T, int S>
 int ordered_launch(const DevTasks& t, T* tiles, int grid, cudaStream_t s) {
-    const size_t smem = smem_elems<T>() * sizeof(T);
-    cudaFuncSetAttribute(factor_ordered_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    factor_ordered_kernel<T><<<grid, NT, smem, s>>>(t, tiles);
+    const size_t smem = smem_elems<T, S>() * sizeof(T);
+    cudaFuncSetAttribute(factor_ordered_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    factor_ordered_kernel<T, S><<<grid, NT, smem, s>>>(t, tiles);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <typename T>
+template <typename T, int S>
 int level_launch(const DevTasks& t, T* tiles, const int32_t* items, int nitems, cudaStream_t s) {
     if (nitems <= 0) return 0;
-    const size_t smem = smem_elems<T>() * sizeof(T);
-    cudaFuncSetAttribute(factor_level_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    factor_level_kernel<T><<<nitems, NT, smem, s>>>(t, tiles, items);
+    const size_t smem = smem_elems<T, S>() * sizeof(T);
+    cudaFuncSetAttribute(factor_level_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    factor_level_kernel<T, S><<<nitems, NT, smem, s>>>(t, tiles, items);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -872,27 +878,26 @@ __global__ void widen_kernel(const float* __restrict__ s, double* __restrict__ d
 
 }  // namespace
 
-int factor_queue_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s) {
-    return queue_launch<double>(t, tiles, grid, s);
+// The FP64 path has no tensor-memory stages (S is unused there: one instance).
+int factor_queue_launch(const DevTasks& t, double* tiles, int grid, int, cudaStream_t s) {
+    return queue_launch<double, 2>(t, tiles, grid, s);
 }
-int factor_queue_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s) {
-    return queue_launch<float>(t, tiles, grid, s);
+int factor_queue_launch(const DevTasks& t, float* tiles, int grid, int stages, cudaStream_t s) {
+    return stages == 1 ? queue_launch<float, 1>(t, tiles, grid, s) : queue_launch<float, 2>(t, tiles, grid, s);
 }
-int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s) {
-    return ordered_launch<double>(t, tiles, grid, s);
+int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, int, cudaStream_t s) {
+    return ordered_launch<double, 2>(t, tiles, grid, s);
 }
-int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s) {
-    return ordered_launch<float>(t, tiles, grid, s);
+int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, int stages, cudaStream_t s) {
+    return stages == 1 ? ordered_launch<float, 1>(t, tiles, grid, s) : ordered_launch<float, 2>(t, tiles, grid, s);
 }
-int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, cudaStream_t s) {
-    return level_launch<double>(t, tiles, items, nitems, s);
+int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, int, cudaStream_t s) {
+    return level_launch<double, 2>(t, tiles, items, nitems, s);
 }
-int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, cudaStream_t s) {
-    return level_launch<float>(t, tiles, items, nitems, s);
-}
-
-size_t factor_smem_bytes(bool fp64) {
-    return fp64 ? smem_elems<double>() * sizeof(double) : smem_elems<float>() * sizeof(float);
+int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, int stages,
+                        cudaStream_t s) {
+    return stages == 1 ? level_launch<float, 1>(t, tiles, items, nitems, s)
+                       : level_launch<float, 2>(t, tiles, items, nitems, s);
 }
 
 template <typename K>
@@ -903,13 +908,22 @@ int resident_per_sm(K kernel, size_t smem) {
     return per_sm < 1 ? 1 : per_sm;
 }
 
-int factor_persistent_grid(bool fp64, int num_sms) {
+int factor_persistent_grid(bool fp64, int stages, int num_sms) {
     // both persistent executors launch this many CTAs: the smaller residency of the two
-    const size_t smem = factor_smem_bytes(fp64);
-    int per_sm = fp64 ? std::min(resident_per_sm(factor_queue_kernel<double>, smem),
-                                 resident_per_sm(factor_ordered_kernel<double>, smem))
-                      : std::min(resident_per_sm(factor_queue_kernel<float>, smem),
-                                 resident_per_sm(factor_ordered_kernel<float>, smem));
+    int per_sm;
+    if (fp64) {
+        const size_t smem = smem_elems<double, 2>() * sizeof(double);
+        per_sm = std::min(resident_per_sm(factor_queue_kernel<double, 2>, smem),
+                          resident_per_sm(factor_ordered_kernel<double, 2>, smem));
+    } else if (stages == 1) {
+        const size_t smem = smem_elems<float, 1>() * sizeof(float);
+        per_sm = std::min(resident_per_sm(factor_queue_kernel<float, 1>, smem),
+                          resident_per_sm(factor_ordered_kernel<float, 1>, smem));
+    } else {
+        const size_t smem = smem_elems<float, 2>() * sizeof(float);
+        per_sm = std::min(resident_per_sm(factor_queue_kernel<float, 2>, smem),
+                          resident_per_sm(factor_ordered_kernel<float, 2>, smem));
+    }
     return per_sm * num_sms;
 }
 

@@ -50,15 +50,18 @@ struct DevTasks {
 
 // ---- factor (factor.cu) ----
 // tiles: block id -> tiles + id*4096 elements. double => SOG_FP64, float => SOG_MIXED.
-int factor_queue_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
-int factor_queue_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
+// stages: tensor-core operand stages of the mixed path (1 or 2; ignored for FP64).
+int factor_queue_launch(const DevTasks& t, double* tiles, int grid, int stages, cudaStream_t s);
+int factor_queue_launch(const DevTasks& t, float* tiles, int grid, int stages, cudaStream_t s);
 // ordered executor: one persistent launch claiming items in the static order
-int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, cudaStream_t s);
-int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, cudaStream_t s);
-int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, cudaStream_t s);
-int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, cudaStream_t s);
+int factor_ordered_launch(const DevTasks& t, double* tiles, int grid, int stages, cudaStream_t s);
+int factor_ordered_launch(const DevTasks& t, float* tiles, int grid, int stages, cudaStream_t s);
+int factor_level_launch(const DevTasks& t, double* tiles, const int32_t* items, int nitems, int stages,
+                        cudaStream_t s);
+int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, int nitems, int stages,
+                        cudaStream_t s);
 // persistent grid size (CTAs co-resident on the device)
-int factor_persistent_grid(bool fp64, int num_sms);
+int factor_persistent_grid(bool fp64, int stages, int num_sms);
 size_t factor_smem_bytes(bool fp64);
 
 // value scatter into input tiles: tiles[tile[k]*4096 + off[k]] = V[k] (tile < 0: skip)

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -180,6 +181,8 @@ struct sog_system {
     bool factored = false;
     float t_factor = 0, t_solve = 0;
     int grid_factor = 0;
+    int stages = 2;           // tensor-core operand stages of the mixed path
+    bool tune_pending = false;  // time the candidate configurations at the next factorisation
     int64_t launches = 0;  // kernels launched by this system
     unsigned long long* trace = nullptr;  // optional timing trace (tasks, then block rows)
     uint64_t trace_bytes = 0;
@@ -188,6 +191,31 @@ struct sog_system {
 };
 
 namespace {
+
+// Tuning memory: task graphs of about the same size and parallelism (tasks per
+// dependency level) behave alike.
+struct Tuned {
+    int executor, stages;
+};
+std::mutex g_tune_mu;
+std::map<uint64_t, Tuned> g_tuned;
+uint64_t tune_key(const TaskGraph& g, bool fp64) {
+    const double par = (double)g.ntasks / std::max(1, g.nlevels);
+    const uint64_t a = (uint64_t)std::lround(2.0 * std::log2(std::max(1.0, par)));
+    const uint64_t b = (uint64_t)std::lround(2.0 * std::log2(std::max(1.0, (double)g.ntasks)));
+    return (a << 32) | (b << 1) | (fp64 ? 1 : 0);
+}
+bool tuned_config(uint64_t key, Tuned& t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it == g_tuned.end()) return false;
+    t = it->second;
+    return true;
+}
+void remember_config(uint64_t key, const Tuned& t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = t;
+}
 
 sog_options default_options() {
     sog_options o;
@@ -320,7 +348,7 @@ int check_status(sog_system* s, bool factor) {
     return SOG_OK;
 }
 
-int run_factor(sog_system* s) {
+int run_factor_once(sog_system* s) {
     sog_ctx* c = s->ctx;
     cudaStream_t st = c->stream;
     const TaskGraph& g = s->tg;
@@ -340,17 +368,17 @@ int run_factor(sog_system* s) {
     if (s->opt.executor == SOG_EXEC_LEVELS) {
         for (int l = 0; l < g.nlevels && rc == 0; l++) {
             const int a = g.level_ptr[l], b = g.level_ptr[l + 1];
-            rc = s->fp64 ? factor_level_launch(s->dt, (double*)s->tiles, s->d_level_items + a, b - a, st)
-                         : factor_level_launch(s->dt, (float*)s->tiles, s->d_level_items + a, b - a, st);
+            rc = s->fp64 ? factor_level_launch(s->dt, (double*)s->tiles, s->d_level_items + a, b - a, s->stages, st)
+                         : factor_level_launch(s->dt, (float*)s->tiles, s->d_level_items + a, b - a, s->stages, st);
             s->launches++;
         }
     } else if (s->opt.executor == SOG_EXEC_QUEUE) {
-        rc = s->fp64 ? factor_queue_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
-                     : factor_queue_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
+        rc = s->fp64 ? factor_queue_launch(s->dt, (double*)s->tiles, s->grid_factor, s->stages, st)
+                     : factor_queue_launch(s->dt, (float*)s->tiles, s->grid_factor, s->stages, st);
         s->launches++;
     } else {
-        rc = s->fp64 ? factor_ordered_launch(s->dt, (double*)s->tiles, s->grid_factor, st)
-                     : factor_ordered_launch(s->dt, (float*)s->tiles, s->grid_factor, st);
+        rc = s->fp64 ? factor_ordered_launch(s->dt, (double*)s->tiles, s->grid_factor, s->stages, st)
+                     : factor_ordered_launch(s->dt, (float*)s->tiles, s->grid_factor, s->stages, st);
         s->launches++;
     }
     if (rc) return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -361,6 +389,40 @@ int run_factor(sog_system* s) {
     if (r) return r;
     s->factored = true;
     return SOG_OK;
+}
+
+// Autotuning (SOG_EXEC_AUTO): the first factorisation of a system whose kind
+// of task graph has not been seen runs every candidate configuration twice
+// (the second run is timed) and keeps the fastest; the choice is remembered
+// per key. Candidates: the static-order and the ready-queue executors, and for
+// SOG_MIXED one operand stage where that lets two CTAs share an SM.
+int run_factor(sog_system* s) {
+    if (!s->tune_pending) return run_factor_once(s);
+    s->tune_pending = false;
+    std::vector<Tuned> cands = {{SOG_EXEC_PERSISTENT, 2}, {SOG_EXEC_QUEUE, 2}};
+    const int sms = s->ctx->num_sms;
+    if (!s->fp64 && factor_persistent_grid(false, 1, sms) > factor_persistent_grid(false, 2, sms))
+        cands.push_back({SOG_EXEC_PERSISTENT, 1});
+    float best = 1e30f;
+    Tuned pick = cands[0];
+    for (const Tuned& c : cands) {
+        s->opt.executor = c.executor;
+        s->stages = c.stages;
+        s->grid_factor = factor_persistent_grid(s->fp64, c.stages, sms);
+        for (int rep = 0; rep < 2; rep++) {
+            const int r = run_factor_once(s);
+            if (r) return r;
+        }
+        if (s->t_factor < best) {
+            best = s->t_factor;
+            pick = c;
+        }
+    }
+    remember_config(tune_key(s->tg, s->fp64), pick);
+    s->opt.executor = pick.executor;
+    s->stages = pick.stages;
+    s->grid_factor = factor_persistent_grid(s->fp64, pick.stages, sms);
+    return run_factor_once(s);
 }
 
 int trisolve(sog_system* s, void* vec, int nrhs) {
@@ -646,7 +708,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     *out = nullptr;
     sog_options o = opt ? *opt : default_options();
     if (o.precision != SOG_FP64 && o.precision != SOG_MIXED) return fail(SOG_EINVAL, "bad precision");
-    if (o.executor != SOG_EXEC_PERSISTENT && o.executor != SOG_EXEC_LEVELS && o.executor != SOG_EXEC_QUEUE)
+    if (o.executor != SOG_EXEC_PERSISTENT && o.executor != SOG_EXEC_LEVELS && o.executor != SOG_EXEC_QUEUE &&
+        o.executor != SOG_EXEC_AUTO)
         return fail(SOG_EINVAL, "bad executor");
     if (o.tol <= 0) o.tol = 1e-10;
     if (o.max_refine < 0) o.max_refine = 0;
@@ -880,7 +943,18 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         return fail(SOG_ENOMEM, "pinned host buffers");
     }
     s->d_V = reinterpret_cast<double*>(A + o_V);
-    s->grid_factor = factor_persistent_grid(s->fp64, c->num_sms);
+    s->stages = o.pipeline_stages == 1 ? 1 : 2;
+    if (o.executor == SOG_EXEC_AUTO) {
+        Tuned known;
+        if (tuned_config(tune_key(g, s->fp64), known)) {
+            s->opt.executor = known.executor;
+            s->stages = known.stages;
+        } else {
+            s->opt.executor = SOG_EXEC_PERSISTENT;
+            s->tune_pending = true;
+        }
+    }
+    s->grid_factor = factor_persistent_grid(s->fp64, s->stages, c->num_sms);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         std::string m = cudaGetErrorString(cudaGetLastError());
         sog_system_destroy(s);

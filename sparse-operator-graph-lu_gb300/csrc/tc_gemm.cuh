@@ -27,8 +27,9 @@ constexpr int ROW_GROUP_BYTES = 8 * 64 * 4;                 // 8 rows x K=64 fp3
 constexpr int A_BYTES = 128 / 8 * ROW_GROUP_BYTES;         // [A_hi; A_lo] = 32768
 constexpr int B_BYTES = 64 / 8 * ROW_GROUP_BYTES;          // 16384 per part
 constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;         // 65536
-constexpr int STAGES = 2;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES;           // 131072
+// operand stages per CTA: 2 (the next pair stages while this one's MMAs run,
+// 128 KB, one CTA per SM) or 1 (64 KB, two CTAs per SM)
+constexpr int MAX_STAGES = 2;
 constexpr uint32_t TMEM_COLS = 64;
 
 // byte offset of element (row, k) in the K-major core-matrix layout:
@@ -134,7 +135,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // holds, per stage s, the parity of that stage's next mbarrier phase (bit s);
 // pending, per stage, whether a commit on it is not yet waited for.
 struct State {
-    uint64_t bar[STAGES];
+    uint64_t bar[MAX_STAGES];
     uint32_t tmem;
     int32_t fail;
 };

@@ -149,3 +149,24 @@ def test_bench_config_fp64_vs_reference(sg, wl, ctx):
     assert st["rel_resid"] <= 1e-10
     assert rel(x, g["x"]) <= 1e-7
     sys_.close()
+
+
+@pytest.mark.parametrize("cfg", [(0, 1), (0, 2), (3, 0)], ids=["one-stage", "two-stage", "autotuned"])
+@pytest.mark.parametrize("name", ["lap2d_32", "var3d_16"])
+def test_mixed_pipeline_and_autotune(sg, wl, ctx, name, cfg):
+    """The mixed path with one or two tensor-core operand stages, and with the
+    executor configuration picked by timing the candidates, converges; the
+    autotuned system keeps a persistent grid of whole SMs."""
+    executor, stages = cfg
+    s = golden_cases(wl)[name]()
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=executor, pipeline_stages=stages)
+    sys_.factor(s.vals)
+    x, st = sys_.solve(rhs_of(s))
+    assert st["rel_resid"] <= 1e-10
+    import torch
+    assert sys_.task_info()["grid"] % torch.cuda.get_device_properties(0).multi_processor_count == 0
+    sys_.factor(s.vals)  # the tuned choice is reused
+    x2, st2 = sys_.solve(rhs_of(s))
+    assert st2["rel_resid"] <= 1e-10
+    sys_.close()
