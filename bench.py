@@ -129,8 +129,8 @@ MEASURED = _measured_peaks()
 
 # DRAM bytes (read + write) of one mixed factor launch, from a one-pass ncu
 # capture of the full-size launch (dram__bytes_read.sum + dram__bytes_write.sum:
-# 421.45 MB + 3.83 GB at var48); None where no capture covers the workload
-TRAFFIC: dict = {"var48": 421.45e6 + 3.83e9}
+# 251.71 MB + 3.45 GB at var48); None where no capture covers the workload
+TRAFFIC: dict = {"var48": 251.71e6 + 3.45e9}
 
 
 def algorithmic_flops(op_count) -> float:
@@ -470,8 +470,8 @@ def run_ours(args):
         # 3xTF32: three TF32 products per FP32 product -> effective peak = TF32 peak / 3
         eff_peak = peaks["tf32_tflops"] / 3
         ach = flops / (fm * 1e-3) / 1e12
-        roof = {"bound": "tensor", "kernel": "factor_persistent_kernel<float> (3xTF32 tile products + LU/inverse "
-                                                "tasks, one launch per factorisation)",
+        roof = {"bound": "tensor", "kernel": "factor_ordered_kernel<float> (3xTF32 tile products on tcgen05 + LU/"
+                                                "inverse tasks, one launch per factorisation)",
                 "achieved": ach, "peak": eff_peak, "unit": "TFLOP/s", "frac": ach / eff_peak,
                 "traffic": TRAFFIC.get(args.workload),
                 "peak_source": f"cuBLAS TF32 GEMM measured in this run ({peaks['tf32_tflops']:.1f} TFLOP/s) / 3",
@@ -523,6 +523,7 @@ def run_ours(args):
                        "factor_ctas": grid_mixed, "pipeline_stages": args.stages or "tuned"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),
+            "factor_ms_steps": [round(v, 3) for v in rm["factor_ms"]],
             "rel_resid": rm["stats"]["rel_resid"], "backward_error": rm["stats"]["backward_error"], **fwd,
             "fp64_plain": {"value": v64, "unit": "solves/s", "steps": k64, "ms_per_step": r64["ms"] / k64,
                            "factor_ms": f64m, "solve_ms": statistics.mean(r64["solve_ms"]),
