@@ -128,6 +128,20 @@ int sog_plan_import(int32_t block_rows, int32_t storage_count, int32_t n_input, 
                     const int32_t *lleaf, int64_t n_lleaf, const int32_t *uleaf, int64_t n_uleaf, sog_plan **out);
 void sog_plan_destroy(sog_plan *plan);
 
+/* ---- MatrixMarket input --------------------------------------------------------
+ * SOGLU::mtx::readMTX (mtx.cpp:44-117): coordinate file, header "symmetric" =>
+ * lower triangle given; lines of <= 3 characters and lines containing '%'
+ * skipped; zero values dropped; 1-based indices (returned 0-based). Entry
+ * lines are parsed in parallel chunks, in file order. use_cache: read
+ * <path>.sogbin when it matches the text file's size and modification time,
+ * else parse and write it (no reference counterpart). */
+typedef struct sog_mtx sog_mtx;
+int sog_mtx_read(const char *path, int32_t use_cache, sog_mtx **out);
+int sog_mtx_info(const sog_mtx *m, int32_t *n, int64_t *nnz, int32_t *symmetric);
+/* copy the triplets out (arrays of nnz entries; any pointer may be NULL) */
+int sog_mtx_copy(const sog_mtx *m, int32_t *I, int32_t *J, double *V);
+void sog_mtx_destroy(sog_mtx *m);
+
 /* ---- batches -----------------------------------------------------------------
  * No counterpart in the reference, which factors one system per process
  * (solver.cpp:121). A batch plan is the block-diagonal union of independent

@@ -87,7 +87,7 @@ EXPORTS = [
     "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
     "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
-    "sog_server_destroy",
+    "sog_server_destroy", "sog_mtx_read", "sog_mtx_info", "sog_mtx_copy", "sog_mtx_destroy",
 ]
 
 _lib = None
@@ -128,6 +128,8 @@ def lib() -> C.CDLL:
         "sog_server_wait": ([P, I64, D, P, P], I32), "sog_server_solve": ([P, I64, I32, P, P, P], I32),
         "sog_server_release": ([P, I64], I32), "sog_server_counters": ([P, P], I32),
         "sog_server_destroy": ([P], None),
+        "sog_mtx_read": ([C.c_char_p, I32, P], I32), "sog_mtx_info": ([P, P, P, P], I32),
+        "sog_mtx_copy": ([P, P, P, P], I32), "sog_mtx_destroy": ([P], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -484,6 +486,23 @@ class Server:
     def __del__(self):
         if _lib is not None:
             self.close()
+
+
+def read_mtx(path: str, cache: bool = False):
+    """MatrixMarket coordinate file with the reference reader's rules
+    (sog_mtx_read): (n, rows, cols, vals, symmetric), 0-based."""
+    h = C.c_void_p()
+    _check(lib().sog_mtx_read(os.fsencode(path), int(cache), C.byref(h)))
+    try:
+        n, nnz, sym = C.c_int32(), C.c_int64(), C.c_int32()
+        _check(lib().sog_mtx_info(h, C.byref(n), C.byref(nnz), C.byref(sym)))
+        r = np.empty(nnz.value, np.int32)
+        c = np.empty(nnz.value, np.int32)
+        v = np.empty(nnz.value, np.float64)
+        _check(lib().sog_mtx_copy(h, _p(r), _p(c), _p(v)))
+        return n.value, r, c, v, bool(sym.value)
+    finally:
+        lib().sog_mtx_destroy(h)
 
 
 def solveLU(dim: int, rows, cols, vals, b, symmetric: bool = False, precision: int = FP64) -> np.ndarray:

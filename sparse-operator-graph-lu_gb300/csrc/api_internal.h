@@ -12,6 +12,11 @@ struct sog_plan {
     int64_t nnz = 0;  // triplets as given (before mirroring)
 };
 
+struct sog_mtx {
+    sog::MtxData d;
+    bool from_cache = false;
+};
+
 namespace sog_internal {
 extern thread_local std::string g_err;
 int fail(int code, const std::string& msg);

@@ -123,6 +123,9 @@ struct MtxData {
     std::vector<double> V;
 };
 bool read_mtx(const std::string& path, MtxData& out, std::string& err);
+// read_mtx through a binary cache <path>.sogbin (written after a text parse,
+// used while the text file's size and modification time are unchanged)
+bool read_mtx_cached(const std::string& path, MtxData& out, std::string& err, bool* from_cache = nullptr);
 // Array reader (mtx.cpp:145-181): missing entries are 1.
 std::vector<double> read_rhs(const std::string& path, int n);
 

@@ -170,4 +170,43 @@ int sog_plan_segments(const sog_plan* plan, int32_t* count, int32_t* n) {
 
 void sog_plan_destroy(sog_plan* plan) { delete plan; }
 
+int sog_mtx_read(const char* path, int32_t use_cache, sog_mtx** out) {
+    if (!path || !out) return fail(SOG_EINVAL, "NULL argument");
+    *out = nullptr;
+    try {
+        sog_mtx* m = new sog_mtx();
+        std::string err;
+        bool cached = false;
+        const bool ok = use_cache ? sog::read_mtx_cached(path, m->d, err, &cached) : sog::read_mtx(path, m->d, err);
+        if (!ok) {
+            delete m;
+            return fail(SOG_EINVAL, err);
+        }
+        m->from_cache = cached;
+        *out = m;
+        return SOG_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(SOG_ENOMEM, "host allocation failed while reading");
+    }
+}
+
+int sog_mtx_info(const sog_mtx* m, int32_t* n, int64_t* nnz, int32_t* symmetric) {
+    if (!m) return fail(SOG_EINVAL, "NULL matrix");
+    if (n) *n = m->d.n;
+    if (nnz) *nnz = (int64_t)m->d.I.size();
+    if (symmetric) *symmetric = m->d.symmetric ? 1 : 0;
+    return SOG_OK;
+}
+
+int sog_mtx_copy(const sog_mtx* m, int32_t* I, int32_t* J, double* V) {
+    if (!m) return fail(SOG_EINVAL, "NULL matrix");
+    const size_t k = m->d.I.size();
+    if (I) std::memcpy(I, m->d.I.data(), 4 * k);
+    if (J) std::memcpy(J, m->d.J.data(), 4 * k);
+    if (V) std::memcpy(V, m->d.V.data(), 8 * k);
+    return SOG_OK;
+}
+
+void sog_mtx_destroy(sog_mtx* m) { delete m; }
+
 }  // extern "C"

@@ -9,6 +9,7 @@
 //
 // options: --mixed (FP32 factors + FP64 refinement) | --fp64 (default)
 //          --levels (stage-synchronous executor) --queue (ready-queue executor)
+//          --cache (binary cache of the parsed matrix beside the .mtx file)
 //          --device N --threads N
 #include <chrono>
 #include <cmath>
@@ -28,11 +29,12 @@ static double now_s() {
 
 int main(int argc, char** argv) {
     if (argc <= 1 || std::string(argv[1]).find(".mtx") == std::string::npos) {
-        std::printf("usage: ./solve filename.mtx [--fp64|--mixed] [--levels|--queue] [--device N] [--threads N]\n");
+        std::printf("usage: ./solve filename.mtx [--fp64|--mixed] [--levels|--queue] [--cache] [--device N] [--threads N]\n");
         return 0;
     }
     std::string fname = argv[1];
     int precision = SOG_FP64, executor = SOG_EXEC_PERSISTENT, device = 0, threads = 0;
+    bool cache = false;
     for (int i = 2; i < argc; i++) {
         std::string a = argv[i];
         if (a == "--mixed") precision = SOG_MIXED;
@@ -41,15 +43,18 @@ int main(int argc, char** argv) {
         else if (a == "--queue") executor = SOG_EXEC_QUEUE;
         else if (a == "--device" && i + 1 < argc) device = std::atoi(argv[++i]);
         else if (a == "--threads" && i + 1 < argc) threads = std::atoi(argv[++i]);
+        else if (a == "--cache") cache = true;
     }
     std::string base = fname.substr(0, fname.find(".mtx"));
     sog::MtxData m;
     std::string err;
-    if (!sog::read_mtx(fname, m, err) || m.I.empty()) {
+    const double tr = now_s();
+    if (!(cache ? sog::read_mtx_cached(fname, m, err) : sog::read_mtx(fname, m, err)) || m.I.empty()) {
         std::printf("%s\n", err.empty() ? "empty matrix" : err.c_str());
         return 1;
     }
     std::vector<double> b = sog::read_rhs(base + "_b.mtx", m.n);
+    std::printf("read time: %g\n", now_s() - tr);
     double t0 = now_s();
     sog_plan* plan = nullptr;
     int r = sog_plan_build(m.n, (int64_t)m.I.size(), m.symmetric, m.I.data(), m.J.data(), m.V.data(), threads, &plan);

@@ -68,3 +68,41 @@ def test_mtx_reader_acceptance_rules(sg, tmp_path):
     r = subprocess.run([exe, str(p)], capture_output=True, text=True, timeout=60)
     # 66 accepted entries, n = 64 -> 2 block rows, one lu per block row
     assert "inputSize: 64" in r.stdout and "op count: 2" in r.stdout
+
+
+def test_mtx_reader_triplets_parallel_and_cache(sg, wl, tmp_path):
+    """sog_mtx_read returns the accepted triplets in file order, also when the
+    entry lines are parsed in parallel chunks (a file of several MB), and the
+    binary cache returns the same triplets until the text file changes."""
+    import numpy as np
+    s = wl.lap3d(40)  # 438k entries: several parallel chunks
+    p = tmp_path / "lap.mtx"
+    with open(p, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate real general\n%\n")
+        f.write(f"{s.n} {s.n} {s.nnz + 3}\n")
+        f.write("1 1 0\n")  # zero value: dropped
+        for k in range(s.nnz):
+            f.write(f"{s.rows[k] + 1} {s.cols[k] + 1} {float(s.vals[k])!r}\n")
+            if k == s.nnz // 2:
+                f.write("% a comment in the middle\n12\n")  # skipped lines
+        f.write(f"{s.n + 5} 1 3.0\n")  # beyond the size: dropped
+    n, r, c, v, sym = sg.read_mtx(str(p))
+    assert n == s.n and not sym
+    np.testing.assert_array_equal(r, s.rows)
+    np.testing.assert_array_equal(c, s.cols)
+    np.testing.assert_array_equal(v, s.vals)
+    cache = tmp_path / "lap.mtx.sogbin"
+    assert not cache.exists()
+    first = sg.read_mtx(str(p), cache=True)
+    assert cache.exists()
+    second = sg.read_mtx(str(p), cache=True)
+    for a, b in zip(first[1:4], second[1:4]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(second[3], s.vals)
+    # the text file changes: the stale cache is not used
+    with open(p, "a") as f:
+        f.write("1 2 -0.5\n")
+    third = sg.read_mtx(str(p), cache=True)
+    assert third[1].size == s.nnz + 1 and third[3][-1] == -0.5
+    with pytest.raises(sg.SOGError):
+        sg.read_mtx(str(tmp_path / "missing.mtx"))
