@@ -106,7 +106,8 @@ const char *sog_version(void);
  * GOrder::sortInBlock (GPSOrder.cpp:55-650), config::set (config.cpp:41),
  * blockMatrixLU + copyOperatorL2 + blockPlan (BlockPlanner.cpp:103-374,
  * 865-1577). I/J are 0-based; symmetric = lower triangle given (mtx.cpp:60,
- * solver.cpp:132-149; the LL^T path is not built: symmetric returns SOG_EINVAL).
+ * solver.cpp:132-149; the LL^T recursion, BlockPlanner.cpp:941-989, with llt
+ * and mult ops and L leaves only).
  * threads = OpenMP threads for the ordering search (0 = default). */
 int sog_plan_build(int32_t n, int64_t nnz, int32_t symmetric, const int32_t *I, const int32_t *J,
                    const double *V, int32_t threads, sog_plan **out);
@@ -208,7 +209,8 @@ int sog_solve_batch_device(sog_system *sys, const int32_t *nrhs, const double *b
  * in the planner's (permuted, padded) ordering; one right-hand side; no
  * refinement. */
 int sog_solve_permuted(sog_system *sys, const double *b_ext, double *x_ext);
-/* Copy resident L/U leaf tiles (in plan leaf order) to host, FP64. */
+/* Copy resident L/U leaf tiles (in plan leaf order) to host, FP64 (an LL^T
+ * plan has L leaves only). */
 int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
 /* Device time of the last factor / solve in milliseconds (CUDA events on the
  * context's stream). */

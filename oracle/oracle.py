@@ -65,11 +65,25 @@ def solve(block_rows: int, L: np.ndarray, U: np.ndarray, tiles: np.ndarray, b_ex
     return x, int(nan)
 
 
+def transposed_upper(L: np.ndarray, tiles: np.ndarray):
+    """For an LL^T plan (no U leaves): U = L^T as leaves over transposed copies
+    of the L tiles appended to `tiles` (upperSolverT, BlockPlanner.cpp:752-797,
+    solves with the transposed L blocks). Returns (tiles, U leaves)."""
+    L = np.asarray(L, dtype=np.int32).reshape(-1, 3)
+    extra = np.ascontiguousarray(np.transpose(tiles[L[:, 2]], (0, 2, 1)))
+    ids = np.arange(tiles.shape[0], tiles.shape[0] + L.shape[0], dtype=np.int32)
+    U = np.stack([L[:, 1], L[:, 0], ids], axis=1).astype(np.int32)
+    return np.concatenate([tiles, extra]), U
+
+
 def solve_system(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, storage_count, input_tiles, L, U,
                  b: np.ndarray, threads: int = 0):
     """Full executor path in the original ordering: permute b (padded rows = 1,
-    solver.cpp:159-161), calculate, substitute, un-permute (GPSOrder.cpp:41-53)."""
+    solver.cpp:159-161), calculate, substitute, un-permute (GPSOrder.cpp:41-53).
+    An empty U means an LL^T plan: the back substitution uses L^T."""
     tiles = calculate(ops, storage_count, input_tiles, threads)
+    if len(U) == 0:
+        tiles, U = transposed_upper(L, tiles)
     b_ext = np.ones(block_rows * 64)
     b_ext[:n] = np.asarray(b)[perm_new_to_old]
     x_ext, nan = solve(block_rows, L, U, tiles, b_ext)
@@ -83,6 +97,8 @@ def solve_system_multi(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops
     """One calculate, then one substitution per right-hand side (rows of B,
     original ordering): the reference's factor-once, solve-each path."""
     tiles = calculate(ops, storage_count, input_tiles, threads)
+    if len(U) == 0:
+        tiles, U = transposed_upper(L, tiles)
     B = np.atleast_2d(np.asarray(B, dtype=np.float64))
     X = np.empty_like(B)
     for r in range(B.shape[0]):

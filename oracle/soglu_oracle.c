@@ -5,7 +5,7 @@
  *
  * A plain-C restatement of the reference's executor path for one system:
  *   oracle_calculate : BlockPlanner::calculate (BlockPlanner.cpp:376-651) with
- *                      the unit ops of MatrixStdDouble.cpp
+ *                      the unit ops of MatrixStdDouble.cpp (LU and LL^T paths)
  *   oracle_solve     : BlockPlanner::solve (BlockPlanner.cpp:652-862)
  * on dense 64x64 row-major FP64 tiles indexed by block id. Like the reference
  * it runs each stage's ops in parallel (OpenMP), serialising ops that write
@@ -25,7 +25,8 @@
 #define B 64
 #define TILE (B * B)
 
-enum { OP_INV = 0, OP_LU = 1, OP_LOWERINV = 2, OP_UPPERINV = 3, OP_SUB = 4, OP_MUL = 8, OP_MULNEG = 9 };
+enum { OP_INV = 0, OP_LU = 1, OP_LOWERINV = 2, OP_UPPERINV = 3, OP_SUB = 4, OP_MUL = 8, OP_MULNEG = 9, OP_LLT = 10,
+       OP_MULT = 11 };
 
 /* 8x8 occupancy: bit kb of m[ib] set when sub-tile (ib, kb) has a nonzero. */
 static void occupancy(const double *t, uint8_t m[8]) {
@@ -89,6 +90,37 @@ static void tile_lu(const double *a, double *l, double *u) {
             l[j * B + i] = r * (a[j * B + i] - s);
         }
         l[i * B + i] = 1.0;
+    }
+}
+
+/* C += A * B^T (mat_mult, MatrixStdDouble.cpp:704-1555). */
+static void tile_mult(double *restrict c, const double *restrict a, const double *restrict b) {
+    for (int i = 0; i < B; i++)
+        for (int j = 0; j < B; j++) {
+            double s = 0;
+            for (int k = 0; k < B; k++) s += a[i * B + k] * b[j * B + k];
+            c[i * B + j] += s;
+        }
+}
+
+/* Cholesky L L^T = A from the lower triangle of a, column by column; pivots
+ * below 1e-20 (TINY, MatrixStdDouble.cpp:29) are raised to it before the
+ * square root (lltdcmpSimple, MatrixStdDouble.cpp:2629-2668). */
+static void tile_llt(const double *a, double *l) {
+    memset(l, 0, sizeof(double) * TILE);
+    for (int j = 0; j < B; j++) {
+        double s = 0;
+        for (int r = 0; r < j; r++) s += l[j * B + r] * l[j * B + r];
+        double p = a[j * B + j] - s;
+        if (p < 1e-20) p = 1e-20;
+        p = sqrt(p);
+        l[j * B + j] = p;
+        const double rp = 1.0 / p;
+        for (int i = j + 1; i < B; i++) {
+            double t = 0;
+            for (int r = 0; r < j; r++) t += l[i * B + r] * l[j * B + r];
+            l[i * B + j] = rp * (a[i * B + j] - t);
+        }
     }
 }
 
@@ -176,6 +208,8 @@ int oracle_calculate(int64_t nops, const int32_t *ops_flat, int32_t storage_coun
                     case OP_UPPERINV: tile_inv_upper(a, r); break;
                     case OP_MUL: tile_gemm(r, a, b2, 1.0); break;
                     case OP_MULNEG: tile_gemm(r, a, b2, -1.0); break;
+                    case OP_LLT: tile_llt(a, r); break;
+                    case OP_MULT: tile_mult(r, a, b2); break;
                     case OP_SUB: /* r = src2 - src; copy / negate when one is absent (BlockPlanner.cpp:553-572) */
                         for (int e = 0; e < TILE; e++) {
                             double v = 0;

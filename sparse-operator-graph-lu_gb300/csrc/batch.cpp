@@ -50,8 +50,10 @@ Plan merge_plans(const std::vector<const Plan*>& ps) {
     m.pad_off.reserve(npad);
     m.ord.new_to_old.assign(R * 64, -1);
 
+    bool any_mirror = false;
+    for (const Plan* p : ps) any_mirror = any_mirror || !p->mirror_src.empty();
     int32_t in_off = 0, other_off = (int32_t)n_in, row_blocks = 0;
-    int64_t noff = 0, toff = 0;
+    int64_t noff = 0, toff = 0, voff = 0;
     for (size_t k = 0; k < ps.size(); k++) {
         const Plan& p = *ps[k];
         const int32_t ni = p.n_input;
@@ -74,6 +76,9 @@ Plan merge_plans(const std::vector<const Plan*>& ps) {
             m.scatter_tile.push_back(t < 0 ? t : t + in_off);
             m.scatter_off.push_back(p.scatter_off[q]);
         }
+        if (any_mirror)
+            for (size_t q = 0; q < p.scatter_tile.size(); q++)
+                m.mirror_src.push_back((int32_t)(voff + (p.mirror_src.empty() ? (int64_t)q : p.mirror_src[q])));
         for (size_t q = 0; q < p.pad_tile.size(); q++) {
             m.pad_tile.push_back(p.pad_tile[q] + in_off);
             m.pad_off.push_back(p.pad_off[q]);
@@ -99,7 +104,10 @@ Plan merge_plans(const std::vector<const Plan*>& ps) {
         row_blocks += p.cfg.block_rows;
         noff += p.cfg.n;
         toff += (int64_t)p.scatter_tile.size();
+        voff += p.nval;
     }
+    m.nval = voff;
+    if (voff > std::numeric_limits<int32_t>::max()) throw std::runtime_error("merge_plans: too many values");
     // the executor contract: ops ascending by stage (stable, so each system's
     // own order is kept and systems follow one another within a stage)
     std::vector<int64_t> order(m.ops.size());

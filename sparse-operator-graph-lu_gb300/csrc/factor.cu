@@ -91,17 +91,23 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3, rg = warp & 3, ch = warp >> 2;
     const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
+    // stage: sA = A rows r0..r0+31; sB = B[0:64][c0:c0+32] as [k][40], or for
+    // a transposed operand X (B = X^T) the rows X[c0:c0+32][0:64] as [n][68]
     auto issue = [&](int p, int s) {
         double* sA = sm + s * F64_STAGE;
         double* sB = sA + 32 * 68;
-        const int pbs = tk.pair_b[p];
+        const int pbs = tk.pair_b[p], pb = (pbs < 0 ? -pbs : pbs);
         const double* A = tiles + (size_t)tk.pair_a[p] * 4096 + r0 * 64;
-        const double* B = tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096 + c0;
+        const bool tr = (pb & PAIR_TRANS) != 0;
+        const double* X = tiles + (size_t)(pb & ~PAIR_TRANS) * 4096;
         for (int i = tid; i < 1024; i += NT) {
             const int ra = i >> 5, ca = (i & 31) * 2;
             cp_async16(sA + ra * 68 + ca, A + ra * 64 + ca);
-            const int rb = i >> 4, cb = (i & 15) * 2;
-            cp_async16(sB + rb * 40 + cb, B + rb * 64 + cb);
+            if (tr) cp_async16(sB + ra * 68 + ca, X + (c0 + ra) * 64 + ca);
+            else {
+                const int rb = i >> 4, cb = (i & 15) * 2;
+                cp_async16(sB + rb * 40 + cb, X + rb * 64 + c0 + cb);
+            }
         }
         cp_commit();
     };
@@ -131,11 +137,15 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
         const double* sA = sm + s * F64_STAGE;
         const double* sB = sA + 32 * 68;
         const double sgn = tk.pair_b[p] < 0 ? -1.0 : 1.0;
+        // B[k][n] at sB[k * sk + n * sn]: [k][40] layout, or [n][68] for a transposed operand
+        const bool tr = ((tk.pair_b[p] < 0 ? -tk.pair_b[p] : tk.pair_b[p]) & PAIR_TRANS) != 0;
+        const int sk = tr ? 1 : 40, sn = tr ? 68 : 1;
+        const double* bq = sB + (ch * 16 + g) * sn + t * sk;
 #pragma unroll
         for (int k0 = 0; k0 < 64; k0 += 4) {
             const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
 #pragma unroll
-            for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, sB[(k0 + t) * 40 + ch * 16 + nt * 8 + g]);
+            for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, bq[k0 * sk + nt * 8 * sn]);
         }
         __syncthreads();
     }
@@ -144,102 +154,6 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
     for (int nt = 0; nt < 2; nt++) {
         const int row = r0 + rg * 8 + g, col = c0 + ch * 16 + nt * 8 + 2 * t;
         *reinterpret_cast<double2*>(C + row * 64 + col) = make_double2(acc[nt][0], acc[nt][1]);
-    }
-}
-
-// ---------------------------------------------------------------- FP32 GEMM (3xTF32)
-__device__ __forceinline__ uint32_t to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// C = init + sum_p s_p A_p * B_p, full 64x64 per CTA. 8 warps: warp w owns rows
-// (w&3)*16..+16 and columns (w>>2)*32..+32 (four m16n8 tiles).
-__device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = lane >> 2, t = lane & 3, rt = warp & 3, cg = warp >> 2;
-    const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
-    auto issue = [&](int p, int s) {
-        float* sA = sm + s * F32_STAGE;
-        float* sB = sA + 64 * 68;
-        const int pbs = tk.pair_b[p];
-        const float* A = tiles + (size_t)tk.pair_a[p] * 4096;
-        const float* B = tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096;
-        for (int i = tid; i < 1024; i += NT) {
-            const int row = i >> 4, c4 = (i & 15) * 4;
-            cp_async16(sA + row * 68 + c4, A + row * 64 + c4);
-            cp_async16(sB + row * 72 + c4, B + row * 64 + c4);
-        }
-        cp_commit();
-    };
-    float acc[4][4];
-    const int init = tk.a[task];
-#pragma unroll
-    for (int nt = 0; nt < 4; nt++) {
-        if (init > 0) {
-            const float* I = tiles + (size_t)init * 4096 + (rt * 16 + g) * 64 + cg * 32 + nt * 8 + 2 * t;
-            const float2 u = __ldcg(reinterpret_cast<const float2*>(I));
-            const float2 v = __ldcg(reinterpret_cast<const float2*>(I + 8 * 64));
-            acc[nt][0] = u.x; acc[nt][1] = u.y; acc[nt][2] = v.x; acc[nt][3] = v.y;
-        } else {
-            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-        }
-    }
-    if (p0 < p1) issue(p0, 0);
-    for (int p = p0; p < p1; p++) {
-        const int s = (p - p0) & 1;
-        if (p + 1 < p1) {
-            issue(p + 1, s ^ 1);
-            cp_wait<1>();
-        } else {
-            cp_wait<0>();
-        }
-        __syncthreads();
-        const float* sA = sm + s * F32_STAGE;
-        const float* sB = sA + 64 * 68;
-        const float sgn = tk.pair_b[p] < 0 ? -1.f : 1.f;
-#pragma unroll 2
-        for (int k0 = 0; k0 < 64; k0 += 8) {
-            const float af[4] = {sgn * sA[(rt * 16 + g) * 68 + k0 + t], sgn * sA[(rt * 16 + g + 8) * 68 + k0 + t],
-                                 sgn * sA[(rt * 16 + g) * 68 + k0 + t + 4],
-                                 sgn * sA[(rt * 16 + g + 8) * 68 + k0 + t + 4]};
-            uint32_t ahi[4], alo[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                ahi[i] = to_tf32(af[i]);
-                alo[i] = to_tf32(af[i] - __uint_as_float(ahi[i]));
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const int col = cg * 32 + nt * 8 + g;
-                const float b0 = sB[(k0 + t) * 72 + col], b1 = sB[(k0 + t + 4) * 72 + col];
-                uint32_t bhi[2], blo[2];
-                bhi[0] = to_tf32(b0);
-                bhi[1] = to_tf32(b1);
-                blo[0] = to_tf32(b0 - __uint_as_float(bhi[0]));
-                blo[1] = to_tf32(b1 - __uint_as_float(bhi[1]));
-                mma_tf32(acc[nt], alo, bhi);
-                mma_tf32(acc[nt], ahi, blo);
-                mma_tf32(acc[nt], ahi, bhi);
-            }
-        }
-        __syncthreads();
-    }
-    float* C = tiles + (size_t)tk.out[task] * 4096;
-#pragma unroll
-    for (int nt = 0; nt < 4; nt++) {
-        const int col = cg * 32 + nt * 8 + 2 * t;
-        const int row = rt * 16 + g;
-        *reinterpret_cast<float2*>(C + row * 64 + col) = make_float2(acc[nt][0], acc[nt][1]);
-        *reinterpret_cast<float2*>(C + (row + 8) * 64 + col) = make_float2(acc[nt][2], acc[nt][3]);
     }
 }
 
@@ -259,7 +173,11 @@ __device__ void gemm_f32_full(const DevTasks& tk, float* __restrict__ tiles, int
 __device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double fast_rcp(double x) { return __drcp_rn(x); }
 
-template <typename T, bool WITH_LINV>
+// LU task; with CHOL the LL^T task of a symmetric tile (lltdcmpSimple,
+// MatrixStdDouble.cpp:2629-2668): the same elimination on the tile
+// symmetrised from its lower triangle, pivots below 1e-20 raised to it, and
+// L = L_lu diag(sqrt(pivots)), L^-1 = diag(1/sqrt(pivots)) L_lu^-1.
+template <typename T, bool WITH_LINV, bool CHOL = false>
 __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
     T* rowbuf = sm;          // [2][8][64] scaled pivot rows of A for the current block
     T* wbuf = sm + 1024;     // [2][8][64] rows of the running L^-1 for the current block
@@ -273,11 +191,12 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         s_maxu = 0.f;
     }
     const T* A = tiles + (size_t)tk.a[task] * 4096 + r * 64 + q;
+    const T* At = tiles + (size_t)tk.a[task] * 4096 + q * 64 + r;  // column r: A[q + 4m][r]
     T a[16], w[16];
     float ma = 0.f;
 #pragma unroll
     for (int m = 0; m < 16; m++) {
-        a[m] = __ldcg(A + 4 * m);
+        a[m] = (CHOL && q + 4 * m > r) ? __ldcg(At + 4 * m * 64) : __ldcg(A + 4 * m);
         ma = fmaxf(ma, fabsf((float)a[m]));
         if (WITH_LINV) w[m] = (q + 4 * m == r) ? T(1) : T(0);
     }
@@ -296,9 +215,10 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         T* wb = wbuf + (k & 1) * 64;
         const T aik = __shfl_sync(FULL, a[km], (lane & ~3) | kq);  // a[r][k] for this thread's row
         if (r == k) {
-            // clamp |u_kk| < 1e-9 to +-1e-9 (0 -> +1e-9), in the working precision
+            // LU: clamp |u_kk| < 1e-9 to +-1e-9 (0 -> +1e-9); LL^T: p < 1e-20 -> 1e-20
             const T tiny = T(1e-9);
-            const T p = (aik < tiny && aik > -tiny) ? (aik < T(0) ? -tiny : tiny) : aik;
+            const T p = CHOL ? (aik < T(1e-20) ? T(1e-20) : aik)
+                             : ((aik < tiny && aik > -tiny) ? (aik < T(0) ? -tiny : tiny) : aik);
             const T rp = fast_rcp(p);
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -325,20 +245,37 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         }
     }
     T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
-    T* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + q;
     float mu = 0.f;
+    if (CHOL) {
+        const T sr = sqrt(piv[r]);
 #pragma unroll
-    for (int m = 0; m < 16; m++) {
-        const int c = q + 4 * m;
-        L[4 * m] = r > c ? a[m] : (r == c ? T(1) : T(0));
-        const T u = r < c ? a[m] : (r == c ? piv[r] : T(0));
-        U[4 * m] = u;
-        mu = fmaxf(mu, fabsf((float)u));
-    }
-    if (WITH_LINV) {
-        T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+        for (int m = 0; m < 16; m++) {
+            const int c = q + 4 * m;
+            const T v = r > c ? a[m] * sqrt(piv[c]) : (r == c ? sr : T(0));
+            L[4 * m] = v;
+            mu = fmaxf(mu, fabsf((float)v));
+        }
+        if (WITH_LINV) {
+            T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+            const T isr = T(1) / sr;
 #pragma unroll
-        for (int m = 0; m < 16; m++) W[4 * m] = w[m];
+            for (int m = 0; m < 16; m++) W[4 * m] = w[m] * isr;
+        }
+    } else {
+        T* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + q;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int c = q + 4 * m;
+            L[4 * m] = r > c ? a[m] : (r == c ? T(1) : T(0));
+            const T u = r < c ? a[m] : (r == c ? piv[r] : T(0));
+            U[4 * m] = u;
+            mu = fmaxf(mu, fabsf((float)u));
+        }
+        if (WITH_LINV) {
+            T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+#pragma unroll
+            for (int m = 0; m < 16; m++) W[4 * m] = w[m];
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         ma = fmaxf(ma, __shfl_xor_sync(FULL, ma, o));
@@ -356,7 +293,7 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         for (int k = lane; k < 64; k += 32) {
             const double v = fabs((double)raw[k]);
             mn = fmin(mn, v);
-            cl += v < 1e-9;
+            cl += CHOL ? (double)raw[k] < 1e-20 : v < 1e-9;
         }
         for (int o = 16; o > 0; o >>= 1) {
             mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
@@ -434,6 +371,17 @@ __device__ void sub_task(const DevTasks& tk, T* __restrict__ tiles, int task) {
     }
 }
 
+// R = A^T through shared memory (coalesced reads and writes): the upper
+// factor L^T of an LL^T plan for the back substitution
+template <typename T>
+__device__ void trans_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
+    const T* A = tiles + (size_t)tk.a[task] * 4096;
+    T* R = tiles + (size_t)tk.out[task] * 4096;
+    for (int e = threadIdx.x; e < 4096; e += NT) sm[(e & 63) * LD + (e >> 6)] = __ldcg(A + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 4096; e += NT) R[e] = sm[(e >> 6) * LD + (e & 63)];
+}
+
 // C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh). The
 // next pair's operands load from L2 into registers while the current pair's
 // MMAs run; `phase` is this CTA's mbarrier parity, carried across tasks.
@@ -446,8 +394,9 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
     const unsigned long long lim = tk.wait_limit_ns;
     float4 a4[4], b4[4];
     auto operands = [&](int p) {
-        const int pbs = tk.pair_b[p];
-        tc::load_pair(tiles + (size_t)tk.pair_a[p] * 4096, tiles + (size_t)(pbs < 0 ? -pbs : pbs) * 4096, a4, b4);
+        const int pbs = tk.pair_b[p], pb = pbs < 0 ? -pbs : pbs;
+        tc::load_pair(tiles + (size_t)tk.pair_a[p] * 4096, tiles + (size_t)(pb & ~PAIR_TRANS) * 4096,
+                      (pb & PAIR_TRANS) != 0, a4, b4);
     };
     const int n = p1 - p0;
     // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
@@ -557,9 +506,14 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
             if (tk.b[task] > 0) lu_task<T, true>(tk, tiles, task, sm);
             else lu_task<T, false>(tk, tiles, task, sm);
             break;
+        case K_LLT:
+            if (tk.b[task] > 0) lu_task<T, true, true>(tk, tiles, task, sm);
+            else lu_task<T, false, true>(tk, tiles, task, sm);
+            break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;
         case K_UINV: inv_task<T, false>(tk, tiles, task, sm); break;
         case K_SUB: sub_task<T>(tk, tiles, task); break;
+        case K_TRANS: trans_task<T>(tk, tiles, task, sm); break;
         default: break;
     }
 }
@@ -848,16 +802,20 @@ int level_launch(const DevTasks& t, T* tiles, const int32_t* items, int nitems, 
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-__global__ void scatter_kernel(const double* __restrict__ V, const int32_t* __restrict__ tile,
-                               const int16_t* __restrict__ off, int64_t nnz, const int32_t* __restrict__ pad_tile,
-                               const int16_t* __restrict__ pad_off, int64_t npad, double* t64, float* t32) {
+// input tiles from the caller's values; vidx (symmetric input): value index of
+// each mirrored triplet
+__global__ void scatter_kernel(const double* __restrict__ V, const int32_t* __restrict__ vidx,
+                               const int32_t* __restrict__ tile, const int16_t* __restrict__ off, int64_t nnz,
+                               const int32_t* __restrict__ pad_tile, const int16_t* __restrict__ pad_off, int64_t npad,
+                               double* t64, float* t32) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nnz) {
         const int32_t tl = tile[i];
         if (tl >= 0) {
             const int64_t e = (int64_t)tl * 4096 + off[i];
-            if (t64) t64[e] = V[i];
-            else t32[e] = (float)V[i];
+            const double v = V[vidx ? vidx[i] : i];
+            if (t64) t64[e] = v;
+            else t32[e] = (float)v;
         }
     } else if (i - nnz < npad) {
         const int64_t k = i - nnz;
@@ -927,13 +885,13 @@ int factor_persistent_grid(bool fp64, int stages, int num_sms) {
     return per_sm * num_sms;
 }
 
-void scatter_values_launch(const double* V, const int32_t* tile, const int16_t* off, int64_t nnz,
+void scatter_values_launch(const double* V, const int32_t* vidx, const int32_t* tile, const int16_t* off, int64_t nnz,
                            const int32_t* pad_tile, const int16_t* pad_off, int64_t npad, double* tiles64,
                            float* tiles32, cudaStream_t s) {
     const int64_t n = nnz + npad;
     if (n == 0) return;
-    scatter_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(V, tile, off, nnz, pad_tile, pad_off, npad, tiles64,
-                                                               tiles32);
+    scatter_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(V, vidx, tile, off, nnz, pad_tile, pad_off, npad,
+                                                               tiles64, tiles32);
 }
 void convert_tiles_launch(const double* src, float* dst, int64_t n, cudaStream_t s) {
     if (n > 0) convert_kernel<<<1216, 256, 0, s>>>(src, dst, n);

@@ -62,10 +62,9 @@ int factor_level_launch(const DevTasks& t, float* tiles, const int32_t* items, i
                         cudaStream_t s);
 // persistent grid size (CTAs co-resident on the device)
 int factor_persistent_grid(bool fp64, int stages, int num_sms);
-size_t factor_smem_bytes(bool fp64);
 
-// value scatter into input tiles: tiles[tile[k]*4096 + off[k]] = V[k] (tile < 0: skip)
-void scatter_values_launch(const double* V, const int32_t* tile, const int16_t* off, int64_t nnz,
+// value scatter into input tiles: tiles[tile[k]*4096 + off[k]] = V[vidx ? vidx[k] : k] (tile < 0: skip)
+void scatter_values_launch(const double* V, const int32_t* vidx, const int32_t* tile, const int16_t* off, int64_t nnz,
                            const int32_t* pad_tile, const int16_t* pad_off, int64_t npad, double* tiles64,
                            float* tiles32, cudaStream_t s);
 // FP64 input tiles -> FP32 input tiles (first n elements)
@@ -119,8 +118,9 @@ struct DevCSR {
 constexpr int RED = 6;
 void residual_launch(const DevCSR& A, const double* b, const double* x, double* r, int nrhs, double* red,
                      int n_stat, cudaStream_t s);
-// csr_val[pos[k]] = V[k] for pos[k] >= 0
-void scatter_csr_launch(const double* V, const int32_t* pos, int64_t nnz, double* csr_val, cudaStream_t s);
+// csr_val[pos[k]] = V[vidx ? vidx[k] : k] for pos[k] >= 0
+void scatter_csr_launch(const double* V, const int32_t* vidx, const int32_t* pos, int64_t nnz, double* csr_val,
+                        cudaStream_t s);
 void cast_f64_to_f32_launch(const double* src, float* dst, int64_t n, cudaStream_t s);
 void axpy_f32_to_f64_launch(const float* d, double* x, int64_t n, int assign, cudaStream_t s);
 // The systems of a solve. Permuted row i belongs to system of_brow[i >> 6]

@@ -27,6 +27,8 @@ enum OpKind : int32_t {
 //   upperInv:  res = inverse of upper-triangular block src
 //   sub:       res = src2 - src; src == 0: res = src2 (copy); src2 == 0: res = -src (neg)
 //   mul:       res += src * src2;   mulneg: res -= src * src2   (res starts at zero)
+//   llt:       res = L with L L^T = src (lower triangle of src read)
+//   mult:      res += src * src2^T  (res starts at zero)
 struct Op {
     int32_t op, src, src2, res, res2, stage;
     int32_t seq, group;
@@ -74,13 +76,19 @@ struct Plan {
     int32_t storage_count = 0;   // block ids are 1..storage_count-1
     int32_t n_input = 0;         // input tiles carry ids 1..n_input
     std::vector<int32_t> input_bi, input_bj;  // block coordinates of input tiles (index id-1)
-    std::vector<Leaf> L, U;      // leaves of the L and U block quadtrees
+    std::vector<Leaf> L, U;      // leaves of the L and U block quadtrees (U empty for LL^T)
+    bool symmetric = false;      // LL^T plan: ops llt / mult, A = L L^T
     int32_t stages = 0;
     // Value scatter for (re)factorisation with the same pattern: triplet k goes
     // to input tile scatter_tile[k] (0-based, -1 = superseded duplicate) at
     // element scatter_off[k] (row*64+col). Padded rows carry a unit diagonal.
     std::vector<int32_t> scatter_tile;
     std::vector<int16_t> scatter_off;
+    // Symmetric input: the scatter runs over the mirrored triplets; value
+    // source of each (index into the caller's triplets), else empty. Callers
+    // always pass values in their own triplet order (nval of them).
+    std::vector<int32_t> mirror_src;
+    int64_t nval = 0;
     std::vector<int32_t> pad_tile;  // tile index of each padded row's diagonal
     std::vector<int16_t> pad_off;
     // Batch plans only: the merged systems in order. Then ord.new_to_old has
@@ -105,9 +113,9 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I, const int3
 // cannot be merged (imported plans, batch plans, size overflow).
 Plan merge_plans(const std::vector<const Plan*>& ps);
 
-// Dense input tiles (n_input x 64 x 64, row-major) for values V of the same
-// triplets build_plan saw (after mirroring when symmetric).
-void scatter_tiles(const Plan& p, const double* Vmirrored, double* tiles);
+// Dense input tiles (n_input x 64 x 64, row-major) for values V of the
+// triplets given to build_plan (mirrored here when symmetric).
+void scatter_tiles(const Plan& p, const double* V, double* tiles);
 
 // Triplets after mirroring (what build_plan and scatter_tiles index).
 void mirror_triplets(int n, int64_t nnz, bool symmetric, const int32_t* I, const int32_t* J, const double* V,

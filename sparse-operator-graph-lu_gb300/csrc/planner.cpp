@@ -76,6 +76,27 @@ struct Emitter {
                     }
                 }
     }
+    // c += a * b^T (BlockPlanner.cpp:1203-1229): quadrant (i, j) of c takes
+    // a(i, k) * b(j, k)^T
+    void mult(int32_t a, int32_t b, int32_t c, int32_t group) {
+        if (a == 0 || b == 0) return;
+        if (at(a).level == 0) {
+            if (at(a).id > 0 && at(b).id > 0) {
+                if (at(c).id <= 0) at(c).id = fresh_id();
+                emit(OP_MULT, at(a).id, at(b).id, at(c).id, 0, group);
+            }
+            return;
+        }
+        for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++)
+                for (int k = 0; k < 2; k++) {
+                    int32_t ak = at(a).ch[i * 2 + k], bk = at(b).ch[j * 2 + k];
+                    if (ak != 0 && bk != 0) {
+                        int32_t ck = child_or_new(c, i * 2 + j);
+                        mult(ak, bk, ck, group);
+                    }
+                }
+    }
     // c = a - b, with copy / negate where one side is absent (BlockPlanner.cpp:1126-1201)
     void sub(int32_t a, int32_t b, int32_t c, int32_t group) {
         if (at(a).level == 0) {
@@ -233,6 +254,42 @@ struct Emitter {
         at(u).ch[3] = nu1;
     }
 
+    // l = LL^T factor of symmetric a; l3, when given, receives the inverse of
+    // l's leading quadrant (BlockPlanner.cpp:941-989):
+    //   L11 = LLT(A11); Li = L11^-1; L21 = A21 Li^T; S = A22 - L21 L21^T; L22 = LLT(S)
+    void llt(int32_t a, int32_t l, int32_t l3, int32_t group) {
+        if (at(a).level == 0) {
+            if (at(a).id > 0) {
+                if (at(l).id <= 0) at(l).id = fresh_id();
+                emit(OP_LLT, at(a).id, 0, at(l).id, 0, group);
+            }
+            return;
+        }
+        const int lev = at(a).level;
+        int32_t ha = at(a).ch[0];
+        int32_t l1 = node(lev - 1);
+        int32_t l2 = l3 != 0 ? l3 : node(lev - 1);
+        int32_t hl1 = lev > 1 ? node(lev - 2) : 0;
+        llt(ha, l1, hl1, group);
+        inv_lower(l1, l2, hl1, group);
+        at(l).ch[0] = l1;
+        int32_t dsub = node(lev - 1);
+        int32_t d = at(a).ch[3], c = at(a).ch[2];
+        if (c != 0) {
+            int32_t ca1 = node(lev - 1), ca2 = node(lev - 1);
+            mult(c, l2, ca1, group);
+            at(l).ch[2] = ca1;
+            mult(ca1, ca1, ca2, group);
+            sub(d, ca2, dsub, group);
+        } else {
+            dsub = d;
+        }
+        int32_t nl1 = node(lev - 1);
+        int32_t dl1 = lev > 1 ? node(lev - 2) : 0;
+        llt(dsub, nl1, dl1, group);
+        at(l).ch[3] = nl1;
+    }
+
     // quadtree of input blocks over a grid of `rows` x `rows` blocks
     int32_t root_for(int rows) { return node(__builtin_popcount((unsigned)(rows - 1))); }
     // get-or-create the leaf at (bi, bj) (matrix.cpp:65-88); returns the leaf node
@@ -374,13 +431,20 @@ void mirror_triplets(int n, int64_t nnz, bool symmetric, const int32_t* I, const
 
 Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int32_t* J0, const double* V0,
                 int threads) {
-    if (symmetric) throw std::runtime_error("symmetric (LL^T) input is not supported by this executor");
     if (n <= 0) throw std::runtime_error("dimension must be positive");
     Plan p;
     double t0 = now_s();
     std::vector<int32_t> I, J;
     std::vector<double> V;
     mirror_triplets(n, nnz, symmetric, I0, J0, V0, I, J, V);
+    p.nval = nnz;
+    if (symmetric) {
+        p.mirror_src.reserve(I.size());
+        for (int64_t k = 0; k < nnz; k++) {
+            p.mirror_src.push_back((int32_t)k);
+            if (I0[k] != J0[k]) p.mirror_src.push_back((int32_t)k);
+        }
+    }
     p.cfg = make_config(n);
     p.ord = gps_order(n, I, J, V, threads);
     for (size_t k = 0; k < I.size(); k++) { I[k] = p.ord.old_to_new[I[k]]; J[k] = p.ord.old_to_new[J[k]]; }
@@ -403,12 +467,15 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
     };
     for (size_t k = 0; k < I.size(); k++) ctouch(I[k] >> sh2, J[k] >> sh2);
     for (int i = n; i < n_ext; i++) ctouch(i / bs2, i / bs2);
+    // symmetric input: the LL^T recursion (solver.cpp:70-71), L only
+    p.symmetric = symmetric;
     int32_t cl = cz.root_for(R2), cu = cz.root_for(R2);
-    cz.lu(croot, cl, cu, 0, 0, 0);
+    if (symmetric) cz.llt(croot, cl, 0, 0);
+    else cz.lu(croot, cl, cu, 0, 0, 0);
     p.coarse_ops_emitted = (int64_t)cz.ops.size();
     std::vector<Leaf> cL, cU;
     cz.collect(cl, 0, 0, cL);
-    cz.collect(cu, 0, 0, cU);
+    if (!symmetric) cz.collect(cu, 0, 0, cU);
     {
         std::vector<int32_t> outs;
         for (auto& lf : cL) outs.push_back(lf.id);
@@ -495,6 +562,8 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
             case OP_LOWERINV: fz.inv_lower(zoom[o.src], zoom[o.res], 0, g); break;
             case OP_UPPERINV: fz.inv_upper(zoom[o.src], zoom[o.res], 0, g); break;
             case OP_LU: fz.lu(zoom[o.src], zoom[o.res], zoom[o.res2], 0, 0, g); break;
+            case OP_LLT: fz.llt(zoom[o.src], zoom[o.res], 0, g); break;
+            case OP_MULT: fz.mult(zoom[o.src], zoom[o.src2], zoom[o.res], g); break;
             case OP_MUL: fz.mul(zoom[o.src], zoom[o.src2], zoom[o.res], g, OP_MUL); break;
             case OP_MULNEG: fz.mul(zoom[o.src], zoom[o.src2], zoom[o.res], g, OP_MULNEG); break;
             case OP_SUB:
@@ -537,8 +606,10 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
 
 void scatter_tiles(const Plan& p, const double* V, double* tiles) {
     std::memset(tiles, 0, sizeof(double) * 4096 * (size_t)p.n_input);
+    const bool mir = !p.mirror_src.empty();
     for (size_t k = 0; k < p.scatter_tile.size(); k++)
-        if (p.scatter_tile[k] >= 0) tiles[(size_t)p.scatter_tile[k] * 4096 + p.scatter_off[k]] = V[k];
+        if (p.scatter_tile[k] >= 0)
+            tiles[(size_t)p.scatter_tile[k] * 4096 + p.scatter_off[k]] = V[mir ? p.mirror_src[k] : (int64_t)k];
     for (size_t k = 0; k < p.pad_tile.size(); k++) tiles[(size_t)p.pad_tile[k] * 4096 + p.pad_off[k]] = 1.0;
 }
 

@@ -135,10 +135,11 @@ struct sog_ctx {
 struct sog_system {
     sog_ctx* ctx = nullptr;
     sog_options opt{};
-    bool fp64 = true, imported = false;
+    bool fp64 = true, imported = false, symmetric = false;
     int n = 0, n_ext = 0, R = 0, n_input = 0;
     int32_t storage = 0;
     int64_t ntrip = 0, npad = 0;
+    int64_t nval = 0;  // values the caller passes (its own triplets; mirrored inside when symmetric)
     TaskGraph tg;
     // pool allocations
     void* tiles = nullptr;
@@ -164,6 +165,7 @@ struct sog_system {
     std::vector<Segment> segs;
     int32_t *d_seg_brow = nullptr, *d_seg_n = nullptr, *d_n2o = nullptr;
     double* d_V = nullptr;
+    int32_t* d_vidx = nullptr;  // symmetric: value index of each mirrored triplet (NULL = identity)
     // vectors (for up to vec_nrhs right-hand sides)
     double *d_bext = nullptr, *d_xext = nullptr, *d_r = nullptr, *d_red = nullptr;
     float* d_v32 = nullptr;
@@ -695,8 +697,10 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     if (!plan || !bytes) return fail(SOG_EINVAL, "NULL argument");
     sog_options o = opt ? *opt : default_options();
     const Plan& p = plan->p;
-    // + diagonal inverses and look-ahead products added for the substitution
-    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows) * 4096 * elem_bytes(o);
+    // + diagonal inverses and look-ahead products added for the substitution,
+    // + the transposed L leaves of an LL^T plan
+    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows + (p.symmetric ? p.L.size() : 0)) * 4096 *
+                     elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
     *bytes = tiles + aux;
@@ -726,23 +730,28 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->n_input = p.n_input;
     s->storage = p.storage_count;
     s->ntrip = (int64_t)p.scatter_tile.size();
+    s->nval = p.mirror_src.empty() ? s->ntrip : p.nval;
     s->npad = (int64_t)p.pad_tile.size();
     s->L = p.L;
     s->U = p.U;
+    s->symmetric = p.symmetric;
     int gemm_parts = o.gemm_split == 1 ? 1 : (o.gemm_split == 4 ? 4 : (s->fp64 ? 4 : 1));
     if (!s->fp64) gemm_parts = 1;
     // inverses of the diagonal factor blocks for the substitution (reused
     // where the DAG already computes them)
     std::vector<Op> ops2 = p.ops;
     int32_t storage2 = p.storage_count;
+    // LL^T: the upper factor of the substitution is L^T (upperSolverT,
+    // BlockPlanner.cpp:752-797), materialised as transposed L leaves
+    if (p.symmetric) add_transposed_leaves(ops2, storage2, s->L, s->U);
     std::vector<int32_t> ldinv, udinv;
-    add_diag_inverses(ops2, storage2, s->R, p.L, p.U, ldinv, udinv);
+    add_diag_inverses(ops2, storage2, s->R, s->L, s->U, ldinv, udinv);
     std::vector<int32_t> lla, ula;
-    if (o.solve_lookahead >= 0) add_lookahead_products(ops2, storage2, s->R, p.L, p.U, ldinv, udinv, lla, ula);
+    if (o.solve_lookahead >= 0) add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla, ula);
     s->storage = storage2;
     std::vector<int32_t> outputs;
-    for (const Leaf& lf : p.L) outputs.push_back(lf.id);
-    for (const Leaf& lf : p.U) outputs.push_back(lf.id);
+    for (const Leaf& lf : s->L) outputs.push_back(lf.id);
+    for (const Leaf& lf : s->U) outputs.push_back(lf.id);
     for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : lla) if (id > 0) outputs.push_back(id);
@@ -851,7 +860,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()),
              o_order = L.add<int32_t>(order.size()),
-             o_V = L.add<double>(s->ntrip);
+             o_V = L.add<double>(s->nval), o_vidx = L.add<int32_t>(p.mirror_src.size());
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
     if (!s->tiles) {
@@ -943,6 +952,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         return fail(SOG_ENOMEM, "pinned host buffers");
     }
     s->d_V = reinterpret_cast<double*>(A + o_V);
+    if (!p.mirror_src.empty()) s->d_vidx = put(A, o_vidx, p.mirror_src, st);
     s->stages = o.pipeline_stages == 1 ? 1 : 2;
     if (o.executor == SOG_EXEC_AUTO) {
         Tuned known;
@@ -992,21 +1002,21 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
     CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
     // input tile k (0-based, as the scatter map counts) is block id k+1
     s->launches++;
-    scatter_values_launch(V_dev, s->d_sc_tile, s->d_sc_off, s->ntrip, s->d_pad_tile, s->d_pad_off, s->npad,
+    scatter_values_launch(V_dev, s->d_vidx, s->d_sc_tile, s->d_sc_off, s->ntrip, s->d_pad_tile, s->d_pad_off, s->npad,
                           s->fp64 ? (double*)s->tiles + 4096 : nullptr, s->fp64 ? nullptr : (float*)s->tiles + 4096,
                           st);
     s->launches++;
-    scatter_csr_launch(V_dev, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
+    scatter_csr_launch(V_dev, s->d_vidx, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
     return run_factor(s);
 }
 
 int sog_factor(sog_system* s, const double* V) {
     if (!s) return fail(SOG_EINVAL, "NULL system");
     if (s->imported) return fail(SOG_ESTATE, "imported plan: use sog_factor_tiles");
-    if (!V && s->ntrip) return fail(SOG_EINVAL, "NULL values");
+    if (!V && s->nval) return fail(SOG_EINVAL, "NULL values");
     CK(cudaSetDevice(s->ctx->device));
-    if (s->ntrip)
-        CK(cudaMemcpyAsync(s->d_V, V, sizeof(double) * s->ntrip, cudaMemcpyHostToDevice, s->ctx->stream));
+    if (s->nval)
+        CK(cudaMemcpyAsync(s->d_V, V, sizeof(double) * s->nval, cudaMemcpyHostToDevice, s->ctx->stream));
     return sog_factor_device(s, s->d_V);
 }
 
@@ -1104,7 +1114,7 @@ int sog_system_export_factors(sog_system* s, double* ltiles, double* utiles) {
     for (int side = 0; side < 2; side++) {
         const std::vector<Leaf>& lv = side == 0 ? s->L : s->U;
         double* dst = side == 0 ? ltiles : utiles;
-        if (!dst) continue;
+        if (!dst || (side == 1 && s->symmetric)) continue;  // LL^T: the plan has no U leaves
         for (size_t k = 0; k < lv.size(); k++) {
             const char* src = (const char*)s->tiles + (uint64_t)lv[k].id * 4096 * eb;
             if (s->fp64) {
@@ -1209,6 +1219,7 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
         counts[2] = g.total_items;
         counts[3] = g.gemm_pairs;
         for (int k = 0; k < 5; k++) counts[4 + k] = g.count[k];
+        counts[5] += g.count[K_LLT];
         counts[9] = g.fused_subs;
         counts[10] = storage2 - p.storage_count;
         counts[11] = g.ntasks ? *std::max_element(g.prio.begin(), g.prio.end()) + 1 : 0;
@@ -1229,6 +1240,8 @@ int sog_system_task_info(const sog_system* s, int64_t* counts) {
     counts[2] = g.total_items;
     counts[3] = g.gemm_pairs;
     for (int k = 0; k < 5; k++) counts[4 + k] = g.count[k];
+    counts[5] += g.count[K_LLT];
+    counts[8] += g.count[K_TRANS];
     counts[9] = s->grid_factor;
     counts[10] = s->launches;
     return SOG_OK;
@@ -1248,10 +1261,7 @@ int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_
     sog_system* s = nullptr;
     r = sog_system_create(c, plan, &o, &s);
     if (!r) {
-        std::vector<int32_t> Io, Jo;
-        std::vector<double> Vo;
-        mirror_triplets(dim, valcount, symmetric != 0, index_i, index_j, vals, Io, Jo, Vo);
-        r = sog_factor(s, Vo.data());
+        r = sog_factor(s, vals);
         if (!r) r = sog_solve(s, 1, b, x_out, nullptr);
         sog_system_destroy(s);
     }

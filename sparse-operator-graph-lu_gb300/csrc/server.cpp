@@ -181,7 +181,9 @@ int sog_server::run_batch(std::vector<Request*>& group) {
             group.resize(keep);
             return 1;
         }
-        if (any_resident()) {
+        // memory still held by resident requests, or by released batches the
+        // scheduler has not freed yet: wait for it instead of failing
+        if (any_resident() || !dead.empty()) {
             group[0]->state = R_PLANNED;
             planned.push_front(group[0]);
             group.clear();
@@ -302,7 +304,7 @@ void sog_server::scheduler_loop() {
             }
             if (group.empty()) {
                 Request* r = planned.front();
-                if (!any_resident()) {
+                if (!any_resident() && dead.empty()) {
                     // larger than the whole pool: refuse it rather than wait forever
                     planned.pop_front();
                     r->state = R_FAILED;

@@ -309,10 +309,10 @@ __global__ void residual_kernel(DevCSR A, const double* __restrict__ b, const do
         }
     }
 }
-__global__ void scatter_csr_kernel(const double* __restrict__ V, const int32_t* __restrict__ pos, int64_t nnz,
-                                   double* __restrict__ val) {
+__global__ void scatter_csr_kernel(const double* __restrict__ V, const int32_t* __restrict__ vidx,
+                                   const int32_t* __restrict__ pos, int64_t nnz, double* __restrict__ val) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nnz && pos[k] >= 0) val[pos[k]] = V[k];
+    if (k < nnz && pos[k] >= 0) val[pos[k]] = V[vidx ? vidx[k] : k];
 }
 
 __global__ void cast_kernel(const double* __restrict__ s, float* __restrict__ d, int64_t n) {
@@ -431,8 +431,9 @@ void residual_launch(const DevCSR& A, const double* b, const double* x, double* 
     cudaMemsetAsync(red, 0, sizeof(double) * RED * nrhs, s);
     residual_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A, b, x, r, nrhs, red, n_stat);
 }
-void scatter_csr_launch(const double* V, const int32_t* pos, int64_t nnz, double* csr_val, cudaStream_t s) {
-    if (nnz > 0) scatter_csr_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(V, pos, nnz, csr_val);
+void scatter_csr_launch(const double* V, const int32_t* vidx, const int32_t* pos, int64_t nnz, double* csr_val,
+                        cudaStream_t s) {
+    if (nnz > 0) scatter_csr_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(V, vidx, pos, nnz, csr_val);
 }
 void cast_f64_to_f32_launch(const double* src, float* dst, int64_t n, cudaStream_t s) {
     if (n > 0) cast_kernel<<<608, 256, 0, s>>>(src, dst, n);

@@ -75,10 +75,7 @@ int main(int argc, char** argv) {
     opt.tol = 1e-10;
     sog_system* sys = nullptr;
     if ((r = sog_system_create(ctx, plan, &opt, &sys))) { std::printf("system: %s\n", sog_last_error()); return 4; }
-    std::vector<int32_t> Io, Jo;
-    std::vector<double> Vo;
-    sog::mirror_triplets(m.n, (int64_t)m.I.size(), m.symmetric, m.I.data(), m.J.data(), m.V.data(), Io, Jo, Vo);
-    if ((r = sog_factor(sys, Vo.data()))) { std::printf("factor: %s\n", sog_last_error()); return 5; }
+    if ((r = sog_factor(sys, m.V.data()))) { std::printf("factor: %s\n", sog_last_error()); return 5; }
     std::vector<double> x(m.n);
     sog_solve_stats st;
     r = sog_solve(sys, 1, b.data(), x.data(), &st);

@@ -97,11 +97,13 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         if (o.src2 > 0) readers[o.src2]++;
         uint8_t k;
         switch (o.op) {
-            case OP_MUL: case OP_MULNEG: k = K_GEMM; break;
+            case OP_MUL: case OP_MULNEG: case OP_MULT: k = K_GEMM; break;
             case OP_LU: k = K_LU; break;
+            case OP_LLT: k = K_LLT; break;
             case OP_LOWERINV: k = K_LINV; break;
             case OP_UPPERINV: k = K_UINV; break;
             case OP_SUB: k = K_SUB; break;
+            case OP_TRANSPOSE: k = K_TRANS; break;
             default: throw std::runtime_error("unsupported op kind " + std::to_string(o.op));
         }
         int32_t t = producer[o.res];
@@ -125,7 +127,8 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         if (k == K_GEMM) {
             if (o.src <= 0 || o.src2 <= 0) throw std::runtime_error("mul with absent operand");
             tl[t].pa.push_back(o.src);
-            tl[t].pb.push_back(o.op == OP_MULNEG ? -o.src2 : o.src2);
+            const int32_t b = o.op == OP_MULT ? (o.src2 | PAIR_TRANS) : o.src2;
+            tl[t].pb.push_back(o.op == OP_MULNEG ? -b : b);
         }
     }
     // fuse  S = D - X  with  X = GEMM (X read only by S, not an output)
@@ -159,7 +162,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         T0& X = tl[s];
         if (X.dead || X.kind != K_LINV || X.a <= 0) continue;
         const int32_t t = producer[X.a];
-        if (t < 0 || tl[t].kind != K_LU || tl[t].out != X.a || tl[t].b != 0) continue;
+        if (t < 0 || (tl[t].kind != K_LU && tl[t].kind != K_LLT) || tl[t].out != X.a || tl[t].b != 0) continue;
         tl[t].b = X.out;
         producer[X.out] = t;
         X.dead = true;
@@ -207,7 +210,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         if (g.kind[t] == K_SUB) dep_on(t, g.b[t]);
         for (int32_t p = g.pair_ptr[t]; p < g.pair_ptr[t + 1]; p++) {
             dep_on(t, g.pair_a[p]);
-            dep_on(t, g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]);
+            dep_on(t, (g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]) & ~PAIR_TRANS);
         }
     }
     g.ndep.assign(g.ntasks, 0);
@@ -295,13 +298,27 @@ void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_r
     }
 }
 
+void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const std::vector<Leaf>& L,
+                           std::vector<Leaf>& U) {
+    U.clear();
+    int32_t seq = ops.empty() ? 0 : ops.back().seq;
+    const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    for (const Leaf& lf : L) {
+        const int32_t id = storage_count++;
+        ops.push_back({OP_TRANSPOSE, lf.id, 0, id, 0, stage, ++seq, 0});
+        U.push_back({lf.bj, lf.bi, id});
+    }
+    std::sort(U.begin(), U.end(), [](const Leaf& a, const Leaf& b) { return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj; });
+}
+
 std::vector<int32_t> static_order(const TaskGraph& g, bool fp64) {
     // single-CTA task latencies on GB300 (us), enough to rank start times
     auto cost = [&](int32_t t) -> double {
         const int np = g.pair_ptr[t + 1] - g.pair_ptr[t];
         switch (g.kind[t]) {
             case K_GEMM: return fp64 ? 5.0 + 20.0 * np / g.parts[t] : 1.5 + 2.0 * np;
-            case K_LU: return fp64 ? 140.0 : 24.0;
+            case K_LU:
+            case K_LLT: return fp64 ? 140.0 : 24.0;
             case K_LINV:
             case K_UINV: return fp64 ? 95.0 : 14.0;
             default: return fp64 ? 6.0 : 3.0;

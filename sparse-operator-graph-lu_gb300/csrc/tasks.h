@@ -22,7 +22,14 @@
 
 namespace sog {
 
-enum TaskKind : uint8_t { K_GEMM = 0, K_LU = 1, K_LINV = 2, K_UINV = 3, K_SUB = 4 };
+enum TaskKind : uint8_t { K_GEMM = 0, K_LU = 1, K_LINV = 2, K_UINV = 3, K_SUB = 4, K_LLT = 5, K_TRANS = 6 };
+constexpr int NUM_KINDS = 7;
+// GEMM operand pairs: pair_b = +-(id | PAIR_TRANS): a negative entry subtracts
+// the product, PAIR_TRANS multiplies by the transpose of block id (mult ops)
+constexpr int32_t PAIR_TRANS = 1 << 30;
+// Internal op kind (not in the reference's enum): res = src^T; used to give an
+// LL^T plan the upper factor L^T for the back substitution
+constexpr int32_t OP_TRANSPOSE = 100;
 
 struct TaskGraph {
     int32_t ntasks = 0;
@@ -45,7 +52,7 @@ struct TaskGraph {
     int64_t fused_inverses = 0;  // lowerInv tasks folded into their LU task
     int64_t aliased_copies = 0;  // copy ops (sub with src = 0) replaced by aliasing
     int64_t aliased_inverses = 0;  // repeated lowerInv / upperInv of one block replaced by aliasing
-    int64_t count[5] = {0, 0, 0, 0, 0};
+    int64_t count[NUM_KINDS] = {0, 0, 0, 0, 0, 0, 0};
     // block -> block whose tile holds its value: identity except the result of
     // a copy, which reads its source's tile (every block is written once, so
     // a copy's source never changes after the copy would have run)
@@ -65,6 +72,11 @@ TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t
 // diagonal L and U blocks. storage_count grows by the number of new blocks.
 void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv);
+// LL^T plans have no U leaves: U = L^T is materialised by one transpose op
+// per L leaf (new blocks), so the back substitution runs as for LU.
+void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const std::vector<Leaf>& L,
+                           std::vector<Leaf>& U);
+
 // Claim order of the ordered executor: items by estimated start time (longest
 // weighted path from a source, single-CTA task latencies as weights), ties by
 // longest remaining path. Every task comes after its predecessors.

@@ -153,14 +153,18 @@ __device__ __forceinline__ void chunk_of(int j, int& row, int& k) {
 // Load this thread's share of one pair from global (L2; produced by other
 // SMs): 4 chunks of A (4 consecutive k of one row) and of B^T (4 consecutive
 // k of one column of B).
-__device__ __forceinline__ void load_pair(const float* A, const float* B, float4 (&a4)[4], float4 (&b4)[4]) {
+// B is the tile itself, or with trans the transpose of the tile at B (so the
+// K-major rows of the MMA's B operand are the tile's rows: one 16-byte load)
+__device__ __forceinline__ void load_pair(const float* A, const float* B, bool trans, float4 (&a4)[4],
+                                          float4 (&b4)[4]) {
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         int row, k;
         chunk_of(j, row, k);
         a4[j] = __ldcg(reinterpret_cast<const float4*>(A + row * 64 + k));
-        b4[j] = make_float4(__ldcg(B + (k + 0) * 64 + row), __ldcg(B + (k + 1) * 64 + row),
-                            __ldcg(B + (k + 2) * 64 + row), __ldcg(B + (k + 3) * 64 + row));
+        b4[j] = trans ? __ldcg(reinterpret_cast<const float4*>(B + row * 64 + k))
+                      : make_float4(__ldcg(B + (k + 0) * 64 + row), __ldcg(B + (k + 1) * 64 + row),
+                                    __ldcg(B + (k + 2) * 64 + row), __ldcg(B + (k + 3) * 64 + row));
     }
 }
 

@@ -22,6 +22,7 @@ class System:
     b: np.ndarray  # float64, (n,) or (n, nrhs) column-major stacked as (nrhs, n)
     x_true: np.ndarray | None = None
     name: str = ""
+    symmetric: bool = False  # triplets hold the lower triangle of a symmetric A
 
     @property
     def nnz(self) -> int:
@@ -33,14 +34,32 @@ class System:
         if x.ndim == 1:
             y = np.zeros(self.n)
             np.add.at(y, self.rows, self.vals * x[self.cols])
+            if self.symmetric:
+                off = self.rows != self.cols
+                np.add.at(y, self.cols[off], self.vals[off] * x[self.rows[off]])
             return y
+        if self.symmetric:
+            return np.stack([self.matvec(xi) for xi in x])
         import scipy.sparse as sp
         a = sp.csr_matrix((self.vals, (self.rows, self.cols)), shape=(self.n, self.n))
         return np.ascontiguousarray((a @ x.T).T)
 
     def to_scipy(self):
         import scipy.sparse as sp
-        return sp.csr_matrix((self.vals, (self.rows, self.cols)), shape=(self.n, self.n))
+        a = sp.csr_matrix((self.vals, (self.rows, self.cols)), shape=(self.n, self.n))
+        if self.symmetric:
+            a = a + sp.tril(a, -1).T.tocsr()
+        return a
+
+
+def spd_lower(s: "System") -> "System":
+    """The same symmetric system given as its lower triangle (MatrixMarket
+    `symmetric` storage: the reader mirrors it, solveLU factors it as L L^T)."""
+    keep = s.rows >= s.cols
+    out = System(n=s.n, rows=np.ascontiguousarray(s.rows[keep]), cols=np.ascontiguousarray(s.cols[keep]),
+                 vals=np.ascontiguousarray(s.vals[keep]), b=s.b, x_true=s.x_true, name="spd_" + s.name,
+                 symmetric=True)
+    return out
 
 
 def _finish(n, r, c, v, x_true, name, nrhs_b=None):
@@ -199,9 +218,10 @@ def serving_requests(count: int, seed: int = 3, n_lo: int = 2000, n_hi: int = 20
 
 # ---------------------------------------------------------------- MatrixMarket
 def write_mtx(path: str, s: System) -> None:
-    """Write A as `%%MatrixMarket matrix coordinate real general`, 1-based."""
+    """Write A as `%%MatrixMarket matrix coordinate real general` (or
+    `symmetric`, lower triangle, for a symmetric system), 1-based."""
     with open(path, "w") as f:
-        f.write("%%MatrixMarket matrix coordinate real general\n")
+        f.write("%%MatrixMarket matrix coordinate real " + ("symmetric" if s.symmetric else "general") + "\n")
         f.write(f"{s.n} {s.n} {s.nnz}\n")
         lines = [f"{r + 1} {c + 1} {v:.17g}\n" for r, c, v in zip(s.rows.tolist(), s.cols.tolist(), s.vals.tolist())]
         f.writelines(lines)

@@ -79,6 +79,9 @@ def golden_cases(wl):
         "band_3000": lambda: wl.random_band(3000, seed=5),
         "band_130": lambda: wl.random_band(130, seed=7),
         "zdiag_600": zdiag,
+        "spd_lap2d_32": lambda: wl.spd_lower(wl.lap2d(32)),
+        "spd_var3d_16": lambda: wl.spd_lower(wl.varcoef3d(16)),
+        "spd_lap2d_8": lambda: wl.spd_lower(wl.lap2d(8)),
     }
 
 

@@ -73,6 +73,10 @@ def cases(wl):
         "lap2d_8": (lambda: wl.lap2d(8), True),
         "zdiag_600": (lambda: zero_diag_case(wl), False),
         "var3d_48": (lambda: wl.varcoef3d(48), False),
+        # symmetric input: lower triangle given, the reference factors L L^T
+        "spd_lap2d_32": (lambda: wl.spd_lower(wl.lap2d(32)), True),
+        "spd_var3d_16": (lambda: wl.spd_lower(wl.varcoef3d(16)), False),
+        "spd_lap2d_8": (lambda: wl.spd_lower(wl.lap2d(8)), True),
     }
     return c
 

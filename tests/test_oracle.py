@@ -8,13 +8,16 @@ from conftest import golden, golden_cases, rhs_of
 
 
 @pytest.mark.parametrize("name", ["lap2d_8", "lap2d_32", "lap2d_128", "var3d_16", "cd_40", "cd_17", "band_3000",
-                                  "band_130"])
+                                  "band_130", "spd_lap2d_8", "spd_lap2d_32", "spd_var3d_16"])
 def test_oracle_solution_matches_reference(sg, wl, oracle, name):
+    """spd_* cases take the reference's LL^T path (llt / mult ops; the back
+    substitution with L^T)."""
     s = golden_cases(wl)[name]()
     g = golden(name)
     # run the oracle on the REFERENCE's own DAG and ordering
-    n_input = sg.Plan(s.n, s.rows, s.cols, s.vals).info.n_input
-    tiles_in = sg.Plan(s.n, s.rows, s.cols, s.vals).input_tiles(s.vals)
+    plan = sg.Plan(s.n, s.rows, s.cols, s.vals, symmetric=s.symmetric)
+    n_input = plan.info.n_input
+    tiles_in = plan.input_tiles(s.vals)
     stats = dict(l.split("=") for l in str(g["stats"]).split())
     R = int(stats["block_rows"])
     x, tiles, nan = oracle.solve_system(g["perm"], s.n, R, g["dag"], int(stats["storage_count"]), tiles_in,

@@ -20,12 +20,13 @@ def triplet_hash(s):
 
 
 @pytest.mark.parametrize("name", ["lap2d_8", "lap2d_32", "lap2d_128", "var3d_16", "cd_40", "cd_17", "band_3000",
-                                  "band_130", "zdiag_600"])
+                                  "band_130", "zdiag_600", "spd_lap2d_8", "spd_lap2d_32", "spd_var3d_16"])
 def test_plan_matches_reference(sg, wl, name):
+    """symmetric (spd_*) inputs give the reference's LL^T DAG (llt / mult ops, L leaves only)."""
     s = golden_cases(wl)[name]()
     g = golden(name)
     assert triplet_hash(s) == str(g["ahash"]), "generator drifted from the fixture"
-    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals, symmetric=s.symmetric)
     perm, ops, L, U = p.export()
     np.testing.assert_array_equal(perm, g["perm"])
     assert ops.shape == g["dag"].shape
@@ -83,14 +84,12 @@ def test_input_tiles_scatter(sg, wl):
     np.testing.assert_array_equal(full[:s.n, :s.n], Ap)
 
 
-@pytest.mark.parametrize("bad", ["symmetric", "index", "zero_block"])
+@pytest.mark.parametrize("bad", ["index", "zero_block"])
 def test_plan_rejects_bad_input(sg, wl, bad):
     s = wl.lap2d(16)
     rows, cols, vals = s.rows.copy(), s.cols.copy(), s.vals.copy()
     sym = False
-    if bad == "symmetric":
-        sym = True
-    elif bad == "index":
+    if bad == "index":
         rows[3] = s.n + 5
     else:  # drop every entry of block row 0 -> structurally zero diagonal block
         keep = (rows >= 64) & (cols >= 64)
