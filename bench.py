@@ -49,6 +49,8 @@ METRIC = "solves/s mixed+IR vs plain FP64 GPU LU at resid<=1e-10; p50/p99 latenc
 WORKLOADS = {
     "var48": "3D 7-point var-coef diffusion 48^3 (n=110592, nnz=760320), 1 RHS, factor+solve to rel resid<=1e-10",
     "lap64": "3D 7-point Laplacian 64^3 (n=262144, nnz=1810432), 64 RHS, factor+solve to rel resid<=1e-10",
+    "lap64spd": "3D 7-point Laplacian 64^3 given as its lower triangle (symmetric: LL^T path), 64 RHS, "
+                "factor+solve to rel resid<=1e-10",
     "var24": "3D 7-point var-coef diffusion 24^3 (n=13824, nnz=93312), 1 RHS, factor+solve to rel resid<=1e-10",
     "serving": "serving stream: Poisson arrivals, random band systems n log-uniform [2000, 200000], 3-27 nnz/row "
                "within half-band 0.02n, diag 1.1 x row abs sum, 1-16 RHS; continuous batching, pool admission",
@@ -67,7 +69,7 @@ class Work:
         self.desc = WORKLOADS[name]
         self.systems = make_workload(name)
         t0 = time.perf_counter()
-        self.plans = [sg.Plan(s.n, s.rows, s.cols, s.vals) for s in self.systems]
+        self.plans = [sg.Plan(s.n, s.rows, s.cols, s.vals, symmetric=s.symmetric) for s in self.systems]
         self.plan = self.plans[0] if len(self.plans) == 1 else sg.merge_plans(self.plans)
         self.t_plan = time.perf_counter() - t0
         s0 = self.systems[0]
@@ -112,6 +114,8 @@ def make_workload(name: str):
     import soglu_gb300.workloads as wl
     if name == "lap64":
         return [wl.lap3d(64, nrhs=64)]
+    if name == "lap64spd":
+        return [wl.spd_lower(wl.lap3d(64, nrhs=64))]
     if name == "batch1024":
         return wl.convdiff_batch(1024)
     return [wl.varcoef3d(24 if name == "var24" else 48)]
@@ -134,11 +138,11 @@ TRAFFIC: dict = {"var48": 251.71e6 + 3.45e9}
 
 
 def algorithmic_flops(op_count) -> float:
-    """Dense-tile flops of the DAG: mul/mulneg 2*64^3, lu 2/3*64^3,
-    lowerInv/upperInv 1/3*64^3, sub 64^2 (per unit op)."""
+    """Dense-tile flops of the DAG: mul/mulneg/mult 2*64^3, lu 2/3*64^3,
+    llt and lowerInv/upperInv 1/3*64^3, sub 64^2 (per unit op)."""
     t = 64.0 ** 3
-    return (op_count[8] + op_count[9]) * 2 * t + op_count[1] * 2 / 3 * t + (op_count[2] + op_count[3]) * t / 3 \
-        + op_count[4] * 64.0 ** 2
+    return (op_count[8] + op_count[9] + op_count[11]) * 2 * t + op_count[1] * 2 / 3 * t \
+        + (op_count[2] + op_count[3] + op_count[10]) * t / 3 + op_count[4] * 64.0 ** 2
 
 
 class ClockSampler:
@@ -338,7 +342,7 @@ def run_reference(args):
         return 0
     build_native()
     sg = load_package()
-    if args.workload == "lap64":
+    if args.workload in ("lap64", "lap64spd"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU executor restatement keeps every 64^3 tile "
                           "resident (50 GB of host memory, no free-after-last-use); run the default workload"}))
         return 0
@@ -493,7 +497,7 @@ def run_ours(args):
                      "frac": flops / (f64m * 1e-3) / 1e12 / peaks["fp64_tflops"],
                      "peak_source": "cuBLAS DGEMM measured in this run", "avg_factor_ms": f64m}
         cpu = None
-        if world == 1 and args.workload != "lap64" and not args.no_cpu_baseline:
+        if world == 1 and args.workload not in ("lap64", "lap64spd") and not args.no_cpu_baseline:
             cores = os.cpu_count() or 1
             d, dt, _ = cpu_sample(work, sg, cores, 15.0)
             cpu = {"value": d / dt, "unit": "solves/s", "cores": cores, "kind": "port",
@@ -561,8 +565,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="var48")
-    ap.add_argument("--executor", type=int, default=0,
-                    help="0 persistent (static order), 1 per level, 2 ready queue, 3 autotuned")
+    ap.add_argument("--executor", type=int, default=3,
+                    help="0 persistent (static order), 1 per level, 2 ready queue, 3 autotuned (default: the "
+                         "first, untimed factorisation times the persistent executors and keeps the faster)")
     ap.add_argument("--stages", type=int, default=0, help="mixed path operand stages: 1, 2, or 0 = tuned")
     ap.add_argument("--requests", type=int, default=32, help="serving: requests per rate")
     ap.add_argument("--rates", default="0.5,2,8", help="serving: Poisson arrival rates (requests/s)")

@@ -137,15 +137,20 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
         const double* sA = sm + s * F64_STAGE;
         const double* sB = sA + 32 * 68;
         const double sgn = tk.pair_b[p] < 0 ? -1.0 : 1.0;
-        // B[k][n] at sB[k * sk + n * sn]: [k][40] layout, or [n][68] for a transposed operand
-        const bool tr = ((tk.pair_b[p] < 0 ? -tk.pair_b[p] : tk.pair_b[p]) & PAIR_TRANS) != 0;
-        const int sk = tr ? 1 : 40, sn = tr ? 68 : 1;
-        const double* bq = sB + (ch * 16 + g) * sn + t * sk;
+        if ((tk.pair_b[p] < 0 ? -tk.pair_b[p] : tk.pair_b[p]) & PAIR_TRANS) {  // B[k][n] = sB[n][k]
 #pragma unroll
-        for (int k0 = 0; k0 < 64; k0 += 4) {
-            const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
+            for (int k0 = 0; k0 < 64; k0 += 4) {
+                const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
 #pragma unroll
-            for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, bq[k0 * sk + nt * 8 * sn]);
+                for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, sB[(ch * 16 + nt * 8 + g) * 68 + k0 + t]);
+            }
+        } else {
+#pragma unroll
+            for (int k0 = 0; k0 < 64; k0 += 4) {
+                const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
+#pragma unroll
+                for (int nt = 0; nt < 2; nt++) dmma_8x8x4(acc[nt], a, sB[(k0 + t) * 40 + ch * 16 + nt * 8 + g]);
+            }
         }
         __syncthreads();
     }
@@ -247,11 +252,14 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
     T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
     float mu = 0.f;
     if (CHOL) {
-        const T sr = sqrt(piv[r]);
+        T* sq = rowbuf;  // sqrt of the pivots (the pivot-row buffers are free now)
+        if (tid < 64) sq[tid] = sqrt(piv[tid]);
+        __syncthreads();
+        const T sr = sq[r];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int c = q + 4 * m;
-            const T v = r > c ? a[m] * sqrt(piv[c]) : (r == c ? sr : T(0));
+            const T v = r > c ? a[m] * sq[c] : (r == c ? sr : T(0));
             L[4 * m] = v;
             mu = fmaxf(mu, fabsf((float)v));
         }
