@@ -314,8 +314,9 @@ typedef struct {
 } sog_request_info;
 /* opt: the systems' options (NULL = SOG_MIXED, 10 refinement steps, 1e-10) */
 int sog_server_create(sog_ctx *ctx, const sog_options *opt, const sog_server_options *sopt, sog_server **out);
+/* symmetric: lower triangle given, factored L L^T (as sog_plan_build) */
 int sog_server_submit(sog_server *srv, int32_t n, int64_t nnz, const int32_t *I, const int32_t *J, const double *V,
-                      int32_t nrhs, const double *b, int64_t *id);
+                      int32_t symmetric, int32_t nrhs, const double *b, int64_t *id);
 /* Wait for the answer (timeout_ms < 0: no limit; SOG_ETIMEOUT if still
  * running). x (if not NULL) receives nrhs x n values. */
 int sog_server_wait(sog_server *srv, int64_t id, double timeout_ms, double *x, sog_request_info *info);

@@ -124,7 +124,7 @@ def lib() -> C.CDLL:
         "sog_plan_merge": ([P, I32, P], I32), "sog_plan_segments": ([P, P, P], I32),
         "sog_solve_batch": ([P, P, P, P, P], I32), "sog_solve_batch_device": ([P, P, P, P, P], I32),
         "sog_ctx_trim": ([P], I32), "sog_server_create": ([P, P, P, P], I32),
-        "sog_server_submit": ([P, I32, I64, P, P, P, I32, P, P], I32),
+        "sog_server_submit": ([P, I32, I64, P, P, P, I32, I32, P, P], I32),
         "sog_server_wait": ([P, I64, D, P, P], I32), "sog_server_solve": ([P, I64, I32, P, P, P], I32),
         "sog_server_release": ([P, I64], I32), "sog_server_counters": ([P, P], I32),
         "sog_server_destroy": ([P], None),
@@ -431,7 +431,7 @@ class Server:
         self._n = {}
         _check(lib().sog_server_create(ctx._h, C.byref(self.opt), C.byref(self.sopt), C.byref(self._h)))
 
-    def submit(self, n: int, rows, cols, vals, b) -> int:
+    def submit(self, n: int, rows, cols, vals, b, symmetric: bool = False) -> int:
         r = np.ascontiguousarray(rows, dtype=np.int32)
         c = np.ascontiguousarray(cols, dtype=np.int32)
         v = np.ascontiguousarray(vals, dtype=np.float64)
@@ -440,7 +440,8 @@ class Server:
         if bb.size != k * n:
             raise ValueError(f"right-hand sides must have shape ({n},) or (k, {n})")
         rid = C.c_int64()
-        _check(lib().sog_server_submit(self._h, int(n), r.size, _p(r), _p(c), _p(v), k, _p(bb), C.byref(rid)))
+        _check(lib().sog_server_submit(self._h, int(n), r.size, _p(r), _p(c), _p(v), int(symmetric), k, _p(bb),
+                                       C.byref(rid)))
         self._n[rid.value] = (n, bb.shape)
         return rid.value
 

@@ -92,6 +92,7 @@ Plan merge_plans(const std::vector<const Plan*>& ps) {
         sg.noff = noff;
         sg.trip_off = toff;
         sg.ntrip = (int64_t)p.scatter_tile.size();
+        sg.symmetric = p.symmetric;
         m.segs.push_back(sg);
         m.stages = std::max(m.stages, p.stages);
         m.t_order += p.t_order;

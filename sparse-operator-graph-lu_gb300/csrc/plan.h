@@ -66,6 +66,7 @@ struct Leaf {
 struct Segment {
     int32_t row0 = 0, n = 0, R = 0;
     int64_t noff = 0, trip_off = 0, ntrip = 0;
+    bool symmetric = false;  // an LL^T system (its L leaves only)
 };
 
 // Everything the executor needs, in the reference's terms.

@@ -699,7 +699,9 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     const Plan& p = plan->p;
     // + diagonal inverses and look-ahead products added for the substitution,
     // + the transposed L leaves of an LL^T plan
-    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows + (p.symmetric ? p.L.size() : 0)) * 4096 *
+    bool any_sym = p.symmetric;
+    for (const Segment& sg : p.segs) any_sym = any_sym || sg.symmetric;
+    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
                      elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
@@ -741,9 +743,29 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // where the DAG already computes them)
     std::vector<Op> ops2 = p.ops;
     int32_t storage2 = p.storage_count;
-    // LL^T: the upper factor of the substitution is L^T (upperSolverT,
-    // BlockPlanner.cpp:752-797), materialised as transposed L leaves
-    if (p.symmetric) add_transposed_leaves(ops2, storage2, s->L, s->U);
+    // LL^T systems: the upper factor of the substitution is L^T (upperSolverT,
+    // BlockPlanner.cpp:752-797), materialised as transposed L leaves (in a
+    // batch, of the symmetric systems only)
+    {
+        std::vector<Leaf> lsym;
+        if (p.segs.empty()) {
+            if (p.symmetric) lsym = s->L;
+        } else {
+            std::vector<char> sym_row(s->R, 0);
+            for (const Segment& sg : p.segs)
+                if (sg.symmetric)
+                    for (int r = 0; r < sg.R; r++) sym_row[sg.row0 / 64 + r] = 1;
+            for (const Leaf& lf : s->L)
+                if (sym_row[lf.bi]) lsym.push_back(lf);
+        }
+        if (!lsym.empty()) {
+            std::vector<Leaf> ut;
+            add_transposed_leaves(ops2, storage2, lsym, ut);
+            s->U.insert(s->U.end(), ut.begin(), ut.end());
+            std::sort(s->U.begin(), s->U.end(),
+                      [](const Leaf& a, const Leaf& b) { return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj; });
+        }
+    }
     std::vector<int32_t> ldinv, udinv;
     add_diag_inverses(ops2, storage2, s->R, s->L, s->U, ldinv, udinv);
     std::vector<int32_t> lla, ula;

@@ -41,6 +41,7 @@ struct Batch;
 struct Request {
     int64_t id = 0;
     int32_t n = 0, nrhs = 0;
+    bool symmetric = false;
     std::vector<int32_t> I, J;
     std::vector<double> V, b, x;
     sog_plan* plan = nullptr;
@@ -130,7 +131,7 @@ void sog_server::planner_loop() {
         }
         const Clock::time_point t0 = Clock::now();
         sog_plan* p = nullptr;
-        int rc = sog_plan_build(r->n, (int64_t)r->I.size(), 0, r->I.data(), r->J.data(), r->V.data(),
+        int rc = sog_plan_build(r->n, (int64_t)r->I.size(), r->symmetric ? 1 : 0, r->I.data(), r->J.data(), r->V.data(),
                                 sopt.planner_omp_threads, &p);
         std::string err = rc ? sog_last_error() : "";
         uint64_t bytes = 0;
@@ -371,12 +372,13 @@ int sog_server_create(sog_ctx* ctx, const sog_options* opt, const sog_server_opt
 }
 
 int sog_server_submit(sog_server* s, int32_t n, int64_t nnz, const int32_t* I, const int32_t* J, const double* V,
-                      int32_t nrhs, const double* b, int64_t* id) {
+                      int32_t symmetric, int32_t nrhs, const double* b, int64_t* id) {
     if (!s || !id || n <= 0 || nnz < 0 || nrhs <= 0 || !b || (nnz > 0 && (!I || !J || !V)))
         return fail(SOG_EINVAL, "bad request");
     auto r = std::make_unique<Request>();
     r->n = n;
     r->nrhs = nrhs;
+    r->symmetric = symmetric != 0;
     r->I.assign(I, I + nnz);
     r->J.assign(J, J + nnz);
     r->V.assign(V, V + nnz);

@@ -110,3 +110,24 @@ def test_further_rhs_on_resident_factors(sg, wl):
         srv.solve(rid, b2)
     srv.close()
     ctx.close()
+
+
+def test_symmetric_request_in_a_mixed_batch(sg, wl):
+    """A symmetric request (lower triangle, LL^T) and general requests share
+    one launch; each gets its own solution."""
+    spd = wl.spd_lower(wl.lap2d(40))
+    gen = wl.random_band(2500, seed=77, nrhs=2)
+    ctx = sg.Context()
+    srv = sg.Server(ctx, precision=sg.MIXED, planners=2, batch_window_ms=5000)
+    a = srv.submit(spd.n, spd.rows, spd.cols, spd.vals, spd.b, symmetric=True)
+    g = srv.submit(gen.n, gen.rows, gen.cols, gen.vals, gen.b)
+    xa, ia = srv.wait(a)
+    xg, ig = srv.wait(g)
+    assert ia["batch_id"] == ig["batch_id"] and ia["batch_size"] == 2
+    assert np.linalg.norm(xa - spd.x_true) <= 1e-8 * np.linalg.norm(spd.x_true)
+    r = gen.b - gen.matvec(xg)
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(gen.b) * 2
+    srv.release(a)
+    srv.release(g)
+    srv.close()
+    ctx.close()
