@@ -8,6 +8,7 @@
 // Block matrices are quadtrees over a power-of-two grid of blocks; absent
 // children are zero blocks and generate no ops.
 #include <omp.h>
+#include <parallel/algorithm>
 
 #include <algorithm>
 #include <chrono>
@@ -447,7 +448,8 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
     }
     p.cfg = make_config(n);
     p.ord = gps_order(n, I, J, V, threads);
-    for (size_t k = 0; k < I.size(); k++) { I[k] = p.ord.old_to_new[I[k]]; J[k] = p.ord.old_to_new[J[k]]; }
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < (int64_t)I.size(); k++) { I[k] = p.ord.old_to_new[I[k]]; J[k] = p.ord.old_to_new[J[k]]; }
     p.t_order = now_s() - t0;
     double t1 = now_s();
 
@@ -489,9 +491,10 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
     int32_t froot = fz.root_for(R);
     {
         std::vector<int64_t> keys(I.size());
-        for (size_t k = 0; k < I.size(); k++) keys[k] = (int64_t)(I[k] >> 6) * R + (J[k] >> 6);
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < (int64_t)I.size(); k++) keys[k] = (int64_t)(I[k] >> 6) * R + (J[k] >> 6);
         std::vector<int64_t> uk(keys);
-        std::sort(uk.begin(), uk.end());
+        __gnu_parallel::sort(uk.begin(), uk.end());
         uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
         for (int64_t key : uk) {
             int32_t lf = fz.leaf_at(froot, (int)(key / R), (int)(key % R));
@@ -519,18 +522,18 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
         // value scatter: last occurrence of a duplicate wins
         p.scatter_tile.resize(I.size());
         p.scatter_off.resize(I.size());
-        std::vector<int32_t> order(I.size());
-        for (size_t k = 0; k < I.size(); k++) {
-            int32_t lf = fz.find_leaf(froot, I[k] >> 6, J[k] >> 6);
-            p.scatter_tile[k] = fz.at(lf).id - 1;
+        const int64_t nt = (int64_t)I.size();
+        std::vector<std::pair<int64_t, int32_t>> slot(nt);  // (tile element, triplet): sorts stably by element
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < nt; k++) {
+            const int32_t lf = fz.find_leaf(froot, I[k] >> 6, J[k] >> 6);  // read-only walk
+            p.scatter_tile[k] = fz.nodes[lf].id - 1;
             p.scatter_off[k] = (int16_t)((I[k] & 63) * 64 + (J[k] & 63));
-            order[k] = (int32_t)k;
+            slot[k] = {(int64_t)p.scatter_tile[k] * 4096 + p.scatter_off[k], (int32_t)k};
         }
-        std::vector<int64_t> slot(I.size());
-        for (size_t k = 0; k < I.size(); k++) slot[k] = (int64_t)p.scatter_tile[k] * 4096 + p.scatter_off[k];
-        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return slot[a] < slot[b]; });
-        for (size_t k = 0; k + 1 < order.size(); k++)
-            if (slot[order[k]] == slot[order[k + 1]]) p.scatter_tile[order[k]] = -1;
+        __gnu_parallel::sort(slot.begin(), slot.end());
+        for (int64_t k = 0; k + 1 < nt; k++)
+            if (slot[k].first == slot[k + 1].first) p.scatter_tile[slot[k].second] = -1;
     }
     std::vector<int32_t> finputs;
     for (int32_t id = 1; id <= p.n_input; id++) finputs.push_back(id);
