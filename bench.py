@@ -217,7 +217,7 @@ def barrier(world: int):
 
 def measure_peaks(torch, device) -> dict:
     """cuBLAS TF32 and FP64 GEMM throughput on this GPU (denominators for the
-    3xTF32 and DMMA tile products; the generated file holds bf16/HBM only)."""
+    3xTF32 and DMMA tile products; MEASURED_PEAKS.json holds bf16 and HBM figures only)."""
     out = {}
     torch.backends.cuda.matmul.allow_tf32 = True
     for name, dt, n, reps in (("tf32_tflops", torch.float32, 8192, 5), ("fp64_tflops", torch.float64, 4096, 3)):
