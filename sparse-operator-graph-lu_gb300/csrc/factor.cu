@@ -171,18 +171,24 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
 // kept, 0 -> +1e-9) as ludcmpSimple does (MatrixStdDouble.cpp:2751-2761); the
 // pivot test, clamp and growth ratio are evaluated in FP64 in both precisions.
 //
-// With WITH_LINV the elimination runs on the augmented block [A | I]: the same
-// multipliers applied to the identity leave L^-1 in the right half, so the
-// inverse of the unit lower factor (lowerInv of this LU's L, which the
-// recursion always needs next) comes out of the same 64 steps.
+// Both triangular inverses come out of the same 64 steps, in one register
+// array y per row: for c <= r it holds L^-1[r][c] (the multipliers applied to
+// the identity beside A, i.e. elimination on [A | I]: lowerInv of this LU's L,
+// which the recursion always needs next); for c > r it holds X[r][c] of
+// X = (D^-1 U)^-1, built by column operations: at step k every row r <= k
+// subtracts X[r][k] times the published scaled pivot row, and U^-1 = X D^-1
+// (upperInv of this LU's U). Rows below the pivot touch only columns <= k of
+// y, rows at or above it only columns > k, so the halves never collide, and
+// the column operations run on rows the elimination leaves idle.
 __device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double fast_rcp(double x) { return __drcp_rn(x); }
 
-// LU task; with CHOL the LL^T task of a symmetric tile (lltdcmpSimple,
-// MatrixStdDouble.cpp:2629-2668): the same elimination on the tile
-// symmetrised from its lower triangle, pivots below 1e-20 raised to it, and
-// L = L_lu diag(sqrt(pivots)), L^-1 = diag(1/sqrt(pivots)) L_lu^-1.
-template <typename T, bool WITH_LINV, bool CHOL = false>
+// LU task (outputs L, U; L^-1 if tk.b, U^-1 if tk.c); with CHOL the LL^T task
+// of a symmetric tile (lltdcmpSimple, MatrixStdDouble.cpp:2629-2668): the same
+// elimination on the tile symmetrised from its lower triangle, pivots below
+// 1e-20 raised to it, and L = L_lu diag(sqrt(pivots)),
+// L^-1 = diag(1/sqrt(pivots)) L_lu^-1.
+template <typename T, bool CHOL = false>
 __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* sm) {
     T* rowbuf = sm;          // [2][8][64] scaled pivot rows of A for the current block
     T* wbuf = sm + 1024;     // [2][8][64] rows of the running L^-1 for the current block
@@ -190,35 +196,37 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
     T* rpiv = piv + 64;      // [64] their reciprocals
     T* raw = piv + 128;      // [64] pivots before the clamp
     __shared__ float s_maxa, s_maxu;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, r = tid >> 2, q = tid & 3;
+    const int tid = threadIdx.x, lane = tid & 31, r = tid >> 2, q = tid & 3;
     if (tid == 0) {
         s_maxa = 0.f;
         s_maxu = 0.f;
     }
     const T* A = tiles + (size_t)tk.a[task] * 4096 + r * 64 + q;
     const T* At = tiles + (size_t)tk.a[task] * 4096 + q * 64 + r;  // column r: A[q + 4m][r]
-    T a[16], w[16];
+    T a[16], y[16];
     float ma = 0.f;
 #pragma unroll
     for (int m = 0; m < 16; m++) {
         a[m] = (CHOL && q + 4 * m > r) ? __ldcg(At + 4 * m * 64) : __ldcg(A + 4 * m);
         ma = fmaxf(ma, fabsf((float)a[m]));
-        if (WITH_LINV) w[m] = (q + 4 * m == r) ? T(1) : T(0);
+        y[m] = (q + 4 * m == r) ? T(1) : T(0);
     }
     __syncthreads();
-    (void)warp;
     // One pivot per step: the four owners of row k publish it (scaled by the
     // pivot reciprocal) and their row of L^-1; after one CTA barrier every
-    // lower row applies the rank-1 update. Buffers alternate by step so one
-    // barrier per step suffices. (A variant factoring 8-row panels inside one
-    // warp with 8 CTA barriers measured slower on GB300: the single-warp panel
-    // serialises more than the barriers cost.)
+    // lower row applies the rank-1 update and every upper row its column
+    // operation. Buffers alternate by step so one barrier per step suffices.
+    // (A variant factoring 8-row panels inside one warp with 8 CTA barriers
+    // measured slower on GB300: the single-warp panel serialises more than the
+    // barriers cost.)
 #pragma unroll
     for (int k = 0; k < 64; k++) {
         const int km = k >> 2, kq = k & 3;
         T* ub = rowbuf + (k & 1) * 64;
         T* wb = wbuf + (k & 1) * 64;
-        const T aik = __shfl_sync(FULL, a[km], (lane & ~3) | kq);  // a[r][k] for this thread's row
+        const int src = (lane & ~3) | kq;
+        const T aik = __shfl_sync(FULL, a[km], src);  // a[r][k] for this thread's row
+        const T xrk = CHOL ? T(0) : __shfl_sync(FULL, y[km], src);  // X[r][k] (rows r <= k)
         if (r == k) {
             // LU: clamp |u_kk| < 1e-9 to +-1e-9 (0 -> +1e-9); LL^T: p < 1e-20 -> 1e-20
             const T tiny = T(1e-9);
@@ -229,7 +237,7 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
             for (int m = 0; m < 16; m++) {
                 const int c = q + 4 * m;
                 if (c > k) ub[c] = a[m] * rp;
-                if (WITH_LINV && c <= k) wb[c] = w[m];
+                else wb[c] = y[m];
             }
             if (q == 0) {
                 piv[k] = p;
@@ -244,12 +252,19 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
             for (int m = 0; m < 16; m++) {
                 const int c = q + 4 * m;
                 if (c > k) a[m] -= aik * ub[c];
-                if (WITH_LINV && c <= k) w[m] -= lik * wb[c];
+                else y[m] -= lik * wb[c];
             }
             if (q == kq) a[km] = lik;
+        } else if (!CHOL) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int c = q + 4 * m;
+                if (c > k) y[m] -= xrk * ub[c];
+            }
         }
     }
     T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
+    const int32_t linv = tk.b[task];
     float mu = 0.f;
     if (CHOL) {
         T* sq = rowbuf;  // sqrt of the pivots (the pivot-row buffers are free now)
@@ -263,11 +278,11 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
             L[4 * m] = v;
             mu = fmaxf(mu, fabsf((float)v));
         }
-        if (WITH_LINV) {
-            T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+        if (linv > 0) {
+            T* W = tiles + (size_t)linv * 4096 + r * 64 + q;
             const T isr = T(1) / sr;
 #pragma unroll
-            for (int m = 0; m < 16; m++) W[4 * m] = w[m] * isr;
+            for (int m = 0; m < 16; m++) W[4 * m] = q + 4 * m <= r ? y[m] * isr : T(0);
         }
     } else {
         T* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + q;
@@ -279,10 +294,19 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
             U[4 * m] = u;
             mu = fmaxf(mu, fabsf((float)u));
         }
-        if (WITH_LINV) {
-            T* W = tiles + (size_t)tk.b[task] * 4096 + r * 64 + q;
+        if (linv > 0) {
+            T* W = tiles + (size_t)linv * 4096 + r * 64 + q;
 #pragma unroll
-            for (int m = 0; m < 16; m++) W[4 * m] = w[m];
+            for (int m = 0; m < 16; m++) W[4 * m] = q + 4 * m <= r ? y[m] : T(0);
+        }
+        const int32_t uinv = tk.c[task];
+        if (uinv > 0) {
+            T* V = tiles + (size_t)uinv * 4096 + r * 64 + q;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int c = q + 4 * m;
+                V[4 * m] = c >= r ? y[m] * rpiv[c] : T(0);
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -510,14 +534,8 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                 gemm_f32_tc<S>(tk, tiles, task, sm, st, phase);
             }
             break;
-        case K_LU:
-            if (tk.b[task] > 0) lu_task<T, true>(tk, tiles, task, sm);
-            else lu_task<T, false>(tk, tiles, task, sm);
-            break;
-        case K_LLT:
-            if (tk.b[task] > 0) lu_task<T, true, true>(tk, tiles, task, sm);
-            else lu_task<T, false, true>(tk, tiles, task, sm);
-            break;
+        case K_LU: lu_task<T, false>(tk, tiles, task, sm); break;
+        case K_LLT: lu_task<T, true>(tk, tiles, task, sm); break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;
         case K_UINV: inv_task<T, false>(tk, tiles, task, sm); break;
         case K_SUB: sub_task<T>(tk, tiles, task); break;
@@ -618,7 +636,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
 // producer fills it. The launch ends when every item has completed; no CTA
 // ever waits inside a task.
 template <typename T, int S>
-__global__ void __launch_bounds__(NT) factor_queue_kernel(DevTasks tk, T* tiles) {
+__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_queue_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item, s_next, s_stop;
@@ -715,7 +733,7 @@ __device__ void release_item(const DevTasks& tk, int task) {
 // co-resident the launch cannot deadlock. A critical task is usually claimed
 // before it is ready, so its claimant starts as soon as the count drops.
 template <typename T, int S>
-__global__ void __launch_bounds__(NT) factor_ordered_kernel(DevTasks tk, T* tiles) {
+__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_ordered_kernel(DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item;

@@ -861,6 +861,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),
              o_out2 = L.add<int32_t>(g.ntasks), o_a = L.add<int32_t>(g.ntasks), o_b = L.add<int32_t>(g.ntasks),
+             o_c = L.add<int32_t>(g.ntasks),
              o_pptr = L.add<int32_t>(g.ntasks + 1), o_pa = L.add<int32_t>(g.pair_a.size()),
              o_pb = L.add<int32_t>(g.pair_b.size()), o_sptr = L.add<int32_t>(g.ntasks + 1),
              o_succ = L.add<int32_t>(g.succ.size()), o_ndep0 = L.add<int32_t>(g.ntasks),
@@ -907,6 +908,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.out2 = put(A, o_out2, g.out2, st);
     dt.a = put(A, o_a, g.a, st);
     dt.b = put(A, o_b, g.b, st);
+    dt.c = put(A, o_c, g.c, st);
     dt.prio = put(A, o_prio, g.prio, st);
     dt.pair_ptr = put(A, o_pptr, g.pair_ptr, st);
     dt.pair_a = put(A, o_pa, g.pair_a, st);

@@ -83,7 +83,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     // pass 1: one task per produced block (LU: per result pair)
     struct T0 {
         uint8_t kind;
-        int32_t out, out2, a, b;
+        int32_t out, out2, a, b, c = 0;
         std::vector<int32_t> pa, pb;
         bool dead = false;
     };
@@ -168,6 +168,19 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         X.dead = true;
         fused_inv++;
     }
+    // fuse  Y = U^-1  into the LU task producing U: the same sweep applies the
+    // published pivot rows as column operations to the identity above the
+    // diagonal (LU task field c = Y)
+    for (size_t s = 0; s < tl.size(); s++) {
+        T0& X = tl[s];
+        if (X.dead || X.kind != K_UINV || X.a <= 0) continue;
+        const int32_t t = producer[X.a];
+        if (t < 0 || tl[t].kind != K_LU || tl[t].out2 != X.a || tl[t].c != 0) continue;
+        tl[t].c = X.out;
+        producer[X.out] = t;
+        X.dead = true;
+        fused_inv++;
+    }
     // renumber live tasks
     std::vector<int32_t> newid(tl.size(), -1);
     TaskGraph g;
@@ -189,6 +202,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         g.out2.push_back(x.out2);
         g.a.push_back(x.a);
         g.b.push_back(x.b);
+        g.c.push_back(x.c);
         g.pair_a.insert(g.pair_a.end(), x.pa.begin(), x.pa.end());
         g.pair_b.insert(g.pair_b.end(), x.pb.begin(), x.pb.end());
         g.pair_ptr[newid[t] + 1] = (int32_t)g.pair_a.size();

@@ -35,7 +35,7 @@ struct TaskGraph {
     int32_t ntasks = 0;
     int32_t storage_count = 0;
     std::vector<uint8_t> kind, parts;
-    std::vector<int32_t> out, out2, a, b;      // block ids (see kernels.h DevTasks)
+    std::vector<int32_t> out, out2, a, b, c;   // block ids (see kernels.h DevTasks)
     std::vector<int32_t> pair_ptr;             // ntasks+1; GEMM operand pairs
     std::vector<int32_t> pair_a, pair_b;       // pair_b < 0: subtract A*B(|pair_b|)
     std::vector<int32_t> succ_ptr, succ;       // successor tasks
@@ -49,7 +49,7 @@ struct TaskGraph {
     int64_t total_items = 0;                   // sum of parts
     int64_t gemm_pairs = 0;
     int64_t fused_subs = 0;
-    int64_t fused_inverses = 0;  // lowerInv tasks folded into their LU task
+    int64_t fused_inverses = 0;  // lowerInv / upperInv tasks folded into their LU task
     int64_t aliased_copies = 0;  // copy ops (sub with src = 0) replaced by aliasing
     int64_t aliased_inverses = 0;  // repeated lowerInv / upperInv of one block replaced by aliasing
     int64_t count[NUM_KINDS] = {0, 0, 0, 0, 0, 0, 0};

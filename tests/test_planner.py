@@ -127,7 +127,7 @@ def test_task_graph(sg, wl, name):
     assert tg["sub"] + tg["fused_subs"] + tg["aliased_copies"] == ops.get("sub", 0)
     assert tg["linv"] + tg["uinv"] + tg["fused_inverses"] + tg["aliased_inverses"] == \
         ops.get("lowerInv", 0) + ops.get("upperInv", 0) + tg["added_inverses"]
-    assert 0 < tg["fused_inverses"] <= tg["lu"]
+    assert 0 < tg["fused_inverses"] <= 2 * tg["lu"]  # lowerInv and upperInv of each LU
     assert tg["levels"] <= info["stages"]
     assert tg["critical_path"] == tg["levels"]
     tg4 = p.task_graph_info(gemm_split=4)
