@@ -45,7 +45,9 @@ constexpr int LU_ELEMS = 32 * 64 + 3 * 64;          // 2 x 8 pivot rows of A and
 template <typename T, int S>
 constexpr int smem_elems() {
     // FP64: double-buffered DMMA stages; FP32: the tcgen05 operand area
-    constexpr int g = sizeof(T) == 8 ? 2 * F64_STAGE : S * tc::STAGE_BYTES / 4;
+    // (+128 B: the raw slots start on a 128-byte boundary, as TMA tile copies require)
+    constexpr int g =
+        sizeof(T) == 8 ? 2 * F64_STAGE : (S * tc::STAGE_BYTES + tc::raw_slots<S>() * tc::RAW_BYTES + 128) / 4;
     constexpr int t = INV_ELEMS > LU_ELEMS ? INV_ELEMS : LU_ELEMS;
     return g > t ? g : t;
 }
@@ -414,25 +416,36 @@ __device__ void trans_task(const DevTasks& tk, T* __restrict__ tiles, int task, 
     for (int e = threadIdx.x; e < 4096; e += NT) R[e] = sm[(e >> 6) * LD + (e & 63)];
 }
 
-// C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh). The
-// next pair's operands load from L2 into registers while the current pair's
-// MMAs run; `phase` is this CTA's mbarrier parity, carried across tasks.
+// C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh).
+// Thread 0 keeps up to R operand pairs in flight: the TMA copies the raw FP32
+// tiles (contiguous 16 KB each) into a ring of R slots (mbarrier completion). Every warp splits its
+// share of the oldest slot into a stage of [A_hi; A_lo], B_hi^T, B_lo^T and
+// signals the stage's `full` barrier; thread 0 then issues that stage's MMAs
+// and refills the slot, while the other warps already stage the next pair
+// (no CTA barrier per pair). Only the first pair's copy latency is exposed.
+// `phase` holds this CTA's mbarrier parities (stages free: bits 0-1, stages
+// full: bits 16-17, thread 0 only; raw slots: bits 8-10), carried across tasks.
+constexpr int PAIRS_SMEM = 128;  // operand pair ids staged in shared memory per task
 template <int S>
 __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm, tc::State& st,
                             uint32_t& phase) {
+    constexpr int R = tc::raw_slots<S>();
+    __shared__ int32_t s_pa[PAIRS_SMEM], s_pb[PAIRS_SMEM];
     unsigned char* smb = reinterpret_cast<unsigned char*>(sm);
+    unsigned char* raw = smb + S * tc::STAGE_BYTES;
+    raw += (128u - (tc::smem_u32(raw) & 127u)) & 127u;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int p0 = tk.pair_ptr[task], p1 = tk.pair_ptr[task + 1];
     const unsigned long long lim = tk.wait_limit_ns;
-    float4 a4[4], b4[4];
-    auto operands = [&](int p) {
-        const int pbs = tk.pair_b[p], pb = pbs < 0 ? -pbs : pbs;
-        tc::load_pair(tiles + (size_t)tk.pair_a[p] * 4096, tiles + (size_t)(pb & ~PAIR_TRANS) * 4096,
-                      (pb & PAIR_TRANS) != 0, a4, b4);
-    };
     const int n = p1 - p0;
+    for (int j = tid; j < n && j < PAIRS_SMEM; j += NT) {
+        s_pa[j] = tk.pair_a[p0 + j];
+        s_pb[j] = tk.pair_b[p0 + j];
+    }
+    auto pair_a = [&](int i) { return i < PAIRS_SMEM ? s_pa[i] : tk.pair_a[p0 + i]; };
+    auto pair_b = [&](int i) { return i < PAIRS_SMEM ? s_pb[i] : tk.pair_b[p0 + i]; };
     // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
-    // under the operand loads and the MMAs
+    // under the operand copies and the MMAs
     const int quad = warp & 3, colh = (warp >> 2) * 32, init = tk.a[task];
     float4 u[8];
     if (quad < 2 && init > 0) {
@@ -440,23 +453,41 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
 #pragma unroll
         for (int i = 0; i < 8; i++) u[i] = __ldcg(I + i);
     }
-    if (n > 0) operands(p0);
+    __syncthreads();
+    auto fetch = [&](int i) {  // thread 0: copies of pair p0 + i into raw slot i % R
+        const int slot = i % R, pbs = pair_b(i), pb = pbs < 0 ? -pbs : pbs, b = pb & ~PAIR_TRANS;
+        unsigned char* dst = raw + slot * tc::RAW_BYTES;
+        tc::expect_tx(&st.raw[slot], tc::RAW_BYTES);
+        tc::bulk_copy(dst, tiles + (size_t)pair_a(i) * 4096, tc::RAW_BYTES / 2, &st.raw[slot]);
+        tc::bulk_copy(dst + tc::RAW_BYTES / 2, tiles + (size_t)b * 4096, tc::RAW_BYTES / 2, &st.raw[slot]);
+    };
+    if (tid == 0 && n > 0) {
+        tc::fence_proxy_async_global();  // the acquired producers' writes, then the copies
+        for (int i = 0; i < n && i < R; i++) fetch(i);
+    }
     for (int i = 0; i < n; i++) {
-        const int s = i % S;
+        const int s = i % S, slot = i % R;
         unsigned char* stg = smb + s * tc::STAGE_BYTES;
         if (i >= S) {  // the MMAs of pair i-S read this stage
             if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
             phase ^= 1u << s;
         }
-        tc::stage_pair(stg, a4, b4, tk.pair_b[p0 + i] < 0 ? -1.f : 1.f);
+        if (!tc::mbar_wait(&st.raw[slot], (phase >> (8 + slot)) & 1u, lim)) st.fail = 1;
+        phase ^= 1u << (8 + slot);
+        const int pbs = pair_b(i);
+        tc::stage_from_raw(stg, raw + slot * tc::RAW_BYTES, ((pbs < 0 ? -pbs : pbs) & PAIR_TRANS) != 0,
+                           pbs < 0 ? -1.f : 1.f);
         tc::fence_proxy_async();
-        __syncthreads();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&st.full[s]);
         if (tid == 0) {
+            if (!tc::mbar_wait(&st.full[s], (phase >> (16 + s)) & 1u, lim)) st.fail = 1;
+            phase ^= 1u << (16 + s);
             tc::fence_after_sync();
             tc::issue_pair(stg, st.tmem, i == 0);
             tc::mma_commit(&st.bar[s]);
+            if (i + R < n) fetch(i + R);  // every warp has staged from this slot (full barrier)
         }
-        if (i + 1 < n) operands(p0 + i + 1);
     }
     for (int i = n > S ? n - S : 0; i < n; i++) {  // the commits not yet waited for
         const int s = i % S;
@@ -464,22 +495,28 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
         phase ^= 1u << s;
     }
     tc::fence_after_sync();
-    // epilogue: C = init + D[0:64] + D[64:128] (warps 2,3,6,7 hold the lower half)
+    // epilogue: C = init + the four quadrants of D (lanes 0-63: A_hi rows,
+    // 64-127: A_lo rows; columns 0-63: B_hi, 64-127: B_lo). Each warp sums
+    // its lanes' two column halves; warps 2,3,6,7 (the A_lo lanes) pass
+    // theirs through shared memory.
     float* X = sm;  // [64][65], the operand area is free once the MMAs completed
-    float v[32];
+    float v[32], w[32];
+    const uint32_t tq = st.tmem + ((uint32_t)(32 * quad) << 16) + colh;
     if (p0 < p1 && quad >= 2) {
-        tc::tmem_ld32(st.tmem + ((uint32_t)(32 * quad) << 16) + colh, v);
+        tc::tmem_ld32(tq, v);
+        tc::tmem_ld32(tq + 64, w);
         const int row = 32 * quad + lane - 64;
 #pragma unroll
-        for (int i = 0; i < 32; i++) X[row * 65 + colh + i] = v[i];
+        for (int i = 0; i < 32; i++) X[row * 65 + colh + i] = v[i] + w[i];
     }
     __syncthreads();
     if (quad < 2) {
         const int row = 32 * quad + lane;
         if (p0 < p1) {
-            tc::tmem_ld32(st.tmem + ((uint32_t)(32 * quad) << 16) + colh, v);
+            tc::tmem_ld32(tq, v);
+            tc::tmem_ld32(tq + 64, w);
 #pragma unroll
-            for (int i = 0; i < 32; i++) v[i] += X[row * 65 + colh + i];
+            for (int i = 0; i < 32; i++) v[i] += w[i] + X[row * 65 + colh + i];
         } else {
 #pragma unroll
             for (int i = 0; i < 32; i++) v[i] = 0.f;
@@ -503,6 +540,8 @@ __device__ __forceinline__ void tc_setup(tc::State& st) {
     if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&st.tmem);
     if (threadIdx.x == 0) {
         for (int s = 0; s < tc::MAX_STAGES; s++) tc::mbar_init(&st.bar[s], 1);
+        for (int s = 0; s < tc::MAX_STAGES; s++) tc::mbar_init(&st.full[s], NT / 32);
+        for (int s = 0; s < tc::MAX_RAW; s++) tc::mbar_init(&st.raw[s], 1);
         st.fail = 0;
     }
     tc::fence_before_sync();
@@ -636,7 +675,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
 // producer fills it. The launch ends when every item has completed; no CTA
 // ever waits inside a task.
 template <typename T, int S>
-__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_queue_kernel(DevTasks tk, T* tiles) {
+__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_queue_kernel(const __grid_constant__ DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item, s_next, s_stop;
@@ -655,9 +694,10 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
             if (item < 0) {
                 const int slot = atomicAdd(tk.head, 1);
                 if (slot < tk.total_items) {
-                    const unsigned long long t0 = globaltimer_ns();
+                    unsigned long long t0 = 0;
                     unsigned spins = 0;
                     while ((item = ld_acquire(tk.queue + slot)) < 0) {
+                        if (spins == 0) t0 = globaltimer_ns();  // the clock only once waiting
                         if ((++spins & 15) == 0) {
                             if (ld_acquire(tk.done) >= tk.total_items) { item = -1; break; }
                             if (ld_acquire(&tk.status->flags) & ST_TIMEOUT) { item = -1; break; }
@@ -733,7 +773,7 @@ __device__ void release_item(const DevTasks& tk, int task) {
 // co-resident the launch cannot deadlock. A critical task is usually claimed
 // before it is ready, so its claimant starts as soon as the count drops.
 template <typename T, int S>
-__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_ordered_kernel(DevTasks tk, T* tiles) {
+__global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor_ordered_kernel(const __grid_constant__ DevTasks tk, T* tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ int s_item;
@@ -751,9 +791,10 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
                     atomicOr(&tk.status->flags, ST_BAD_ITEM);
                     item = -1;
                 } else {
-                    const unsigned long long t0 = globaltimer_ns();
+                    unsigned long long t0 = 0;
                     unsigned spins = 0;
                     while (ld_acquire(tk.dep + task) > 0) {
+                        if (spins == 0) t0 = globaltimer_ns();  // the clock only once waiting
                         if ((++spins & 15) == 0) {
                             if (ld_acquire(&tk.status->flags) & (ST_TIMEOUT | ST_BAD_ITEM)) { item = -1; break; }
                             if (globaltimer_ns() - t0 > tk.wait_limit_ns) {
@@ -792,7 +833,7 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
 }
 
 template <typename T, int S>
-__global__ void __launch_bounds__(NT) factor_level_kernel(DevTasks tk, T* tiles, const int32_t* items) {
+__global__ void __launch_bounds__(NT) factor_level_kernel(const __grid_constant__ DevTasks tk, T* tiles, const int32_t* items) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     __shared__ tc::State st;

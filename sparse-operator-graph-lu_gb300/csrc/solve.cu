@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     // are ordered after lane 0's acquire by the __syncwarp that follows
     const int* fl = nullptr;  // this position's chunk of the flags
     auto wait_row = [&](int j) -> bool {
-        if (lane == 0) {
+        if (lane == 0 && ld_acquire(fl + j) != epoch) {  // the clock only once waiting
             const unsigned long long t0 = globaltimer_ns();
             while (ld_acquire(fl + j) != epoch) {
                 if (globaltimer_ns() - t0 > s.wait_limit_ns) {

@@ -30,7 +30,14 @@ constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;         // 65536
 // operand stages per CTA: 2 (the next pair stages while this one's MMAs run,
 // 128 KB, one CTA per SM) or 1 (64 KB, two CTAs per SM)
 constexpr int MAX_STAGES = 2;
-constexpr uint32_t TMEM_COLS = 64;
+// raw FP32 operand pairs in flight (A and B tiles as copied from global by
+// the tensor-memory-access unit), ahead of the conversion into a stage: 3
+// with two stages (128 + 96 KB), 1 with one stage (64 + 32 KB)
+constexpr int RAW_BYTES = 2 * 64 * 64 * 4;
+constexpr int MAX_RAW = 3;
+template <int S>
+__host__ __device__ constexpr int raw_slots() { return S == 2 ? 3 : 1; }
+constexpr uint32_t TMEM_COLS = 128;  // D: 128 lanes x 128 FP32 columns
 
 // byte offset of element (row, k) in the K-major core-matrix layout:
 // 8-row groups at ROW_GROUP_BYTES, K-adjacent core matrices at 128 bytes
@@ -51,9 +58,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // instruction descriptor for kind::tf32: D f32, A/B tf32, K-major A and B,
-// N = 64 (bits 17-22 hold N >> 3), M = 128 (bits 24-28 hold M >> 4)
-__host__ __device__ constexpr uint32_t idesc_tf32_m128_n64() {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+// N = 128 (bits 17-22 hold N >> 3), M = 128 (bits 24-28 hold M >> 4)
+__host__ __device__ constexpr uint32_t idesc_tf32_m128_n128() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 // TF32 head of x, rounded to nearest (ties away from zero) on the magnitude
@@ -68,17 +75,22 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 
 // bounded wait for the mbarrier phase `parity` to complete; false on timeout
+// (the clock is read only once the first probe found the phase open)
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
+    if (mbar_try(bar, parity)) return true;
     unsigned long long t0;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
     for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
+        if (mbar_try(bar, parity)) return true;
         unsigned long long t;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
         if (t - t0 > limit_ns) return false;
@@ -135,37 +147,39 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // holds, per stage s, the parity of that stage's next mbarrier phase (bit s);
 // pending, per stage, whether a commit on it is not yet waited for.
 struct State {
-    uint64_t bar[MAX_STAGES];
+    uint64_t bar[MAX_STAGES];   // MMAs of a stage completed (the stage is free again)
+    uint64_t full[MAX_STAGES];  // every warp staged its share of a stage
+    uint64_t raw[MAX_RAW];      // copies into a raw slot landed
     uint32_t tmem;
     int32_t fail;
 };
 
+// ---- copies by the tensor-memory-access unit (TMA) into shared memory
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// contiguous copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// orders this thread's earlier (acquired) generic view of global memory
+// before its later copies by the async proxy
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
 // Thread -> chunk mapping: warp w owns the 8-row group 8w..8w+7; in chunk j,
 // lane l handles row 8w + (l & 7) and K-quad 4j + (l >> 3). Eight consecutive
-// lanes then fill one 128-byte core matrix (conflict-free 16-byte stores) and
-// the global reads cover whole sectors.
+// lanes then touch one 128-byte core matrix (conflict-free 16-byte accesses).
 __device__ __forceinline__ void chunk_of(int j, int& row, int& k) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     row = 8 * warp + (lane & 7);
     k = 4 * (4 * j + (lane >> 3));
-}
-
-// Load this thread's share of one pair from global (L2; produced by other
-// SMs): 4 chunks of A (4 consecutive k of one row) and of B^T (4 consecutive
-// k of one column of B).
-// B is the tile itself, or with trans the transpose of the tile at B (so the
-// K-major rows of the MMA's B operand are the tile's rows: one 16-byte load)
-__device__ __forceinline__ void load_pair(const float* A, const float* B, bool trans, float4 (&a4)[4],
-                                          float4 (&b4)[4]) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        int row, k;
-        chunk_of(j, row, k);
-        a4[j] = __ldcg(reinterpret_cast<const float4*>(A + row * 64 + k));
-        b4[j] = trans ? __ldcg(reinterpret_cast<const float4*>(B + row * 64 + k))
-                      : make_float4(__ldcg(B + (k + 0) * 64 + row), __ldcg(B + (k + 1) * 64 + row),
-                                    __ldcg(B + (k + 2) * 64 + row), __ldcg(B + (k + 3) * 64 + row));
-    }
 }
 
 __device__ __forceinline__ void split4(const float4& x, float sgn, float4& hi, float4& lo) {
@@ -175,35 +189,62 @@ __device__ __forceinline__ void split4(const float4& x, float sgn, float4& hi, f
     hi.w = tf32_head(sgn * x.w); lo.w = sgn * x.w - hi.w;
 }
 
-// Stage one pair into a stage buffer: A (x sgn) as [A_hi; A_lo], B as B_hi^T, B_lo^T.
-__device__ __forceinline__ void stage_pair(unsigned char* st, const float4 (&a4)[4], const float4 (&b4)[4],
-                                           float sgn) {
+// Stage one pair from a raw slot holding the row-major A and B tiles (two
+// 1-D copies): A (x sgn) becomes [A_hi; A_lo] in the K-major core-matrix
+// layout; B becomes B_hi^T, B_lo^T, either from the tile's rows (trans: they
+// are the K-major rows of the MMA's B operand) or transposed here. Every
+// shared-memory access is conflict-free. Row-major to core-matrix chunks use
+// a diagonal assignment: in each group of 8 lanes, lane e takes row 8w + e
+// and k-quad (e + c) mod 16, so the 8 lanes read 8 distinct bank quads of
+// the raw rows and write 8 distinct rows of one core matrix.
+__device__ __forceinline__ void stage_kmajor(unsigned char* hi_dst, unsigned char* lo_dst, const float* src,
+                                             float sgn) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, e = lane & 7, ph = lane >> 3;
+    const int row = 8 * warp + e;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        int row, k;
-        chunk_of(j, row, k);
+        const int k = 4 * ((e + 4 * ph + j) & 15);
         float4 hi, lo;
-        split4(a4[j], sgn, hi, lo);
-        *reinterpret_cast<float4*>(st + kmajor_off(row, k)) = hi;
-        *reinterpret_cast<float4*>(st + kmajor_off(64 + row, k)) = lo;
-        split4(b4[j], 1.f, hi, lo);
-        *reinterpret_cast<float4*>(st + A_BYTES + kmajor_off(row, k)) = hi;
-        *reinterpret_cast<float4*>(st + A_BYTES + B_BYTES + kmajor_off(row, k)) = lo;
+        split4(*reinterpret_cast<const float4*>(src + row * 64 + k), sgn, hi, lo);
+        *reinterpret_cast<float4*>(hi_dst + kmajor_off(row, k)) = hi;
+        *reinterpret_cast<float4*>(lo_dst + kmajor_off(row, k)) = lo;
+    }
+}
+__device__ __forceinline__ void stage_from_raw(unsigned char* st, const unsigned char* raw, bool trans, float sgn) {
+    const float* A = reinterpret_cast<const float*>(raw);
+    const float* B = reinterpret_cast<const float*>(raw + RAW_BYTES / 2);
+    stage_kmajor(st, st + A_BYTES / 2, A, sgn);
+    if (trans) {
+        stage_kmajor(st + A_BYTES, st + A_BYTES + B_BYTES, B, 1.f);
+    } else {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int n = 32 * (warp & 1) + lane;
+        float4 hi, lo;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int k = 4 * (4 * (warp >> 1) + j);
+            const float4 x = make_float4(B[(k + 0) * 64 + n], B[(k + 1) * 64 + n], B[(k + 2) * 64 + n],
+                                         B[(k + 3) * 64 + n]);
+            split4(x, 1.f, hi, lo);
+            *reinterpret_cast<float4*>(st + A_BYTES + kmajor_off(n, k)) = hi;
+            *reinterpret_cast<float4*>(st + A_BYTES + B_BYTES + kmajor_off(n, k)) = lo;
+        }
     }
 }
 
-// Issue the 16 MMAs of one staged pair (8 K-steps x 2).
+// Issue the 8 MMAs of one staged pair (K = 64 in steps of 8): one M = 128,
+// N = 128 product [A_hi; A_lo] x [B_hi^T; B_lo^T]^T per step (the B halves
+// are adjacent 8-row groups of one K-major operand), so D holds the four
+// products hi.hi | hi.lo over lo.hi | lo.lo.
 __device__ __forceinline__ void issue_pair(const unsigned char* st, uint32_t tmem, bool first) {
     const uint32_t base = smem_u32(st);
-    constexpr uint32_t idesc = idesc_tf32_m128_n64();
+    constexpr uint32_t idesc = idesc_tf32_m128_n128();
 #pragma unroll
     for (int ks = 0; ks < 8; ks++) {
         const uint32_t koff = ks * 256;  // K = 8 tf32 = two core matrices of 128 bytes
         const uint64_t a = smem_desc(base + koff, 128, ROW_GROUP_BYTES);
-        const uint64_t bh = smem_desc(base + A_BYTES + koff, 128, ROW_GROUP_BYTES);
-        const uint64_t bl = smem_desc(base + A_BYTES + B_BYTES + koff, 128, ROW_GROUP_BYTES);
-        mma_tf32(tmem, a, bh, idesc, (first && ks == 0) ? 0u : 1u);
-        mma_tf32(tmem, a, bl, idesc, 1u);
+        const uint64_t b = smem_desc(base + A_BYTES + koff, 128, ROW_GROUP_BYTES);
+        mma_tf32(tmem, a, b, idesc, (first && ks == 0) ? 0u : 1u);
     }
 }
 
