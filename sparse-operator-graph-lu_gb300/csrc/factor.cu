@@ -341,6 +341,177 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
     }
 }
 
+// FP32 variant of the same elimination with column pairs: thread (r, q) owns
+// columns 8m + 2q and 8m + 2q + 1 (m = 0..7) of row r, so the rank-1 update
+// and the inverse updates run as paired FMAs (__ffma2_rn, two independent
+// round-to-nearest FMAs: bit-identical to the scalar form) on 8-byte shared
+// loads; only the pair holding column k needs per-element selection. Half the
+// instructions per step of the stride-4 layout above, which the FP64 path keeps
+// (there is no paired FP64 FMA).
+template <bool CHOL>
+__device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm) {
+    float* rowbuf = sm;     // [2][64] published rows
+    float* piv = sm + 128;  // [64]
+    float* rpiv = piv + 64;
+    float* raw = piv + 128;
+    __shared__ float s_maxa, s_maxu;
+    const int tid = threadIdx.x, lane = tid & 31, r = tid >> 2, q = tid & 3;
+    if (tid == 0) { s_maxa = 0.f; s_maxu = 0.f; }
+    const float* A = tiles + (size_t)tk.a[task] * 4096;
+    float2 a2[8], y2[8];
+    float ma = 0.f;
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        const int c0 = 8 * m + 2 * q;
+        if (CHOL) {
+            a2[m].x = c0 > r ? __ldcg(A + c0 * 64 + r) : __ldcg(A + r * 64 + c0);
+            a2[m].y = c0 + 1 > r ? __ldcg(A + (c0 + 1) * 64 + r) : __ldcg(A + r * 64 + c0 + 1);
+        } else {
+            a2[m] = __ldcg(reinterpret_cast<const float2*>(A + r * 64 + c0));
+        }
+        ma = fmaxf(ma, fmaxf(fabsf(a2[m].x), fabsf(a2[m].y)));
+        y2[m] = make_float2(c0 == r ? 1.f : 0.f, c0 + 1 == r ? 1.f : 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 64; k++) {
+        const int km = k >> 3, kq = (k >> 1) & 3, kb = k & 1;
+        float2* P2 = reinterpret_cast<float2*>(rowbuf + (k & 1) * 64);
+        const int src = (lane & ~3) | kq;
+        const float aik = __shfl_sync(FULL, kb ? a2[km].y : a2[km].x, src);
+        const float xrk = CHOL ? 0.f : __shfl_sync(FULL, kb ? y2[km].y : y2[km].x, src);
+        // columns of pair km right of the pivot: c0 > k, c1 > k
+        const bool g0 = q > kq, g1 = q > kq || (q == kq && kb == 0);
+        if (r == k) {
+            const float tiny = 1e-9f;
+            const float p = CHOL ? (aik < 1e-20f ? 1e-20f : aik)
+                                 : ((aik < tiny && aik > -tiny) ? (aik < 0.f ? -tiny : tiny) : aik);
+            const float rp = __frcp_rn(p);
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                float2 o;
+                if (m > km) o = make_float2(a2[m].x * rp, a2[m].y * rp);
+                else if (m < km) o = y2[m];
+                else o = make_float2(g0 ? a2[m].x * rp : y2[m].x, g1 ? a2[m].y * rp : y2[m].y);
+                P2[4 * m + q] = o;
+            }
+            if (q == 0) { piv[k] = p; rpiv[k] = rp; raw[k] = aik; }
+        }
+        __syncthreads();
+        if (r > k) {
+            const float lik = aik * rpiv[k];
+            const float2 na = make_float2(-aik, -aik), nl = make_float2(-lik, -lik);
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const float2 v = P2[4 * m + q];
+                if (m > km) a2[m] = __ffma2_rn(na, v, a2[m]);
+                else if (m < km) y2[m] = __ffma2_rn(nl, v, y2[m]);
+                else {
+                    if (g0) a2[m].x = fmaf(-aik, v.x, a2[m].x); else y2[m].x = fmaf(-lik, v.x, y2[m].x);
+                    if (g1) a2[m].y = fmaf(-aik, v.y, a2[m].y); else y2[m].y = fmaf(-lik, v.y, y2[m].y);
+                }
+            }
+            if (q == kq) { if (kb) a2[km].y = lik; else a2[km].x = lik; }
+        } else if (!CHOL) {
+            const float2 nx = make_float2(-xrk, -xrk);
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                if (m > km) y2[m] = __ffma2_rn(nx, P2[4 * m + q], y2[m]);
+                else if (m == km) {
+                    const float2 v = P2[4 * m + q];
+                    if (g0) y2[m].x = fmaf(-xrk, v.x, y2[m].x);
+                    if (g1) y2[m].y = fmaf(-xrk, v.y, y2[m].y);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    float* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + 2 * q;
+    const int32_t linv = tk.b[task];
+    float mu = 0.f;
+    if (CHOL) {
+        float* sq = rowbuf;
+        if (tid < 64) sq[tid] = sqrtf(piv[tid]);
+        __syncthreads();
+        const float sr = sq[r];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const int c0 = 8 * m + 2 * q, c1 = c0 + 1;
+            const float2 v = make_float2(r > c0 ? a2[m].x * sq[c0] : (r == c0 ? sr : 0.f),
+                                         r > c1 ? a2[m].y * sq[c1] : (r == c1 ? sr : 0.f));
+            *reinterpret_cast<float2*>(L + 8 * m) = v;
+            mu = fmaxf(mu, fmaxf(fabsf(v.x), fabsf(v.y)));
+        }
+        if (linv > 0) {
+            float* W = tiles + (size_t)linv * 4096 + r * 64 + 2 * q;
+            const float isr = 1.f / sr;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int c0 = 8 * m + 2 * q;
+                *reinterpret_cast<float2*>(W + 8 * m) =
+                    make_float2(c0 <= r ? y2[m].x * isr : 0.f, c0 + 1 <= r ? y2[m].y * isr : 0.f);
+            }
+        }
+    } else {
+        float* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + 2 * q;
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const int c0 = 8 * m + 2 * q, c1 = c0 + 1;
+            *reinterpret_cast<float2*>(L + 8 * m) = make_float2(r > c0 ? a2[m].x : (r == c0 ? 1.f : 0.f),
+                                                                r > c1 ? a2[m].y : (r == c1 ? 1.f : 0.f));
+            const float2 u = make_float2(r < c0 ? a2[m].x : (r == c0 ? piv[r] : 0.f),
+                                         r < c1 ? a2[m].y : (r == c1 ? piv[r] : 0.f));
+            *reinterpret_cast<float2*>(U + 8 * m) = u;
+            mu = fmaxf(mu, fmaxf(fabsf(u.x), fabsf(u.y)));
+        }
+        if (linv > 0) {
+            float* W = tiles + (size_t)linv * 4096 + r * 64 + 2 * q;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int c0 = 8 * m + 2 * q;
+                *reinterpret_cast<float2*>(W + 8 * m) = make_float2(c0 <= r ? y2[m].x : 0.f, c0 + 1 <= r ? y2[m].y : 0.f);
+            }
+        }
+        const int32_t uinv = tk.c[task];
+        if (uinv > 0) {
+            float* V = tiles + (size_t)uinv * 4096 + r * 64 + 2 * q;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int c0 = 8 * m + 2 * q, c1 = c0 + 1;
+                *reinterpret_cast<float2*>(V + 8 * m) =
+                    make_float2(c0 >= r ? y2[m].x * rpiv[c0] : 0.f, c1 >= r ? y2[m].y * rpiv[c1] : 0.f);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(FULL, ma, o));
+        mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
+    }
+    if (lane == 0) {
+        atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
+        atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
+    }
+    __syncthreads();
+    if (tid < 32) {
+        double mn = 1e300;
+        int cl = 0;
+        for (int k = lane; k < 64; k += 32) {
+            const double v = fabs((double)raw[k]);
+            mn = fmin(mn, v);
+            cl += CHOL ? (double)raw[k] < 1e-20 : v < 1e-9;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
+            cl += __shfl_xor_sync(FULL, cl, o);
+        }
+        if (lane == 0) {
+            if (cl) atomicAdd(&tk.status->clamped, cl);
+            atomicMin(&tk.status->min_pivot_bits, dbits(mn));
+            if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
+        }
+    }
+}
+
 // ---------------------------------------------------------------- triangular inverses
 // Y = L^-1 by forward elimination on the identity, Y = U^-1 by backward
 // elimination, the working rows held in registers (thread t owns row t>>2,
@@ -573,8 +744,14 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                 gemm_f32_tc<S>(tk, tiles, task, sm, st, phase);
             }
             break;
-        case K_LU: lu_task<T, false>(tk, tiles, task, sm); break;
-        case K_LLT: lu_task<T, true>(tk, tiles, task, sm); break;
+        case K_LU:
+            if constexpr (sizeof(T) == 4) lu_task_f2<false>(tk, tiles, task, sm);
+            else lu_task<T, false>(tk, tiles, task, sm);
+            break;
+        case K_LLT:
+            if constexpr (sizeof(T) == 4) lu_task_f2<true>(tk, tiles, task, sm);
+            else lu_task<T, true>(tk, tiles, task, sm);
+            break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;
         case K_UINV: inv_task<T, false>(tk, tiles, task, sm); break;
         case K_SUB: sub_task<T>(tk, tiles, task); break;
