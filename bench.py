@@ -450,6 +450,9 @@ def run_ours(args):
                       pipeline_stages=args.stages)
     rm = timed(mixed, args.steps, args.warmup)
     grid_mixed = mixed.task_info()["grid"]
+    ex = mixed.executor_config()
+    chosen = (["persistent, static order", "per level", "persistent, ready queue"][ex["executor"]]
+              + (", early products" if ex["early_products"] else "") + f", {ex['stages']} operand stages")
     x_mixed = x.cpu().numpy()
     re2e = timed(mixed, args.steps, args.warmup, host=True)
     x_e2e = hx.numpy().copy()
@@ -523,7 +526,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (FP32 tiles {info.storage_count * 16384 / 1e9:.2f} GB)",
                        "executor": ["persistent, static order", "per level", "persistent, ready queue",
-                                    "autotuned"][args.executor],
+                                    "autotuned"][args.executor] + f" ({chosen})",
                        "factor_ctas": grid_mixed, "pipeline_stages": args.stages or "tuned"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),

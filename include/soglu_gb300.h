@@ -227,6 +227,10 @@ int sog_plan_task_graph_info(const sog_plan *plan, int32_t gemm_split, int64_t *
  * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid,
  * kernel launches issued by this system so far}. */
 int sog_system_task_info(const sog_system *sys, int64_t *counts);
+/* Executor configuration in use (after autotuning, the chosen one):
+ * SOG_EXEC_*, tensor-core operand stages (mixed), and whether products start
+ * before their last producer finished (mixed, static order: 1). */
+int sog_system_executor(const sog_system *sys, int32_t *executor, int32_t *stages, int32_t *early);
 
 /* ---- profiling (no reference counterpart: the reference prints phase
  * timers only, solver.cpp:53-118) ---------------------------------------------

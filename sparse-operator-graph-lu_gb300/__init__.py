@@ -82,7 +82,7 @@ EXPORTS = [
     "sog_plan_import", "sog_plan_destroy", "sog_ctx_create", "sog_ctx_destroy", "sog_ctx_pool_usage", "sog_ctx_stream",
     "sog_system_create", "sog_system_bytes", "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve",
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
-    "sog_system_destroy", "sog_system_task_info", "sog_system_set_wait_limit", "sog_debug_poison_task",
+    "sog_system_destroy", "sog_system_task_info", "sog_system_executor", "sog_system_set_wait_limit", "sog_debug_poison_task",
     "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
     "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
@@ -115,7 +115,7 @@ def lib() -> C.CDLL:
         "sog_solve": ([P, I32, P, P, P], I32), "sog_solve_device": ([P, I32, P, P, P], I32),
         "sog_solve_permuted": ([P, P, P], I32), "sog_system_export_factors": ([P, P, P], I32),
         "sog_system_last_times": ([P, P, P], I32), "sog_system_destroy": ([P], None),
-        "sog_system_task_info": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
+        "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
         "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
@@ -378,6 +378,12 @@ class System:
         _check(lib().sog_system_task_info(self._h, _p(c)))
         keys = ["tasks", "levels", "items", "pairs", "gemm", "lu", "linv", "uinv", "sub", "grid", "launches"]
         return dict(zip(keys, (int(v) for v in c)))
+
+    def executor_config(self) -> dict:
+        """Executor in use (the autotuner's pick once the first factor ran)."""
+        e, st, ea = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().sog_system_executor(self._h, C.byref(e), C.byref(st), C.byref(ea)))
+        return {"executor": e.value, "stages": st.value, "early_products": bool(ea.value)}
 
     def trace_enable(self, on: bool = True) -> None:
         _check(lib().sog_system_trace_enable(self._h, int(on)))

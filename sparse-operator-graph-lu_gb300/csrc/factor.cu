@@ -589,19 +589,28 @@ __device__ void trans_task(const DevTasks& tk, T* __restrict__ tiles, int task, 
 
 // C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh).
 // Thread 0 keeps up to R operand pairs in flight: the TMA copies the raw FP32
-// tiles (contiguous 16 KB each) into a ring of R slots (mbarrier completion). Every warp splits its
-// share of the oldest slot into a stage of [A_hi; A_lo], B_hi^T, B_lo^T and
-// signals the stage's `full` barrier; thread 0 then issues that stage's MMAs
-// and refills the slot, while the other warps already stage the next pair
-// (no CTA barrier per pair). Only the first pair's copy latency is exposed.
-// `phase` holds this CTA's mbarrier parities (stages free: bits 0-1, stages
-// full: bits 16-17, thread 0 only; raw slots: bits 8-10), carried across tasks.
-constexpr int PAIRS_SMEM = 128;  // operand pair ids staged in shared memory per task
+// tiles (contiguous 16 KB each) into a ring of R slots (mbarrier completion).
+// Every warp splits its share of the oldest slot into a stage of
+// [A_hi; A_lo], B_hi^T, B_lo^T and signals the stage's `full` barrier; thread
+// 0 then issues that stage's MMAs and refills the slot, while the other warps
+// already stage the next pair (no CTA barrier per pair). Only the first pair's
+// copy latency is exposed. `phase` holds this CTA's mbarrier parities (stages
+// free: bits 0-1, stages full: bits 16-17, thread 0 only; raw slots: bits
+// 8-10), carried across tasks.
+//
+// early: the task was claimed before its last producer finished (the ordered
+// executor, mixed path). Pairs are ordered by the estimated finish of their
+// producers; thread 0 waits, bounded, for a pair's two producers just before
+// copying it, so the ready pairs accumulate while the late one is computed
+// elsewhere. Warp 0 checks the first 32 pairs' producers at once up front.
+constexpr int PAIRS_SMEM = 64;  // operand pairs listed in shared memory per task
 template <int S>
 __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm, tc::State& st,
-                            uint32_t& phase) {
+                            uint32_t& phase, bool early) {
     constexpr int R = tc::raw_slots<S>();
-    __shared__ int32_t s_pa[PAIRS_SMEM], s_pb[PAIRS_SMEM];
+    __shared__ int32_t s_pa[PAIRS_SMEM], s_pb[PAIRS_SMEM], s_wa[PAIRS_SMEM], s_wb[PAIRS_SMEM];
+    __shared__ unsigned s_ready;  // pairs 0..31 whose producers had finished at the start
+    __shared__ int s_init_ready;
     unsigned char* smb = reinterpret_cast<unsigned char*>(sm);
     unsigned char* raw = smb + S * tc::STAGE_BYTES;
     raw += (128u - (tc::smem_u32(raw) & 127u)) & 127u;
@@ -612,20 +621,63 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
     for (int j = tid; j < n && j < PAIRS_SMEM; j += NT) {
         s_pa[j] = tk.pair_a[p0 + j];
         s_pb[j] = tk.pair_b[p0 + j];
+        if (early) {
+            s_wa[j] = tk.pair_wa[p0 + j];
+            s_wb[j] = tk.pair_wb[p0 + j];
+        }
     }
     auto pair_a = [&](int i) { return i < PAIRS_SMEM ? s_pa[i] : tk.pair_a[p0 + i]; };
     auto pair_b = [&](int i) { return i < PAIRS_SMEM ? s_pb[i] : tk.pair_b[p0 + i]; };
-    // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
-    // under the operand copies and the MMAs
-    const int quad = warp & 3, colh = (warp >> 2) * 32, init = tk.a[task];
-    float4 u[8];
-    if (quad < 2 && init > 0) {
-        const float4* I = reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + (32 * quad + lane) * 64 + colh);
-#pragma unroll
-        for (int i = 0; i < 8; i++) u[i] = __ldcg(I + i);
+    const int init = tk.a[task];
+    if (early && warp == 0) {
+        bool ok = true;
+        if (lane < n) {
+            const int wa = tk.pair_wa[p0 + lane], wb = tk.pair_wb[p0 + lane];
+            ok = (wa < 0 || ld_acquire(tk.task_done + wa) != 0) && (wb < 0 || ld_acquire(tk.task_done + wb) != 0);
+        }
+        const unsigned m = __ballot_sync(FULL, ok);
+        if (lane == 0) {
+            s_ready = m;
+            const int wi = init > 0 ? tk.init_w[task] : -1;
+            s_init_ready = wi < 0 || ld_acquire(tk.task_done + wi) != 0;
+        }
     }
     __syncthreads();
+    // wait (thread 0, bounded) until tasks ta and tb (-1: none) finished;
+    // false on timeout. Both flags are read at once on every probe.
+    auto wait_done = [&](int ta, int tb) -> bool {
+        bool da = ta < 0, db = tb < 0;
+        unsigned long long t0 = 0;
+        for (unsigned spins = 0;; spins++) {
+            const int va = da ? 1 : ld_acquire(tk.task_done + ta), vb = db ? 1 : ld_acquire(tk.task_done + tb);
+            da = da || va != 0;
+            db = db || vb != 0;
+            if (da && db) return true;
+            if (spins == 0) t0 = globaltimer_ns();
+            else if (globaltimer_ns() - t0 > lim) return false;
+        }
+    };
+    // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
+    // under the operand copies and the MMAs (or after its producer, if late)
+    const int quad = warp & 3, colh = (warp >> 2) * 32;
+    const bool init_now = !early || s_init_ready;
+    float4 u[8];
+    auto load_init = [&]() {
+        if (quad < 2 && init > 0) {
+            const float4* I =
+                reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + (32 * quad + lane) * 64 + colh);
+#pragma unroll
+            for (int i = 0; i < 8; i++) u[i] = __ldcg(I + i);
+        }
+    };
+    if (init_now) load_init();
     auto fetch = [&](int i) {  // thread 0: copies of pair p0 + i into raw slot i % R
+        if (early && !(i < 32 && ((s_ready >> i) & 1u))) {
+            const int wa = i < PAIRS_SMEM ? s_wa[i] : tk.pair_wa[p0 + i];
+            const int wb = i < PAIRS_SMEM ? s_wb[i] : tk.pair_wb[p0 + i];
+            if (!wait_done(wa, wb)) st.fail = 1;
+            tc::fence_proxy_async_global();
+        }
         const int slot = i % R, pbs = pair_b(i), pb = pbs < 0 ? -pbs : pbs, b = pb & ~PAIR_TRANS;
         unsigned char* dst = raw + slot * tc::RAW_BYTES;
         tc::expect_tx(&st.raw[slot], tc::RAW_BYTES);
@@ -660,6 +712,7 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
             if (i + R < n) fetch(i + R);  // every warp has staged from this slot (full barrier)
         }
     }
+    if (early && tid == 0 && !init_now && !wait_done(tk.init_w[task], -1)) st.fail = 1;  // a late initial tile
     for (int i = n > S ? n - S : 0; i < n; i++) {  // the commits not yet waited for
         const int s = i % S;
         if (!tc::mbar_wait(&st.bar[s], (phase >> s) & 1u, lim)) st.fail = 1;
@@ -680,7 +733,8 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
 #pragma unroll
         for (int i = 0; i < 32; i++) X[row * 65 + colh + i] = v[i] + w[i];
     }
-    __syncthreads();
+    __syncthreads();  // also orders thread 0's acquire of a late initial tile before its loads
+    if (!init_now) load_init();
     if (quad < 2) {
         const int row = 32 * quad + lane;
         if (p0 < p1) {
@@ -727,7 +781,7 @@ __device__ __forceinline__ void tc_teardown(tc::State& st, const DevTasks& tk) {
 }
 
 template <typename T, int S>
-__device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task, int part, T* sm, tc::State& st,
+__device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task, int part, bool early, T* sm, tc::State& st,
                                          uint32_t& phase) {
     switch (tk.kind[task]) {
         case K_GEMM:
@@ -741,7 +795,7 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
                     }
                 }
             } else {
-                gemm_f32_tc<S>(tk, tiles, task, sm, st, phase);
+                gemm_f32_tc<S>(tk, tiles, task, sm, st, phase, early);
             }
             break;
         case K_LU:
@@ -760,6 +814,9 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
     }
 }
 
+__device__ __forceinline__ void st_relaxed(int* p, int v) {
+    asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ void st_release(int* p, int v) {
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -907,7 +964,7 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+        run_item<T, S>(tk, tiles, item >> 4, item & 7, false, sm, st, phase);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
@@ -937,9 +994,13 @@ __device__ void release_item(const DevTasks& tk, int task) {
         last = __shfl_sync(FULL, last, 0);
         if (last) __threadfence();  // the other parts' writes, acquired above, released with ours
     }
-    if (last)
+    if (last) {
+        // completion flag for products started early (ordered after the
+        // CTA's writes by the fence above), then the successors' counts
+        if (lane == 0 && tk.early) st_relaxed(tk.task_done + task, 1);
         for (int k = tk.succ_ptr[task] + lane; k < tk.succ_ptr[task + 1]; k += 32)
             red_release_add(&tk.dep[tk.succ[k]], -1);
+    }
 }
 
 // Static list scheduling. Every CTA claims the next position of a fixed item
@@ -970,7 +1031,9 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
                 } else {
                     unsigned long long t0 = 0;
                     unsigned spins = 0;
-                    while (ld_acquire(tk.dep + task) > 0) {
+                    // a product started early waits per operand pair instead
+                    const bool early = sizeof(T) == 4 && tk.early && (item & ITEM_EARLY) != 0;
+                    while (!early && ld_acquire(tk.dep + task) > 0) {
                         if (spins == 0) t0 = globaltimer_ns();  // the clock only once waiting
                         if ((++spins & 15) == 0) {
                             if (ld_acquire(&tk.status->flags) & (ST_TIMEOUT | ST_BAD_ITEM)) { item = -1; break; }
@@ -999,7 +1062,7 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
         __syncthreads();
         const int item = s_item;
         if (item < 0) break;
-        run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+        run_item<T, S>(tk, tiles, item >> 4, item & 7, tk.early && (item & ITEM_EARLY) != 0, sm, st, phase);
         __syncthreads();
         if (threadIdx.x < 32) {
             if (tk.trace && threadIdx.x == 0) atomicMax(tk.trace + 4 * (size_t)(item >> 4) + 2, globaltimer_ns());
@@ -1017,7 +1080,7 @@ __global__ void __launch_bounds__(NT) factor_level_kernel(const __grid_constant_
     uint32_t phase = 0;
     if constexpr (sizeof(T) == 4) tc_setup(st);
     const int item = items[blockIdx.x];
-    run_item<T, S>(tk, tiles, item >> 4, item & 15, sm, st, phase);
+    run_item<T, S>(tk, tiles, item >> 4, item & 7, false, sm, st, phase);
     if constexpr (sizeof(T) == 4) tc_teardown(st, tk);
 }
 

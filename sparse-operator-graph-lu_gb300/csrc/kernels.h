@@ -41,13 +41,23 @@ struct DevTasks {
     int32_t* tail;        // next slot to fill
     int32_t* done;        // completed items
     // static claim order of items (the ordered executor): estimated start
-    // time, then longest remaining path
+    // time, then longest remaining path; ITEM_EARLY marks a product that may
+    // start before its last producer finished
     const int32_t* order;
+    // early start (mixed path, ordered executor): producer task of each
+    // pair's A and B tile and of each product's initial tile (-1: none), and
+    // per-task completion flags (set after the task's writes are released)
+    int32_t early;
+    const int32_t *pair_wa, *pair_wb, *init_w;
+    int32_t* task_done;
     DevStatus* status;
     unsigned long long wait_limit_ns;  // bound on any single queue wait
     // optional per-task trace (4 x u64 per task: ready, start, end, sm id), NULL = off
     unsigned long long* trace;
 };
+
+// item = task << 4 | part (parts < 8) | ITEM_EARLY
+constexpr int32_t ITEM_EARLY = 8;
 
 // ---- factor (factor.cu) ----
 // tiles: block id -> tiles + id*4096 elements. double => SOG_FP64, float => SOG_MIXED.

@@ -152,6 +152,8 @@ struct sog_system {
     // device views
     DevTasks dt{};
     int32_t *d_ndep0 = nullptr, *d_parts0 = nullptr, *d_ready0 = nullptr, *d_counters0 = nullptr;
+    bool early = false;     // mixed path, static order: products start before their last producer
+    bool poisoned = false;  // a dependency count raised by the test hook (early start off)
     int32_t* d_level_items = nullptr;
     int nready = 0;
     DevStatus* d_status0 = nullptr;
@@ -198,6 +200,7 @@ namespace {
 // dependency level) behave alike.
 struct Tuned {
     int executor, stages;
+    bool early;  // static order: products may start before their last producer
 };
 std::mutex g_tune_mu;
 std::map<uint64_t, Tuned> g_tuned;
@@ -363,6 +366,7 @@ int run_factor_once(sog_system* s) {
         CK(cudaMemcpyAsync(s->dt.queue, s->d_ready0, sizeof(int32_t) * s->nready, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.head, s->d_counters0, sizeof(int32_t) * 3, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.status, s->d_status0, sizeof(DevStatus), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemsetAsync(s->dt.task_done, 0, sizeof(int32_t) * g.ntasks, st));
     (void)fs;
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(unsigned long long) * 4 * g.ntasks, st));
     CK(cudaEventRecord(c->e0, st));
@@ -401,15 +405,19 @@ int run_factor_once(sog_system* s) {
 int run_factor(sog_system* s) {
     if (!s->tune_pending) return run_factor_once(s);
     s->tune_pending = false;
-    std::vector<Tuned> cands = {{SOG_EXEC_PERSISTENT, 2}, {SOG_EXEC_QUEUE, 2}};
+    std::vector<Tuned> cands = {{SOG_EXEC_PERSISTENT, 2, true}, {SOG_EXEC_QUEUE, 2, false}};
     const int sms = s->ctx->num_sms;
-    if (!s->fp64 && factor_persistent_grid(false, 1, sms) > factor_persistent_grid(false, 2, sms))
-        cands.push_back({SOG_EXEC_PERSISTENT, 1});
+    if (!s->fp64) {
+        cands.push_back({SOG_EXEC_PERSISTENT, 2, false});
+        if (factor_persistent_grid(false, 1, sms) > factor_persistent_grid(false, 2, sms))
+            cands.push_back({SOG_EXEC_PERSISTENT, 1, false});
+    }
     float best = 1e30f;
     Tuned pick = cands[0];
     for (const Tuned& c : cands) {
         s->opt.executor = c.executor;
         s->stages = c.stages;
+        s->dt.early = !s->fp64 && c.early && !s->poisoned;
         s->grid_factor = factor_persistent_grid(s->fp64, c.stages, sms);
         for (int rep = 0; rep < 2; rep++) {
             const int r = run_factor_once(s);
@@ -423,6 +431,8 @@ int run_factor(sog_system* s) {
     remember_config(tune_key(s->tg, s->fp64), pick);
     s->opt.executor = pick.executor;
     s->stages = pick.stages;
+    s->early = pick.early;
+    s->dt.early = !s->fp64 && pick.early && !s->poisoned;
     s->grid_factor = factor_persistent_grid(s->fp64, pick.stages, sms);
     return run_factor_once(s);
 }
@@ -780,6 +790,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (int32_t id : ula) if (id > 0) outputs.push_back(id);
     try {
         s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts);
+        if (!s->fp64) order_pairs_by_ready(s->tg, false);
     } catch (const std::exception& e) {
         delete s;
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
@@ -814,7 +825,26 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (const Leaf& lf : loff) { lptr[lf.bi + 1]++; lcol.push_back(lf.bj); lid.push_back(lf.id); }
     for (const Leaf& lf : uoff) { uptr[lf.bi + 1]++; ucol.push_back(lf.bj); uid.push_back(lf.id); }
     for (int i = 0; i < s->R; i++) { lptr[i + 1] += lptr[i]; uptr[i + 1] += uptr[i]; }
-    const std::vector<int32_t> order = static_order(g, s->fp64);
+    std::vector<int32_t> order = static_order(g, s->fp64);
+    // mixed path: the ordered executor starts a product before its last
+    // producer finished (item bit 3), waiting per operand pair; every pair
+    // lists the tasks producing its two tiles, every product the one
+    // producing its initial tile (-1: an input, nothing to wait for)
+    std::vector<int32_t> pair_wa, pair_wb, init_w;
+    if (!s->fp64) {
+        for (int32_t& it : order)  // one pair has nothing to overlap with
+            if (g.kind[it >> 4] == K_GEMM && g.pair_ptr[(it >> 4) + 1] - g.pair_ptr[it >> 4] > 1) it |= ITEM_EARLY;
+        pair_wa.resize(g.pair_a.size());
+        pair_wb.resize(g.pair_b.size());
+        for (size_t q = 0; q < g.pair_a.size(); q++) {
+            const int32_t b = (g.pair_b[q] < 0 ? -g.pair_b[q] : g.pair_b[q]) & ~PAIR_TRANS;
+            pair_wa[q] = g.pair_a[q] > p.n_input ? g.producer[g.pair_a[q]] : -1;
+            pair_wb[q] = b > p.n_input ? g.producer[b] : -1;
+        }
+        init_w.assign(g.ntasks, -1);
+        for (int32_t t = 0; t < g.ntasks; t++)
+            if (g.kind[t] == K_GEMM && g.a[t] > p.n_input) init_w[t] = g.producer[g.a[t]];
+    }
     HostCSR hc;
     if (!plan->imported) hc = build_csr(p);
     // systems: a plain plan is one system over all block rows
@@ -882,7 +912,9 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()),
-             o_order = L.add<int32_t>(order.size()),
+             o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
+             o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
+             o_done = L.add<int32_t>(g.ntasks),
              o_V = L.add<double>(s->nval), o_vidx = L.add<int32_t>(p.mirror_src.size());
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
@@ -928,6 +960,12 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.done = dt.head + 2;
     s->d_level_items = put(A, o_levels, g.level_items, st);
     dt.order = put(A, o_order, order, st);
+    dt.early = !s->fp64;  // the tuner may turn it off
+    s->early = dt.early;
+    dt.pair_wa = pair_wa.empty() ? nullptr : put(A, o_pwa, pair_wa, st);
+    dt.pair_wb = pair_wb.empty() ? nullptr : put(A, o_pwb, pair_wb, st);
+    dt.init_w = init_w.empty() ? nullptr : put(A, o_initw, init_w, st);
+    dt.task_done = reinterpret_cast<int32_t*>(A + o_done);
     s->d_status0 = put(A, o_st0, st0, st);
     dt.status = reinterpret_cast<DevStatus*>(A + o_st);
     dt.wait_limit_ns = 10ull * 1000 * 1000 * 1000;
@@ -983,6 +1021,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         if (tuned_config(tune_key(g, s->fp64), known)) {
             s->opt.executor = known.executor;
             s->stages = known.stages;
+            s->early = known.early;
+            dt.early = !s->fp64 && known.early;
         } else {
             s->opt.executor = SOG_EXEC_PERSISTENT;
             s->tune_pending = true;
@@ -1171,6 +1211,8 @@ int sog_debug_poison_task(sog_system* s, int32_t task) {
     CK(cudaSetDevice(s->ctx->device));
     int32_t v = s->tg.ndep[task] + 1;
     CK(cudaMemcpy(s->d_ndep0 + task, &v, sizeof(v), cudaMemcpyHostToDevice));
+    s->poisoned = true;  // every task then waits for its whole dependency count
+    s->dt.early = 0;
     return SOG_OK;
 }
 
@@ -1178,6 +1220,8 @@ int sog_debug_unpoison(sog_system* s) {
     if (!s) return fail(SOG_EINVAL, "bad argument");
     CK(cudaSetDevice(s->ctx->device));
     CK(cudaMemcpy(s->d_ndep0, s->tg.ndep.data(), sizeof(int32_t) * s->tg.ntasks, cudaMemcpyHostToDevice));
+    s->poisoned = false;
+    s->dt.early = !s->fp64 && s->early;
     return SOG_OK;
 }
 
@@ -1253,6 +1297,14 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
     } catch (const std::exception& e) {
         return fail(SOG_EINVAL, std::string("DAG: ") + e.what());
     }
+    return SOG_OK;
+}
+
+int sog_system_executor(const sog_system* s, int32_t* executor, int32_t* stages, int32_t* early) {
+    if (!s || !executor || !stages || !early) return fail(SOG_EINVAL, "bad argument");
+    *executor = s->opt.executor;
+    *stages = s->fp64 ? 0 : s->stages;
+    *early = s->dt.early && s->opt.executor == SOG_EXEC_PERSISTENT ? 1 : 0;
     return SOG_OK;
 }
 

@@ -209,6 +209,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     }
     for (int32_t b = 0; b < storage_count; b++)
         if (producer[b] >= 0) producer[b] = newid[producer[b]];
+    g.producer = producer;  // copied: the dependency pass below still reads it
     g.gemm_pairs = (int64_t)g.pair_a.size();
     // dependencies from each task's sources
     std::vector<std::vector<int32_t>> preds(g.ntasks);
@@ -325,28 +326,36 @@ void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const s
     std::sort(U.begin(), U.end(), [](const Leaf& a, const Leaf& b) { return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj; });
 }
 
-std::vector<int32_t> static_order(const TaskGraph& g, bool fp64) {
-    // single-CTA task latencies on GB300 (us), enough to rank start times
-    auto cost = [&](int32_t t) -> double {
-        const int np = g.pair_ptr[t + 1] - g.pair_ptr[t];
-        switch (g.kind[t]) {
-            case K_GEMM: return fp64 ? 5.0 + 20.0 * np / g.parts[t] : 1.5 + 2.0 * np;
-            case K_LU:
-            case K_LLT: return fp64 ? 140.0 : 24.0;
-            case K_LINV:
-            case K_UINV: return fp64 ? 95.0 : 14.0;
-            default: return fp64 ? 6.0 : 3.0;
-        }
-    };
-    const double hop = 2.0;
+// single-CTA task latencies on GB300 (us), enough to rank start times
+static double task_cost(const TaskGraph& g, int32_t t, bool fp64) {
+    const int np = g.pair_ptr[t + 1] - g.pair_ptr[t];
+    switch (g.kind[t]) {
+        case K_GEMM: return fp64 ? 5.0 + 20.0 * np / g.parts[t] : 2.5 + 1.0 * np;
+        case K_LU:
+        case K_LLT: return fp64 ? 140.0 : 20.0;
+        case K_LINV:
+        case K_UINV: return fp64 ? 95.0 : 14.0;
+        default: return fp64 ? 6.0 : 3.0;
+    }
+}
+static constexpr double HOP_US = 2.4;
+
+// earliest start of every task with unlimited CTAs (longest weighted path
+// from a source)
+static std::vector<double> estimate_start(const TaskGraph& g, bool fp64) {
     std::vector<int32_t> by_level(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) by_level[t] = t;
     std::stable_sort(by_level.begin(), by_level.end(), [&](int32_t a, int32_t b) { return g.level[a] < g.level[b]; });
     std::vector<double> est(g.ntasks, 0.0);
     for (int32_t t : by_level) {
-        const double fin = est[t] + cost(t) + hop;
+        const double fin = est[t] + task_cost(g, t, fp64) + HOP_US;
         for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++) est[g.succ[k]] = std::max(est[g.succ[k]], fin);
     }
+    return est;
+}
+
+std::vector<int32_t> static_order(const TaskGraph& g, bool fp64) {
+    const std::vector<double> est = estimate_start(g, fp64);
     std::vector<int32_t> tasks(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) tasks[t] = t;
     std::stable_sort(tasks.begin(), tasks.end(), [&](int32_t a, int32_t b) {
@@ -359,6 +368,33 @@ std::vector<int32_t> static_order(const TaskGraph& g, bool fp64) {
     for (int32_t t : tasks)
         for (int p = 0; p < g.parts[t]; p++) items.push_back((t << 4) | p);
     return items;
+}
+
+void order_pairs_by_ready(TaskGraph& g, bool fp64) {
+    const std::vector<double> est = estimate_start(g, fp64);
+    auto ready = [&](int32_t block) {
+        const int32_t t = block > 0 && block < (int32_t)g.producer.size() ? g.producer[block] : -1;
+        return t < 0 ? -1.0 : est[t] + task_cost(g, t, fp64);
+    };
+    std::vector<std::pair<double, int32_t>> key;
+    std::vector<int32_t> pa, pb;
+    for (int32_t t = 0; t < g.ntasks; t++) {
+        const int32_t p0 = g.pair_ptr[t], p1 = g.pair_ptr[t + 1];
+        if (g.kind[t] != K_GEMM || p1 - p0 < 2) continue;
+        key.clear();
+        for (int32_t p = p0; p < p1; p++) {
+            const int32_t b = (g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]) & ~PAIR_TRANS;
+            key.push_back({std::max(ready(g.pair_a[p]), ready(b)), p});
+        }
+        std::stable_sort(key.begin(), key.end(),
+                         [](const std::pair<double, int32_t>& x, const std::pair<double, int32_t>& y) { return x.first < y.first; });
+        pa.assign(g.pair_a.begin() + p0, g.pair_a.begin() + p1);
+        pb.assign(g.pair_b.begin() + p0, g.pair_b.begin() + p1);
+        for (int32_t i = 0; i < p1 - p0; i++) {
+            g.pair_a[p0 + i] = pa[key[i].second - p0];
+            g.pair_b[p0 + i] = pb[key[i].second - p0];
+        }
+    }
 }
 
 void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,

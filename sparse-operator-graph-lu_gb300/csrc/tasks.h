@@ -57,6 +57,8 @@ struct TaskGraph {
     // a copy, which reads its source's tile (every block is written once, so
     // a copy's source never changes after the copy would have run)
     std::vector<int32_t> alias;
+    // block -> task producing it (-1: an input block or none)
+    std::vector<int32_t> producer;
 };
 
 // outputs: block ids that must be materialised (the L/U leaves; a copied
@@ -81,6 +83,10 @@ void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const s
 // weighted path from a source, single-CTA task latencies as weights), ties by
 // longest remaining path. Every task comes after its predecessors.
 std::vector<int32_t> static_order(const TaskGraph& g, bool fp64);
+// Reorders every product's operand pairs by the estimated finish of their
+// producers (stable), so a task that starts before its last producer ends
+// accumulates the ready pairs first and the late one last.
+void order_pairs_by_ready(TaskGraph& g, bool fp64);
 
 // Look-ahead products for the substitution: for every block row i with an L
 // block at (i, i-1), lla[i] = id of a new block Linv_ii * L_{i,i-1}; for every
