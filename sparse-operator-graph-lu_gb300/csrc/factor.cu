@@ -139,7 +139,24 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
         const double* sA = sm + s * F64_STAGE;
         const double* sB = sA + 32 * 68;
         const double sgn = tk.pair_b[p] < 0 ? -1.0 : 1.0;
-        if ((tk.pair_b[p] < 0 ? -tk.pair_b[p] : tk.pair_b[p]) & PAIR_TRANS) {  // B[k][n] = sB[n][k]
+        // in-tile sparsity (tk.skip_zero): an 8x4 fragment of A or a 4x8
+        // fragment of B that is all zero contributes exact zeros, so its MMA
+        // is skipped after one warp vote (a NaN is not zero). The reference
+        // skips zero 8x8 sub-tiles by their masks (MatrixStdDouble.cpp:268-289).
+        // The votes cost about 5 % on dense tiles, so the autotuner decides.
+        const bool tr = ((tk.pair_b[p] < 0 ? -tk.pair_b[p] : tk.pair_b[p]) & PAIR_TRANS) != 0;
+        if (tk.skip_zero) {
+#pragma unroll
+            for (int k0 = 0; k0 < 64; k0 += 4) {
+                const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];
+                if (!__any_sync(FULL, a != 0.0)) continue;
+#pragma unroll
+                for (int nt = 0; nt < 2; nt++) {
+                    const double b = tr ? sB[(ch * 16 + nt * 8 + g) * 68 + k0 + t] : sB[(k0 + t) * 40 + ch * 16 + nt * 8 + g];
+                    if (__any_sync(FULL, b != 0.0)) dmma_8x8x4(acc[nt], a, b);
+                }
+            }
+        } else if (tr) {  // B[k][n] = sB[n][k]
 #pragma unroll
             for (int k0 = 0; k0 < 64; k0 += 4) {
                 const double a = sgn * sA[(rg * 8 + g) * 68 + k0 + t];

@@ -50,6 +50,8 @@ struct DevTasks {
     int32_t early;
     const int32_t *pair_wa, *pair_wb, *init_w;
     int32_t* task_done;
+    // FP64 products skip MMAs of all-zero operand fragments (in-tile sparsity)
+    int32_t skip_zero;
     DevStatus* status;
     unsigned long long wait_limit_ns;  // bound on any single queue wait
     // optional per-task trace (4 x u64 per task: ready, start, end, sm id), NULL = off

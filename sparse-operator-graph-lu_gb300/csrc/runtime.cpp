@@ -201,6 +201,7 @@ namespace {
 struct Tuned {
     int executor, stages;
     bool early;  // static order: products may start before their last producer
+    bool sparse = true;  // FP64: skip MMAs of all-zero operand fragments
 };
 std::mutex g_tune_mu;
 std::map<uint64_t, Tuned> g_tuned;
@@ -407,6 +408,7 @@ int run_factor(sog_system* s) {
     s->tune_pending = false;
     std::vector<Tuned> cands = {{SOG_EXEC_PERSISTENT, 2, true}, {SOG_EXEC_QUEUE, 2, false}};
     const int sms = s->ctx->num_sms;
+    if (s->fp64) cands.push_back({SOG_EXEC_PERSISTENT, 2, false, false});
     if (!s->fp64) {
         cands.push_back({SOG_EXEC_PERSISTENT, 2, false});
         if (factor_persistent_grid(false, 1, sms) > factor_persistent_grid(false, 2, sms))
@@ -418,6 +420,7 @@ int run_factor(sog_system* s) {
         s->opt.executor = c.executor;
         s->stages = c.stages;
         s->dt.early = !s->fp64 && c.early && !s->poisoned;
+        s->dt.skip_zero = c.sparse;
         s->grid_factor = factor_persistent_grid(s->fp64, c.stages, sms);
         for (int rep = 0; rep < 2; rep++) {
             const int r = run_factor_once(s);
@@ -433,6 +436,7 @@ int run_factor(sog_system* s) {
     s->stages = pick.stages;
     s->early = pick.early;
     s->dt.early = !s->fp64 && pick.early && !s->poisoned;
+    s->dt.skip_zero = pick.sparse;
     s->grid_factor = factor_persistent_grid(s->fp64, pick.stages, sms);
     return run_factor_once(s);
 }
@@ -961,6 +965,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->d_level_items = put(A, o_levels, g.level_items, st);
     dt.order = put(A, o_order, order, st);
     dt.early = !s->fp64;  // the tuner may turn it off
+    dt.skip_zero = 1;
     s->early = dt.early;
     dt.pair_wa = pair_wa.empty() ? nullptr : put(A, o_pwa, pair_wa, st);
     dt.pair_wb = pair_wb.empty() ? nullptr : put(A, o_pwb, pair_wb, st);
@@ -1023,6 +1028,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
             s->stages = known.stages;
             s->early = known.early;
             dt.early = !s->fp64 && known.early;
+            dt.skip_zero = known.sparse;
         } else {
             s->opt.executor = SOG_EXEC_PERSISTENT;
             s->tune_pending = true;
