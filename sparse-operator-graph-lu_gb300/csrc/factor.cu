@@ -365,8 +365,10 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
 // loads; only the pair holding column k needs per-element selection. Half the
 // instructions per step of the stride-4 layout above, which the FP64 path keeps
 // (there is no paired FP64 FMA).
+// blocks: in (source), lo (L), up (U), linv (L^-1, 0 = none), uinv (U^-1, 0 = none)
 template <bool CHOL>
-__device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int task, float* sm) {
+__device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_t in, int32_t lo, int32_t up,
+                           int32_t linv, int32_t uinv, float* sm) {
     float* rowbuf = sm;     // [2][64] published rows
     float* piv = sm + 128;  // [64]
     float* rpiv = piv + 64;
@@ -374,7 +376,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int ta
     __shared__ float s_maxa, s_maxu;
     const int tid = threadIdx.x, lane = tid & 31, r = tid >> 2, q = tid & 3;
     if (tid == 0) { s_maxa = 0.f; s_maxu = 0.f; }
-    const float* A = tiles + (size_t)tk.a[task] * 4096;
+    const float* A = tiles + (size_t)in * 4096;
     float2 a2[8], y2[8];
     float ma = 0.f;
 #pragma unroll
@@ -443,8 +445,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int ta
         }
     }
     __syncthreads();
-    float* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + 2 * q;
-    const int32_t linv = tk.b[task];
+    float* L = tiles + (size_t)lo * 4096 + r * 64 + 2 * q;
     float mu = 0.f;
     if (CHOL) {
         float* sq = rowbuf;
@@ -470,7 +471,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int ta
             }
         }
     } else {
-        float* U = tiles + (size_t)tk.out2[task] * 4096 + r * 64 + 2 * q;
+        float* U = tiles + (size_t)up * 4096 + r * 64 + 2 * q;
 #pragma unroll
         for (int m = 0; m < 8; m++) {
             const int c0 = 8 * m + 2 * q, c1 = c0 + 1;
@@ -489,7 +490,6 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int ta
                 *reinterpret_cast<float2*>(W + 8 * m) = make_float2(c0 <= r ? y2[m].x : 0.f, c0 + 1 <= r ? y2[m].y : 0.f);
             }
         }
-        const int32_t uinv = tk.c[task];
         if (uinv > 0) {
             float* V = tiles + (size_t)uinv * 4096 + r * 64 + 2 * q;
 #pragma unroll
@@ -816,12 +816,25 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
             }
             break;
         case K_LU:
-            if constexpr (sizeof(T) == 4) lu_task_f2<false>(tk, tiles, task, sm);
+            if constexpr (sizeof(T) == 4)
+                lu_task_f2<false>(tk, tiles, tk.a[task], tk.out[task], tk.out2[task], tk.b[task], tk.c[task], sm);
             else lu_task<T, false>(tk, tiles, task, sm);
             break;
         case K_LLT:
-            if constexpr (sizeof(T) == 4) lu_task_f2<true>(tk, tiles, task, sm);
+            if constexpr (sizeof(T) == 4)
+                lu_task_f2<true>(tk, tiles, tk.a[task], tk.out[task], 0, tk.b[task], 0, sm);
             else lu_task<T, true>(tk, tiles, task, sm);
+            break;
+        case K_GEMM_LU:
+        case K_GEMM_LLT:  // the product, then in the same CTA the factorisation of its result
+            if constexpr (sizeof(T) == 4) {
+                gemm_f32_tc<S>(tk, tiles, task, sm, st, phase, early);  // ends with a CTA barrier
+                if (tk.kind[task] == K_GEMM_LU)
+                    lu_task_f2<false>(tk, tiles, tk.out[task], tk.out3[task], tk.out2[task], tk.b[task], tk.c[task],
+                                      sm);
+                else
+                    lu_task_f2<true>(tk, tiles, tk.out[task], tk.out3[task], 0, tk.b[task], 0, sm);
+            }
             break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;
         case K_UINV: inv_task<T, false>(tk, tiles, task, sm); break;

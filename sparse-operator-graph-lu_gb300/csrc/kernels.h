@@ -29,8 +29,10 @@ struct DevTasks {
     const uint8_t* parts;
     // out/out2: result blocks; a: source (LU/inverses), minuend (SUB) or initial
     // tile of a product (GEMM, 0 = zero); b: subtrahend (SUB) or L^-1 of an
-    // LU / LL^T task (0 = none); c: U^-1 of an LU task (0 = none)
-    const int32_t *out, *out2, *a, *b, *c;
+    // LU / LL^T task (0 = none); c: U^-1 of an LU task (0 = none). A product
+    // with its LU (K_GEMM_LU / K_GEMM_LLT): out = the product, which the LU
+    // factors; out3 = L, out2 = U, b = L^-1, c = U^-1.
+    const int32_t *out, *out2, *a, *b, *c, *out3;
     const int32_t* prio;  // longest path to a sink, for choosing which ready successor to keep
     const int32_t *pair_ptr, *pair_a, *pair_b;
     const int32_t *succ_ptr, *succ;

@@ -793,7 +793,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (int32_t id : lla) if (id > 0) outputs.push_back(id);
     for (int32_t id : ula) if (id > 0) outputs.push_back(id);
     try {
-        s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts);
+        s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts, true, !s->fp64);
         if (!s->fp64) order_pairs_by_ready(s->tg, false);
     } catch (const std::exception& e) {
         delete s;
@@ -837,7 +837,9 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     std::vector<int32_t> pair_wa, pair_wb, init_w;
     if (!s->fp64) {
         for (int32_t& it : order)  // one pair has nothing to overlap with
-            if (g.kind[it >> 4] == K_GEMM && g.pair_ptr[(it >> 4) + 1] - g.pair_ptr[it >> 4] > 1) it |= ITEM_EARLY;
+            if ((g.kind[it >> 4] == K_GEMM || g.kind[it >> 4] == K_GEMM_LU || g.kind[it >> 4] == K_GEMM_LLT) &&
+                g.pair_ptr[(it >> 4) + 1] - g.pair_ptr[it >> 4] > 1)
+                it |= ITEM_EARLY;
         pair_wa.resize(g.pair_a.size());
         pair_wb.resize(g.pair_b.size());
         for (size_t q = 0; q < g.pair_a.size(); q++) {
@@ -847,7 +849,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         }
         init_w.assign(g.ntasks, -1);
         for (int32_t t = 0; t < g.ntasks; t++)
-            if (g.kind[t] == K_GEMM && g.a[t] > p.n_input) init_w[t] = g.producer[g.a[t]];
+            if ((g.kind[t] == K_GEMM || g.kind[t] == K_GEMM_LU || g.kind[t] == K_GEMM_LLT) && g.a[t] > p.n_input)
+                init_w[t] = g.producer[g.a[t]];
     }
     HostCSR hc;
     if (!plan->imported) hc = build_csr(p);
@@ -895,7 +898,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),
              o_out2 = L.add<int32_t>(g.ntasks), o_a = L.add<int32_t>(g.ntasks), o_b = L.add<int32_t>(g.ntasks),
-             o_c = L.add<int32_t>(g.ntasks),
+             o_c = L.add<int32_t>(g.ntasks), o_out3 = L.add<int32_t>(g.ntasks),
              o_pptr = L.add<int32_t>(g.ntasks + 1), o_pa = L.add<int32_t>(g.pair_a.size()),
              o_pb = L.add<int32_t>(g.pair_b.size()), o_sptr = L.add<int32_t>(g.ntasks + 1),
              o_succ = L.add<int32_t>(g.succ.size()), o_ndep0 = L.add<int32_t>(g.ntasks),
@@ -945,6 +948,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.a = put(A, o_a, g.a, st);
     dt.b = put(A, o_b, g.b, st);
     dt.c = put(A, o_c, g.c, st);
+    dt.out3 = put(A, o_out3, g.out3, st);
     dt.prio = put(A, o_prio, g.prio, st);
     dt.pair_ptr = put(A, o_pptr, g.pair_ptr, st);
     dt.pair_a = put(A, o_pa, g.pair_a, st);
@@ -1324,6 +1328,8 @@ int sog_system_task_info(const sog_system* s, int64_t* counts) {
     for (int k = 0; k < 5; k++) counts[4 + k] = g.count[k];
     counts[5] += g.count[K_LLT];
     counts[8] += g.count[K_TRANS];
+    counts[4] += g.count[K_GEMM_LU] + g.count[K_GEMM_LLT];  // a product with its LU counts as both
+    counts[5] += g.count[K_GEMM_LU] + g.count[K_GEMM_LLT];
     counts[9] = s->grid_factor;
     counts[10] = s->launches;
     return SOG_OK;

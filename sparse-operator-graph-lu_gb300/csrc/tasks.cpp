@@ -66,7 +66,7 @@ static std::vector<Op> alias_copies(const std::vector<Op>& in, int32_t storage_c
 }
 
 TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int32_t n_input,
-                      const std::vector<int32_t>& outputs_in, int gemm_parts, bool fuse_subs) {
+                      const std::vector<int32_t>& outputs_in, int gemm_parts, bool fuse_subs, bool fuse_lu) {
     if (gemm_parts != 1 && gemm_parts != 4) throw std::runtime_error("gemm_parts must be 1 or 4");
     std::vector<int32_t> alias;
     int64_t ncopies = 0, ndup = 0;
@@ -83,7 +83,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     // pass 1: one task per produced block (LU: per result pair)
     struct T0 {
         uint8_t kind;
-        int32_t out, out2, a, b, c = 0;
+        int32_t out, out2, a, b, c = 0, out3 = 0;
         std::vector<int32_t> pa, pb;
         bool dead = false;
     };
@@ -181,12 +181,37 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         X.dead = true;
         fused_inv++;
     }
+    // fuse  LU(S)  into the product writing S when S is read by nothing else:
+    // the factorisation starts in the same CTA right after the product, with
+    // no dependency hop (product result S stays in out; the LU's L moves to
+    // out3, its U / L^-1 / U^-1 to out2 / b / c)
+    int64_t fused_lu = 0;
+    if (fuse_lu && gemm_parts == 1) {
+        for (size_t s = 0; s < tl.size(); s++) {
+            T0& X = tl[s];
+            if (X.dead || (X.kind != K_LU && X.kind != K_LLT) || X.a <= 0) continue;
+            const int32_t src = X.a;
+            const int32_t t = producer[src];
+            if (t < 0 || tl[t].kind != K_GEMM || tl[t].out != src || readers[src] != 1 || is_out[src]) continue;
+            T0& G = tl[t];
+            G.kind = X.kind == K_LU ? K_GEMM_LU : K_GEMM_LLT;
+            G.out3 = X.out;
+            G.out2 = X.out2;
+            G.b = X.b;
+            G.c = X.c;
+            for (int32_t id : {X.out, X.out2, X.b, X.c})
+                if (id > 0) producer[id] = (int32_t)t;
+            X.dead = true;
+            fused_lu++;
+        }
+    }
     // renumber live tasks
     std::vector<int32_t> newid(tl.size(), -1);
     TaskGraph g;
     g.storage_count = storage_count;
     g.fused_subs = fused;
     g.fused_inverses = fused_inv;
+    g.fused_lu = fused_lu;
     g.aliased_copies = ncopies;
     g.aliased_inverses = ndup;
     g.alias = std::move(alias);
@@ -203,6 +228,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         g.a.push_back(x.a);
         g.b.push_back(x.b);
         g.c.push_back(x.c);
+        g.out3.push_back(x.out3);
         g.pair_a.insert(g.pair_a.end(), x.pa.begin(), x.pa.end());
         g.pair_b.insert(g.pair_b.end(), x.pb.begin(), x.pb.end());
         g.pair_ptr[newid[t] + 1] = (int32_t)g.pair_a.size();
@@ -331,6 +357,8 @@ static double task_cost(const TaskGraph& g, int32_t t, bool fp64) {
     const int np = g.pair_ptr[t + 1] - g.pair_ptr[t];
     switch (g.kind[t]) {
         case K_GEMM: return fp64 ? 5.0 + 20.0 * np / g.parts[t] : 2.5 + 1.0 * np;
+        case K_GEMM_LU:
+        case K_GEMM_LLT: return 2.5 + 1.0 * np + 18.0;
         case K_LU:
         case K_LLT: return fp64 ? 140.0 : 20.0;
         case K_LINV:
@@ -380,7 +408,7 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
     std::vector<int32_t> pa, pb;
     for (int32_t t = 0; t < g.ntasks; t++) {
         const int32_t p0 = g.pair_ptr[t], p1 = g.pair_ptr[t + 1];
-        if (g.kind[t] != K_GEMM || p1 - p0 < 2) continue;
+        if ((g.kind[t] != K_GEMM && g.kind[t] != K_GEMM_LU && g.kind[t] != K_GEMM_LLT) || p1 - p0 < 2) continue;
         key.clear();
         for (int32_t p = p0; p < p1; p++) {
             const int32_t b = (g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]) & ~PAIR_TRANS;

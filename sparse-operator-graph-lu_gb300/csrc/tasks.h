@@ -22,8 +22,12 @@
 
 namespace sog {
 
-enum TaskKind : uint8_t { K_GEMM = 0, K_LU = 1, K_LINV = 2, K_UINV = 3, K_SUB = 4, K_LLT = 5, K_TRANS = 6 };
-constexpr int NUM_KINDS = 7;
+// K_GEMM_LU / K_GEMM_LLT: a product followed, in the same task, by the LU
+// (LL^T) of its result (the diagonal block is read by nothing else)
+enum TaskKind : uint8_t {
+    K_GEMM = 0, K_LU = 1, K_LINV = 2, K_UINV = 3, K_SUB = 4, K_LLT = 5, K_TRANS = 6, K_GEMM_LU = 7, K_GEMM_LLT = 8
+};
+constexpr int NUM_KINDS = 9;
 // GEMM operand pairs: pair_b = +-(id | PAIR_TRANS): a negative entry subtracts
 // the product, PAIR_TRANS multiplies by the transpose of block id (mult ops)
 constexpr int32_t PAIR_TRANS = 1 << 30;
@@ -35,7 +39,7 @@ struct TaskGraph {
     int32_t ntasks = 0;
     int32_t storage_count = 0;
     std::vector<uint8_t> kind, parts;
-    std::vector<int32_t> out, out2, a, b, c;   // block ids (see kernels.h DevTasks)
+    std::vector<int32_t> out, out2, a, b, c, out3;  // block ids (see kernels.h DevTasks)
     std::vector<int32_t> pair_ptr;             // ntasks+1; GEMM operand pairs
     std::vector<int32_t> pair_a, pair_b;       // pair_b < 0: subtract A*B(|pair_b|)
     std::vector<int32_t> succ_ptr, succ;       // successor tasks
@@ -52,7 +56,8 @@ struct TaskGraph {
     int64_t fused_inverses = 0;  // lowerInv / upperInv tasks folded into their LU task
     int64_t aliased_copies = 0;  // copy ops (sub with src = 0) replaced by aliasing
     int64_t aliased_inverses = 0;  // repeated lowerInv / upperInv of one block replaced by aliasing
-    int64_t count[NUM_KINDS] = {0, 0, 0, 0, 0, 0, 0};
+    int64_t count[NUM_KINDS] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t fused_lu = 0;  // LU / LL^T tasks merged into the product producing their block
     // block -> block whose tile holds its value: identity except the result of
     // a copy, which reads its source's tile (every block is written once, so
     // a copy's source never changes after the copy would have run)
@@ -66,8 +71,11 @@ struct TaskGraph {
 // std::runtime_error on a block written by ops of different kinds, a read of a
 // block nobody produces (and not an input), an id out of range, or a cycle.
 // gemm_parts: parts per GEMM task (1 or 4).
+// fuse_lu: merge an LU / LL^T task into the single-part product producing its
+// input block when nothing else reads that block (the mixed path).
 TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input,
-                      const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs = true);
+                      const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs = true,
+                      bool fuse_lu = false);
 
 // Appends, for every diagonal L (U) block without one already in the DAG, a
 // lowerInv (upperInv) op; returns per block row the id of the inverse of the

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import numpy as np
 
-KIND_NAMES = ["gemm", "lu", "linv", "uinv", "sub"]
+KIND_NAMES = ["gemm", "lu", "linv", "uinv", "sub", "llt", "trans", "gemm+lu", "gemm+llt"]
 
 
 def analyze(tt: np.ndarray, kind: np.ndarray, succ_ptr: np.ndarray, succ: np.ndarray,
@@ -50,7 +50,7 @@ def analyze(tt: np.ndarray, kind: np.ndarray, succ_ptr: np.ndarray, succ: np.nda
         seg["exec_us"][nm] = seg["exec_us"].get(nm, 0.0) + float(dur[t])
         seg["latency_us"] += (int(start[t]) - prev_end) / 1e3
         prev_end = int(end[t])
-    seg["count_by_kind"] = {KIND_NAMES[k]: int(sum(1 for t in path if kind[t] == k)) for k in range(5)}
+    seg["count_by_kind"] = {KIND_NAMES[k]: int(sum(1 for t in path if kind[t] == k)) for k in range(len(KIND_NAMES))}
     out["critical_path"] = seg
     return out
 
