@@ -172,6 +172,38 @@ def test_mixed_pipeline_and_autotune(sg, wl, ctx, name, cfg):
     sys_.close()
 
 
+@pytest.mark.parametrize("name", ["lap2d_32", "var3d_16", "cd_40", "spd_var3d_16"])
+def test_executors_agree_bitwise(sg, wl, ctx, name):
+    """Every task computes from its own inputs only, so the schedule cannot
+    change a result: the static order with early-start products (a product
+    begins before its last producer finished), the ready queue and the
+    per-level launches give bit-identical mixed factors and solutions, and
+    the tuned configuration is reported."""
+    s = golden_cases(wl)[name]()
+    sym = name.startswith("spd_")
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals, symmetric=sym)
+    xs = []
+    for executor in (0, 2, 1):
+        sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=executor)
+        cfg = sys_.executor_config()
+        assert cfg["executor"] == executor
+        assert cfg["early_products"] == (executor == 0)
+        sys_.factor(s.vals)
+        x, st = sys_.solve(rhs_of(s))
+        assert st["rel_resid"] <= 1e-10
+        xs.append(x)
+        sys_.close()
+    np.testing.assert_array_equal(xs[0], xs[1])
+    np.testing.assert_array_equal(xs[0], xs[2])
+    auto = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=3)
+    auto.factor(s.vals)
+    cfg = auto.executor_config()
+    assert cfg["executor"] in (0, 2) and cfg["stages"] in (1, 2)
+    x, _ = auto.solve(rhs_of(s))
+    np.testing.assert_array_equal(x, xs[0])
+    auto.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["spd_lap2d_8", "spd_lap2d_32", "spd_var3d_16"])
 def test_llt_path_matches_reference(sg, wl, ctx, oracle, name, precision):
