@@ -754,8 +754,12 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     int gemm_parts = o.gemm_split == 1 ? 1 : (o.gemm_split == 4 ? 4 : (s->fp64 ? 4 : 1));
     if (!s->fp64) gemm_parts = 1;
     // inverses of the diagonal factor blocks for the substitution (reused
-    // where the DAG already computes them)
-    std::vector<Op> ops2 = p.ops;
+    // where the DAG already computes them). Room for everything appended
+    // below (inverses, look-ahead products, transposed leaves), so the op
+    // records are copied once.
+    std::vector<Op> ops2;
+    ops2.reserve(p.ops.size() + 4 * (size_t)p.cfg.block_rows + p.L.size());
+    ops2.assign(p.ops.begin(), p.ops.end());
     int32_t storage2 = p.storage_count;
     // LL^T systems: the upper factor of the substitution is L^T (upperSolverT,
     // BlockPlanner.cpp:752-797), materialised as transposed L leaves (in a
@@ -1285,7 +1289,9 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
     if (!plan || !counts) return fail(SOG_EINVAL, "NULL argument");
     const Plan& p = plan->p;
     try {
-        std::vector<Op> ops2 = p.ops;
+        std::vector<Op> ops2;
+        ops2.reserve(p.ops.size() + 2 * (size_t)p.cfg.block_rows);
+        ops2.assign(p.ops.begin(), p.ops.end());
         int32_t storage2 = p.storage_count;
         std::vector<int32_t> ldinv, udinv, outputs;
         add_diag_inverses(ops2, storage2, p.cfg.block_rows, p.L, p.U, ldinv, udinv);

@@ -11,8 +11,10 @@ namespace sog {
 // and a second lowerInv / upperInv of the same block reads the first one's
 // result (the planner's two levels invert some diagonal blocks twice). Chains
 // resolve to the first non-redundant block.
-static std::vector<Op> alias_copies(const std::vector<Op>& in, int32_t storage_count, std::vector<int32_t>& alias,
-                                    int64_t& ncopies, int64_t& ndup) {
+// Marks in skip the ops replaced by aliasing; readers of the other ops then
+// read alias[src] (a view, not a copy of the op list).
+static void alias_copies(const std::vector<Op>& in, int32_t storage_count, std::vector<int32_t>& alias,
+                         std::vector<char>& skip, int64_t& ncopies, int64_t& ndup) {
     alias.resize(storage_count);
     for (int32_t b = 0; b < storage_count; b++) alias[b] = b;
     ncopies = ndup = 0;
@@ -27,8 +29,8 @@ static std::vector<Op> alias_copies(const std::vector<Op>& in, int32_t storage_c
         return r;
     };
     auto valid = [&](int32_t b) { return b > 0 && b < storage_count; };
-    std::vector<char> skip(in.size(), 0);
-    std::unordered_map<int64_t, int32_t> first_inv;  // (kind, source root) -> result
+    skip.assign(in.size(), 0);
+    std::vector<int32_t> first_inv;  // (source root << 1 | upper) -> result, 0 = none yet
     for (size_t i = 0; i < in.size(); i++) {
         const Op& o = in[i];
         if (o.op == OP_SUB && o.src == 0 && valid(o.src2) && valid(o.res) && alias[o.res] == o.res) {
@@ -37,32 +39,18 @@ static std::vector<Op> alias_copies(const std::vector<Op>& in, int32_t storage_c
             ncopies++;
         } else if ((o.op == OP_LOWERINV || o.op == OP_UPPERINV) && valid(o.src) && valid(o.res) &&
                    alias[o.res] == o.res) {
-            const int64_t key = ((int64_t)find(o.src) << 1) | (o.op == OP_UPPERINV ? 1 : 0);
-            auto it = first_inv.find(key);
-            if (it == first_inv.end()) {
-                first_inv.emplace(key, o.res);
+            if (first_inv.empty()) first_inv.assign(2 * (size_t)storage_count, 0);
+            const size_t key = ((size_t)find(o.src) << 1) | (o.op == OP_UPPERINV ? 1 : 0);
+            if (first_inv[key] == 0) {
+                first_inv[key] = o.res;
             } else {
-                alias[o.res] = it->second;
+                alias[o.res] = first_inv[key];
                 skip[i] = 1;
                 ndup++;
             }
         }
     }
     for (int32_t b = 0; b < storage_count; b++) find(b);
-    std::vector<Op> out;
-    out.reserve(in.size() - ncopies - ndup);
-    for (size_t i = 0; i < in.size(); i++) {
-        const Op& o = in[i];
-        if (skip[i]) continue;
-        if ((o.res > 0 && o.res < storage_count && alias[o.res] != o.res) ||
-            (o.res2 > 0 && o.res2 < storage_count && alias[o.res2] != o.res2))
-            throw std::runtime_error("block written by a copy and by another op");
-        Op q = o;
-        if (q.src > 0 && q.src < storage_count) q.src = alias[q.src];
-        if (q.src2 > 0 && q.src2 < storage_count) q.src2 = alias[q.src2];
-        out.push_back(q);
-    }
-    return out;
 }
 
 TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int32_t n_input,
@@ -70,7 +58,16 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     if (gemm_parts != 1 && gemm_parts != 4) throw std::runtime_error("gemm_parts must be 1 or 4");
     std::vector<int32_t> alias;
     int64_t ncopies = 0, ndup = 0;
-    const std::vector<Op> ops = alias_copies(ops_in, storage_count, alias, ncopies, ndup);
+    std::vector<char> skip;
+    alias_copies(ops_in, storage_count, alias, skip, ncopies, ndup);
+    const std::vector<Op>& ops = ops_in;
+    // an op that survives aliasing, with its sources read through the aliases
+    auto view = [&](int64_t i) {
+        Op q = ops[i];
+        if (q.src > 0 && q.src < storage_count) q.src = alias[q.src];
+        if (q.src2 > 0 && q.src2 < storage_count) q.src2 = alias[q.src2];
+        return q;
+    };
     std::vector<int32_t> outputs;
     outputs.reserve(outputs_in.size());
     for (int32_t id : outputs_in) outputs.push_back(id > 0 && id < storage_count ? alias[id] : id);
@@ -80,17 +77,24 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     auto check_id = [&](int32_t id) {
         if (id < 0 || id >= storage_count) throw std::runtime_error("block id out of range in DAG");
     };
-    // pass 1: one task per produced block (LU: per result pair)
+    // pass 1: one task per produced block (LU: per result pair). Products
+    // keep their operand pairs in op order in flat arrays: counted here,
+    // placed after the pass.
     struct T0 {
         uint8_t kind;
         int32_t out, out2, a, b, c = 0, out3 = 0;
-        std::vector<int32_t> pa, pb;
+        int32_t p0 = 0, np = 0;  // this task's range of fpa / fpb
         bool dead = false;
     };
     std::vector<T0> tl;
+    tl.reserve(nops / 4 + 16);
+    std::vector<int32_t> op_task(nops, -1);  // product op -> its task
     for (int64_t i = 0; i < nops; i++) {
-        const Op& o = ops[i];
+        if (skip[i]) continue;
+        const Op o = view(i);
         check_id(o.src); check_id(o.src2); check_id(o.res); check_id(o.res2);
+        if ((o.res > 0 && alias[o.res] != o.res) || (o.res2 > 0 && alias[o.res2] != o.res2))
+            throw std::runtime_error("block written by a copy and by another op");
         if (o.res <= 0) throw std::runtime_error("op without result");
         if (o.res <= n_input || (o.res2 > 0 && o.res2 <= n_input)) throw std::runtime_error("op writes an input block");
         if (o.src > 0) readers[o.src]++;
@@ -117,7 +121,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
             x.out2 = k == K_LU ? o.res2 : 0;
             x.a = k == K_SUB ? o.src2 : (k == K_GEMM ? 0 : o.src);
             x.b = k == K_SUB ? o.src : 0;
-            tl.push_back(std::move(x));
+            tl.push_back(x);
             producer[o.res] = t;
             if (k == K_LU) {
                 if (o.res2 <= 0 || producer[o.res2] >= 0) throw std::runtime_error("bad LU result pair");
@@ -126,9 +130,26 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         }
         if (k == K_GEMM) {
             if (o.src <= 0 || o.src2 <= 0) throw std::runtime_error("mul with absent operand");
-            tl[t].pa.push_back(o.src);
+            op_task[i] = t;
+            tl[t].np++;
+        }
+    }
+    int64_t npairs = 0;
+    for (T0& x : tl) {
+        x.p0 = (int32_t)npairs;
+        npairs += x.np;
+    }
+    std::vector<int32_t> fpa(npairs), fpb(npairs);
+    {
+        std::vector<int32_t> fill(tl.size(), 0);
+        for (int64_t i = 0; i < nops; i++) {
+            const int32_t t = op_task[i];
+            if (t < 0) continue;
+            const Op o = view(i);
+            const int32_t q = tl[t].p0 + fill[t]++;
+            fpa[q] = o.src;
             const int32_t b = o.op == OP_MULT ? (o.src2 | PAIR_TRANS) : o.src2;
-            tl[t].pb.push_back(o.op == OP_MULNEG ? -b : b);
+            fpb[q] = o.op == OP_MULNEG ? -b : b;
         }
     }
     // fuse  S = D - X  with  X = GEMM (X read only by S, not an output)
@@ -146,7 +167,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
             const int32_t g = producer[x];
             if (g < 0 || tl[g].kind != K_GEMM || tl[g].a != 0 || readers[x] != 1 || is_out[x]) continue;
             T0& G = tl[g];
-            for (auto& v : G.pb) v = -v;
+            for (int32_t q = G.p0; q < G.p0 + G.np; q++) fpb[q] = -fpb[q];
             G.a = S.a;  // initial tile D (0: none)
             producer[x] = -1;
             G.out = S.out;
@@ -218,6 +239,11 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     for (size_t t = 0; t < tl.size(); t++)
         if (!tl[t].dead) newid[t] = g.ntasks++;
     g.pair_ptr.assign(g.ntasks + 1, 0);
+    for (auto* v : {&g.out, &g.out2, &g.a, &g.b, &g.c, &g.out3}) v->reserve(g.ntasks);
+    g.kind.reserve(g.ntasks);
+    g.parts.reserve(g.ntasks);
+    g.pair_a.reserve(npairs);
+    g.pair_b.reserve(npairs);
     for (size_t t = 0; t < tl.size(); t++) {
         if (tl[t].dead) continue;
         const T0& x = tl[t];
@@ -229,46 +255,52 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         g.b.push_back(x.b);
         g.c.push_back(x.c);
         g.out3.push_back(x.out3);
-        g.pair_a.insert(g.pair_a.end(), x.pa.begin(), x.pa.end());
-        g.pair_b.insert(g.pair_b.end(), x.pb.begin(), x.pb.end());
+        g.pair_a.insert(g.pair_a.end(), fpa.begin() + x.p0, fpa.begin() + x.p0 + x.np);
+        g.pair_b.insert(g.pair_b.end(), fpb.begin() + x.p0, fpb.begin() + x.p0 + x.np);
         g.pair_ptr[newid[t] + 1] = (int32_t)g.pair_a.size();
     }
     for (int32_t b = 0; b < storage_count; b++)
         if (producer[b] >= 0) producer[b] = newid[producer[b]];
     g.producer = producer;  // copied: the dependency pass below still reads it
     g.gemm_pairs = (int64_t)g.pair_a.size();
-    // dependencies from each task's sources
-    std::vector<std::vector<int32_t>> preds(g.ntasks);
-    auto dep_on = [&](int32_t t, int32_t src) {
-        if (src <= 0 || src <= n_input) return;
+    // dependencies from each task's sources: per task its producer tasks
+    // (sorted, unique) in one flat array
+    auto prod_of = [&](int32_t t, int32_t src) -> int32_t {
+        if (src <= 0 || src <= n_input) return -1;
         const int32_t pt = producer[src];
         if (pt < 0) throw std::runtime_error("read of a block that no op produces");
         if (pt == t) throw std::runtime_error("task reads its own result");
-        preds[t].push_back(pt);
+        return pt;
     };
-    for (int32_t t = 0; t < g.ntasks; t++) {
-        dep_on(t, g.a[t]);
-        if (g.kind[t] == K_SUB) dep_on(t, g.b[t]);
-        for (int32_t p = g.pair_ptr[t]; p < g.pair_ptr[t + 1]; p++) {
-            dep_on(t, g.pair_a[p]);
-            dep_on(t, (g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]) & ~PAIR_TRANS);
-        }
-    }
+    std::vector<int64_t> pptr(g.ntasks + 1, 0);
+    for (int32_t t = 0; t < g.ntasks; t++)
+        pptr[t + 1] = pptr[t] + 1 + (g.kind[t] == K_SUB ? 1 : 0) + 2 * (g.pair_ptr[t + 1] - g.pair_ptr[t]);
+    std::vector<int32_t> preds(pptr[g.ntasks]);
     g.ndep.assign(g.ntasks, 0);
     std::vector<int32_t> scount(g.ntasks + 1, 0);
     for (int32_t t = 0; t < g.ntasks; t++) {
-        auto& p = preds[t];
-        std::sort(p.begin(), p.end());
-        p.erase(std::unique(p.begin(), p.end()), p.end());
-        g.ndep[t] = (int32_t)p.size();
-        for (int32_t q : p) scount[q + 1]++;
+        int32_t* p = preds.data() + pptr[t];
+        int n = 0;
+        auto add = [&](int32_t pt) {
+            if (pt >= 0) p[n++] = pt;
+        };
+        add(prod_of(t, g.a[t]));
+        if (g.kind[t] == K_SUB) add(prod_of(t, g.b[t]));
+        for (int32_t q = g.pair_ptr[t]; q < g.pair_ptr[t + 1]; q++) {
+            add(prod_of(t, g.pair_a[q]));
+            add(prod_of(t, (g.pair_b[q] < 0 ? -g.pair_b[q] : g.pair_b[q]) & ~PAIR_TRANS));
+        }
+        std::sort(p, p + n);
+        n = (int)(std::unique(p, p + n) - p);
+        g.ndep[t] = n;
+        for (int i = 0; i < n; i++) scount[p[i] + 1]++;
     }
     g.succ_ptr.assign(g.ntasks + 1, 0);
     for (int32_t t = 0; t < g.ntasks; t++) g.succ_ptr[t + 1] = g.succ_ptr[t] + scount[t + 1];
     g.succ.resize(g.succ_ptr[g.ntasks]);
     std::vector<int32_t> sf(g.succ_ptr.begin(), g.succ_ptr.end() - 1);
     for (int32_t t = 0; t < g.ntasks; t++)
-        for (int32_t q : preds[t]) g.succ[sf[q]++] = t;
+        for (int32_t i = 0; i < g.ndep[t]; i++) g.succ[sf[preds[pptr[t] + i]]++] = t;
     // topological order (Kahn); levels = longest path from a source
     std::vector<int32_t> indeg(g.ndep), order;
     order.reserve(g.ntasks);
@@ -312,11 +344,14 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
 
 void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv) {
-    std::unordered_map<int32_t, int32_t> have_l, have_u;
+    // per source block the result of the last lowerInv / upperInv of it (0: none)
+    std::vector<int32_t> have_l(storage_count, 0), have_u(storage_count, 0);
     for (const Op& o : ops) {
+        if (o.src <= 0 || o.src >= storage_count) continue;
         if (o.op == OP_LOWERINV) have_l[o.src] = o.res;
         if (o.op == OP_UPPERINV) have_u[o.src] = o.res;
     }
+    ops.reserve(ops.size() + L.size() + U.size());
     linv.assign(block_rows, 0);
     uinv.assign(block_rows, 0);
     int32_t seq = ops.empty() ? 0 : ops.back().seq;
@@ -327,9 +362,8 @@ void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_r
         auto& dst = side == 0 ? linv : uinv;
         for (const Leaf& lf : lv) {
             if (lf.bi != lf.bj) continue;
-            auto it = have.find(lf.id);
-            if (it != have.end()) {
-                dst[lf.bi] = it->second;
+            if (lf.id > 0 && lf.id < (int32_t)have.size() && have[lf.id] != 0) {
+                dst[lf.bi] = have[lf.id];
                 continue;
             }
             const int32_t id = storage_count++;
