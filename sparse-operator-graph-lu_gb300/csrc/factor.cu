@@ -57,6 +57,10 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+// release/acquire fence at GPU scope: with the CTA barrier before it, it
+// orders every thread's earlier writes before the flag or count that follows
+// (the fence.sc that __threadfence() issues is stronger than a release needs)
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
@@ -869,7 +873,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
     int last = 0;
     // release: the CTA's writes for this item (ordered before this warp by the
     // CTA barrier) become visible before any counter below moves
-    __threadfence();
+    fence_acq_rel_gpu();
     if (lane == 0) last = (tk.parts[task] == 1) || (atom_add_acquire(&tk.parts_left[task], -1) == 1);
     last = __shfl_sync(FULL, last, 0);
     int keep = -1, keep_prio = -1;  // warp-uniform
@@ -911,7 +915,7 @@ __device__ int complete_item(const DevTasks& tk, int task) {
             if (total) {
                 int base_pos = 0;
                 if (lane == 0) {
-                    __threadfence();
+                    fence_acq_rel_gpu();
                     base_pos = atomicAdd(tk.tail, total);
                 }
                 base_pos = __shfl_sync(FULL, base_pos, 0) + incl - np;
@@ -1017,12 +1021,12 @@ __global__ void __launch_bounds__(NT, (S == 1 || sizeof(T) == 8) ? 2 : 1) factor
 // trip): a claimant spinning on a successor's count sees it reach zero.
 __device__ void release_item(const DevTasks& tk, int task) {
     const int lane = threadIdx.x & 31;
-    __threadfence();  // release: the CTA's writes (ordered before this warp by the barrier)
+    fence_acq_rel_gpu();  // release: the CTA's writes (ordered before this warp by the barrier)
     int last = 1;
     if (tk.parts[task] > 1) {
         if (lane == 0) last = atom_add_acquire(&tk.parts_left[task], -1) == 1;
         last = __shfl_sync(FULL, last, 0);
-        if (last) __threadfence();  // the other parts' writes, acquired above, released with ours
+        if (last) fence_acq_rel_gpu();  // the other parts' writes, acquired above, released with ours
     }
     if (last) {
         // completion flag for products started early (ordered after the

@@ -34,6 +34,10 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+// release/acquire fence at GPU scope: with the CTA barrier before it, it
+// orders every thread's earlier writes before the flag or count that follows
+// (the fence.sc that __threadfence() issues is stronger than a release needs)
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
     asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         }
         __syncthreads();
         if (tid == 0) {
-            __threadfence();  // the row written by all threads (ordered by the barrier) before the flag
+            fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
             st_release(s.flags + (size_t)ch * R + i, epoch);
             if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
         }
