@@ -678,17 +678,18 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
             else if (globaltimer_ns() - t0 > lim) return false;
         }
     };
-    // the initial tile is read by warps 0,1,4,5 in the epilogue: load it now,
-    // under the operand copies and the MMAs (or after its producer, if late)
+    // the initial tile is read in the epilogue, 16 columns of one row per
+    // lane: load it now, under the operand copies and the MMAs (or after its
+    // producer, if late)
     const int quad = warp & 3, colh = (warp >> 2) * 32;
+    const int erow = 16 * quad + (lane >> 1), ecol = colh + 16 * (lane & 1);  // this lane's output slice
     const bool init_now = !early || s_init_ready;
-    float4 u[8];
+    float4 u[4];
     auto load_init = [&]() {
-        if (quad < 2 && init > 0) {
-            const float4* I =
-                reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + (32 * quad + lane) * 64 + colh);
+        if (init > 0) {
+            const float4* I = reinterpret_cast<const float4*>(tiles + (size_t)init * 4096 + erow * 64 + ecol);
 #pragma unroll
-            for (int i = 0; i < 8; i++) u[i] = __ldcg(I + i);
+            for (int i = 0; i < 4; i++) u[i] = __ldcg(I + i);
         }
     };
     if (init_now) load_init();
@@ -740,43 +741,43 @@ __device__ void gemm_f32_tc(const DevTasks& tk, float* __restrict__ tiles, int t
         phase ^= 1u << s;
     }
     tc::fence_after_sync();
-    // epilogue: C = init + the four quadrants of D (lanes 0-63: A_hi rows,
-    // 64-127: A_lo rows; columns 0-63: B_hi, 64-127: B_lo). Each warp sums
-    // its lanes' two column halves; warps 2,3,6,7 (the A_lo lanes) pass
-    // theirs through shared memory.
-    float* X = sm;  // [64][65], the operand area is free once the MMAs completed
-    float v[32], w[32];
-    const uint32_t tq = st.tmem + ((uint32_t)(32 * quad) << 16) + colh;
-    if (p0 < p1 && quad >= 2) {
+    // epilogue: C = init + D summed over the split products. Output row r has
+    // its head in TMEM lane 2r and its remainder in lane 2r + 1 (one warp);
+    // columns 0-63 are x B_hi, 64-127 x B_lo. Each lane adds its two column
+    // halves, takes its partner lane's sum by a shuffle, and the pair stores
+    // the row's 32 columns of this warp (16 each). No shared memory, no barrier.
+    float v[32];
+    if (p0 < p1) {
+        float w[32];
+        const uint32_t tq = st.tmem + ((uint32_t)(32 * quad) << 16) + colh;
         tc::tmem_ld32(tq, v);
         tc::tmem_ld32(tq + 64, w);
-        const int row = 32 * quad + lane - 64;
 #pragma unroll
-        for (int i = 0; i < 32; i++) X[row * 65 + colh + i] = v[i] + w[i];
-    }
-    __syncthreads();  // also orders thread 0's acquire of a late initial tile before its loads
-    if (!init_now) load_init();
-    if (quad < 2) {
-        const int row = 32 * quad + lane;
-        if (p0 < p1) {
-            tc::tmem_ld32(tq, v);
-            tc::tmem_ld32(tq + 64, w);
-#pragma unroll
-            for (int i = 0; i < 32; i++) v[i] += w[i] + X[row * 65 + colh + i];
-        } else {
-#pragma unroll
-            for (int i = 0; i < 32; i++) v[i] = 0.f;
+        for (int i = 0; i < 32; i++) {
+            v[i] += w[i];
+            v[i] += __shfl_xor_sync(FULL, v[i], 1);
         }
-        if (init > 0) {
+    } else {
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                v[4 * i] += u[i].x; v[4 * i + 1] += u[i].y; v[4 * i + 2] += u[i].z; v[4 * i + 3] += u[i].w;
-            }
-        }
-        float4* C = reinterpret_cast<float4*>(tiles + (size_t)tk.out[task] * 4096 + row * 64 + colh);
-#pragma unroll
-        for (int i = 0; i < 8; i++) C[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        for (int i = 0; i < 32; i++) v[i] = 0.f;
     }
+    if (!init_now) {
+        __syncthreads();  // orders thread 0's acquire of the late initial tile before the loads
+        load_init();
+    }
+    const bool upper = (lane & 1) != 0;
+    float o[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) o[i] = upper ? v[16 + i] : v[i];
+    if (init > 0) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            o[4 * i] += u[i].x; o[4 * i + 1] += u[i].y; o[4 * i + 2] += u[i].z; o[4 * i + 3] += u[i].w;
+        }
+    }
+    float4* C = reinterpret_cast<float4*>(tiles + (size_t)tk.out[task] * 4096 + erow * 64 + ecol);
+#pragma unroll
+    for (int i = 0; i < 4; i++) C[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
     tc::fence_before_sync();
     __syncthreads();
 }

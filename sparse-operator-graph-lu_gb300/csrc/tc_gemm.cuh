@@ -210,10 +210,28 @@ __device__ __forceinline__ void stage_kmajor(unsigned char* hi_dst, unsigned cha
         *reinterpret_cast<float4*>(lo_dst + kmajor_off(row, k)) = lo;
     }
 }
+// A (x sgn) with the head of row r in operand row 2r and the remainder in
+// 2r + 1, so that one output row's two partial products land in adjacent
+// TMEM lanes of one warp. In each group of 8 lanes, rows 8w..8w+3 store heads
+// while rows 8w+4..8w+7 store remainders and then the other way round: every
+// store instruction hits 8 distinct core-matrix rows (conflict-free).
+__device__ __forceinline__ void stage_a_interleaved(unsigned char* dst, const float* src, float sgn) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, e = lane & 7, ph = lane >> 3;
+    const int row = 8 * warp + e;
+    const bool head_first = e < 4;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int k = 4 * ((e + 4 * ph + j) & 15);
+        float4 hi, lo;
+        split4(*reinterpret_cast<const float4*>(src + row * 64 + k), sgn, hi, lo);
+        *reinterpret_cast<float4*>(dst + kmajor_off(2 * row + (head_first ? 0 : 1), k)) = head_first ? hi : lo;
+        *reinterpret_cast<float4*>(dst + kmajor_off(2 * row + (head_first ? 1 : 0), k)) = head_first ? lo : hi;
+    }
+}
 __device__ __forceinline__ void stage_from_raw(unsigned char* st, const unsigned char* raw, bool trans, float sgn) {
     const float* A = reinterpret_cast<const float*>(raw);
     const float* B = reinterpret_cast<const float*>(raw + RAW_BYTES / 2);
-    stage_kmajor(st, st + A_BYTES / 2, A, sgn);
+    stage_a_interleaved(st, A, sgn);
     if (trans) {
         stage_kmajor(st + A_BYTES, st + A_BYTES + B_BYTES, B, 1.f);
     } else {
