@@ -448,8 +448,17 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
             const int32_t b = (g.pair_b[p] < 0 ? -g.pair_b[p] : g.pair_b[p]) & ~PAIR_TRANS;
             key.push_back({std::max(ready(g.pair_a[p]), ready(b)), p});
         }
-        std::stable_sort(key.begin(), key.end(),
-                         [](const std::pair<double, int32_t>& x, const std::pair<double, int32_t>& y) { return x.first < y.first; });
+        // stable insertion sort: a product has few pairs (at most ~50), and
+        // this avoids a temporary buffer per task
+        for (size_t i = 1; i < key.size(); i++) {
+            const std::pair<double, int32_t> v = key[i];
+            size_t j = i;
+            while (j > 0 && v.first < key[j - 1].first) {
+                key[j] = key[j - 1];
+                j--;
+            }
+            key[j] = v;
+        }
         pa.assign(g.pair_a.begin() + p0, g.pair_a.begin() + p1);
         pb.assign(g.pair_b.begin() + p0, g.pair_b.begin() + p1);
         for (int32_t i = 0; i < p1 - p0; i++) {
