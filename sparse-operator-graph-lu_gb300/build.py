@@ -25,8 +25,8 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRC = ["order.cpp", "planner.cpp", "mtx.cpp", "tasks.cpp", "batch.cpp", "plan_api.cpp", "runtime.cpp", "server.cpp"]
-CUDA_SRC = ["factor.cu", "solve.cu"]
-HEADERS = ["plan.h", "tasks.h", "kernels.h", "api_internal.h"]
+CUDA_SRC = ["factor.cu", "factor_f64.cu", "factor_f32_s1.cu", "factor_f32_s2.cu", "solve.cu"]
+HEADERS = ["plan.h", "tasks.h", "kernels.h", "api_internal.h", "factor_impl.cuh", "factor_units.h", "tc_gemm.cuh"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function", f"-I{CUDA}/include",
             f"-I{ROOT}/include"]
 NVFLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", f"-I{ROOT}/include"]

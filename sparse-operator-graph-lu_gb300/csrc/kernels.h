@@ -1,5 +1,5 @@
 // Launch interface between the host runtime (runtime.cpp) and the sm_103a
-// kernels (factor.cu, solve.cu). Plain structs of device pointers.
+// kernels (factor*.cu, solve.cu). Plain structs of device pointers.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -63,7 +63,7 @@ struct DevTasks {
 // item = task << 4 | part (parts < 8) | ITEM_EARLY
 constexpr int32_t ITEM_EARLY = 8;
 
-// ---- factor (factor.cu) ----
+// ---- factor (factor.cu dispatching to factor_f64.cu / factor_f32_s1.cu / factor_f32_s2.cu) ----
 // tiles: block id -> tiles + id*4096 elements. double => SOG_FP64, float => SOG_MIXED.
 // stages: tensor-core operand stages of the mixed path (1 or 2; ignored for FP64).
 int factor_queue_launch(const DevTasks& t, double* tiles, int grid, int stages, cudaStream_t s);
