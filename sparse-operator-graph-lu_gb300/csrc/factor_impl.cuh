@@ -613,8 +613,9 @@ __device__ void trans_task(const DevTasks& tk, T* __restrict__ tiles, int task, 
 // C = init + sum_p s_p A_p B_p on the tcgen05 tensor cores (tc_gemm.cuh).
 // Thread 0 keeps up to R operand pairs in flight: the TMA copies the raw FP32
 // tiles (contiguous 16 KB each) into a ring of R slots (mbarrier completion).
-// Every warp splits its share of the oldest slot into a stage of
-// [A_hi; A_lo], B_hi^T, B_lo^T and signals the stage's `full` barrier; thread
+// Every warp splits its share of the oldest slot into a stage (A heads and
+// remainders in interleaved rows, B_hi^T, B_lo^T) and signals the stage's
+// `full` barrier; thread
 // 0 then issues that stage's MMAs and refills the slot, while the other warps
 // already stage the next pair (no CTA barrier per pair). Only the first pair's
 // copy latency is exposed. `phase` holds this CTA's mbarrier parities (stages

@@ -3,19 +3,20 @@
 //
 //   C = init + sum_p s_p A_p B_p      (A_p, B_p, C: 64x64 FP32, row-major in HBM)
 //
-// Each operand is split into a TF32 head (rounded to nearest) and the FP32
-// remainder, staged into shared memory in the canonical no-swizzle K-major
-// layout (core matrices of 8 rows x 16 bytes): A as the 128-row stack
-// [A_hi; A_lo], B transposed as B_hi^T and B_lo^T. Per K=8 step two M=128,
-// N=64 MMAs run against the same A stack:
-//   D += [A_hi; A_lo] * B_hi        D += [A_hi; A_lo] * B_lo
-// so D rows 0..63 accumulate A_hi (B_hi + B_lo) and rows 64..127 accumulate
-// A_lo (B_hi + B_lo); the epilogue adds the halves, giving hi*hi + hi*lo +
-// lo*hi (+ the negligible lo*lo). The tensor core reads the TF32 part of each
-// FP32 word, so the remainder enters truncated to TF32 (relative error 2^-22
-// of the element). Two shared-memory stages alternate: pair p+1 is staged
-// while pair p's MMAs run. One thread issues the MMAs and commits them to the
-// stage's mbarrier; every wait is bounded.
+// Operand tiles reach shared memory by TMA bulk copies into a ring of raw
+// slots (mbarrier completion). Each operand is then split into a TF32 head
+// (rounded to nearest) and the FP32 remainder, staged in the canonical
+// no-swizzle K-major layout (core matrices of 8 rows x 16 bytes): A as a
+// 128-row operand with the head of row r in row 2r and its remainder in row
+// 2r + 1, B transposed as the 128-row operand [B_hi^T; B_lo^T]. One M=128,
+// N=128 MMA per K=8 step then accumulates all four split products; output row
+// r's head and remainder parts sit in TMEM lanes 2r and 2r + 1 (one warp), its
+// x B_hi and x B_lo parts in columns c and 64 + c, and the epilogue adds them
+// (hi*hi + hi*lo + lo*hi + the negligible lo*lo). The tensor core reads the
+// TF32 part of each FP32 word, so the remainder enters truncated to TF32
+// (relative error 2^-22 of the element). Two shared-memory stages alternate:
+// pair p+1 is staged while pair p's MMAs run. One thread issues the MMAs and
+// commits them to the stage's mbarrier; every wait is bounded.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -24,7 +25,7 @@ namespace sog {
 namespace tc {
 
 constexpr int ROW_GROUP_BYTES = 8 * 64 * 4;                 // 8 rows x K=64 fp32 = 2048
-constexpr int A_BYTES = 128 / 8 * ROW_GROUP_BYTES;         // [A_hi; A_lo] = 32768
+constexpr int A_BYTES = 128 / 8 * ROW_GROUP_BYTES;         // heads and remainders of A = 32768
 constexpr int B_BYTES = 64 / 8 * ROW_GROUP_BYTES;          // 16384 per part
 constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES;         // 65536
 // operand stages per CTA: 2 (the next pair stages while this one's MMAs run,
@@ -190,8 +191,9 @@ __device__ __forceinline__ void split4(const float4& x, float sgn, float4& hi, f
 }
 
 // Stage one pair from a raw slot holding the row-major A and B tiles (two
-// 1-D copies): A (x sgn) becomes [A_hi; A_lo] in the K-major core-matrix
-// layout; B becomes B_hi^T, B_lo^T, either from the tile's rows (trans: they
+// 1-D copies): A (x sgn) becomes heads and remainders in interleaved rows of
+// the K-major core-matrix layout (stage_a_interleaved); B becomes B_hi^T,
+// B_lo^T, either from the tile's rows (trans: they
 // are the K-major rows of the MMA's B operand) or transposed here. Every
 // shared-memory access is conflict-free. Row-major to core-matrix chunks use
 // a diagonal assignment: in each group of 8 lanes, lane e takes row 8w + e
@@ -251,9 +253,10 @@ __device__ __forceinline__ void stage_from_raw(unsigned char* st, const unsigned
 }
 
 // Issue the 8 MMAs of one staged pair (K = 64 in steps of 8): one M = 128,
-// N = 128 product [A_hi; A_lo] x [B_hi^T; B_lo^T]^T per step (the B halves
-// are adjacent 8-row groups of one K-major operand), so D holds the four
-// products hi.hi | hi.lo over lo.hi | lo.lo.
+// N = 128 product per step of the interleaved A heads/remainders against
+// [B_hi^T; B_lo^T] (the B halves are adjacent 8-row groups of one K-major
+// operand), so D holds all four split products: lanes 2r / 2r + 1 = head /
+// remainder of row r, columns c / 64 + c = x B_hi / x B_lo.
 __device__ __forceinline__ void issue_pair(const unsigned char* st, uint32_t tmem, bool first) {
     const uint32_t base = smem_u32(st);
     constexpr uint32_t idesc = idesc_tf32_m128_n128();
