@@ -206,6 +206,14 @@ __device__ void gemm_f64_quadrant(const DevTasks& tk, double* __restrict__ tiles
 // y, rows at or above it only columns > k, so the halves never collide, and
 // the column operations run on rows the elimination leaves idle.
 __device__ __forceinline__ float fast_rcp(float x) { return __frcp_rn(x); }
+// the hardware reciprocal (within 1 ulp): the FP32 LU's pivot reciprocal is on
+// the per-step critical chain, and the factor's accuracy is refined in FP64
+// anyway (|pivot| >= 1e-9 after the clamp, far from the flush-to-zero range)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ double fast_rcp(double x) { return __drcp_rn(x); }
 
 // LU task (outputs L, U; L^-1 if tk.b, U^-1 if tk.c); with CHOL the LL^T task
@@ -411,7 +419,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_
             const float tiny = 1e-9f;
             const float p = CHOL ? (aik < 1e-20f ? 1e-20f : aik)
                                  : ((aik < tiny && aik > -tiny) ? (aik < 0.f ? -tiny : tiny) : aik);
-            const float rp = __frcp_rn(p);
+            const float rp = rcp_approx(p);
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 float2 o;
