@@ -277,24 +277,36 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
         pptr[t + 1] = pptr[t] + 1 + (g.kind[t] == K_SUB ? 1 : 0) + 2 * (g.pair_ptr[t + 1] - g.pair_ptr[t]);
     std::vector<int32_t> preds(pptr[g.ntasks]);
     g.ndep.assign(g.ntasks, 0);
-    std::vector<int32_t> scount(g.ntasks + 1, 0);
+    // tasks are independent here: their predecessor lists in parallel (the
+    // first malformed read found is reported after the loop)
+    std::string bad;
+#pragma omp parallel for schedule(dynamic, 4096)
     for (int32_t t = 0; t < g.ntasks; t++) {
         int32_t* p = preds.data() + pptr[t];
         int n = 0;
-        auto add = [&](int32_t pt) {
-            if (pt >= 0) p[n++] = pt;
-        };
-        add(prod_of(t, g.a[t]));
-        if (g.kind[t] == K_SUB) add(prod_of(t, g.b[t]));
-        for (int32_t q = g.pair_ptr[t]; q < g.pair_ptr[t + 1]; q++) {
-            add(prod_of(t, g.pair_a[q]));
-            add(prod_of(t, (g.pair_b[q] < 0 ? -g.pair_b[q] : g.pair_b[q]) & ~PAIR_TRANS));
+        try {
+            auto add = [&](int32_t pt) {
+                if (pt >= 0) p[n++] = pt;
+            };
+            add(prod_of(t, g.a[t]));
+            if (g.kind[t] == K_SUB) add(prod_of(t, g.b[t]));
+            for (int32_t q = g.pair_ptr[t]; q < g.pair_ptr[t + 1]; q++) {
+                add(prod_of(t, g.pair_a[q]));
+                add(prod_of(t, (g.pair_b[q] < 0 ? -g.pair_b[q] : g.pair_b[q]) & ~PAIR_TRANS));
+            }
+        } catch (const std::exception& e) {
+#pragma omp critical(sog_tasks_bad)
+            if (bad.empty()) bad = e.what();
+            n = 0;
         }
         std::sort(p, p + n);
         n = (int)(std::unique(p, p + n) - p);
         g.ndep[t] = n;
-        for (int i = 0; i < n; i++) scount[p[i] + 1]++;
     }
+    if (!bad.empty()) throw std::runtime_error(bad);
+    std::vector<int32_t> scount(g.ntasks + 1, 0);
+    for (int32_t t = 0; t < g.ntasks; t++)
+        for (int32_t i = 0; i < g.ndep[t]; i++) scount[preds[pptr[t] + i] + 1]++;
     g.succ_ptr.assign(g.ntasks + 1, 0);
     for (int32_t t = 0; t < g.ntasks; t++) g.succ_ptr[t + 1] = g.succ_ptr[t] + scount[t + 1];
     g.succ.resize(g.succ_ptr[g.ntasks]);
@@ -438,8 +450,11 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
         const int32_t t = block > 0 && block < (int32_t)g.producer.size() ? g.producer[block] : -1;
         return t < 0 ? -1.0 : est[t] + task_cost(g, t, fp64);
     };
+#pragma omp parallel
+    {
     std::vector<std::pair<double, int32_t>> key;
     std::vector<int32_t> pa, pb;
+#pragma omp for schedule(dynamic, 4096)
     for (int32_t t = 0; t < g.ntasks; t++) {
         const int32_t p0 = g.pair_ptr[t], p1 = g.pair_ptr[t + 1];
         if ((g.kind[t] != K_GEMM && g.kind[t] != K_GEMM_LU && g.kind[t] != K_GEMM_LLT) || p1 - p0 < 2) continue;
@@ -465,6 +480,7 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
             g.pair_a[p0 + i] = pa[key[i].second - p0];
             g.pair_b[p0 + i] = pb[key[i].second - p0];
         }
+    }
     }
 }
 
