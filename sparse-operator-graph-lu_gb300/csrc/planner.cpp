@@ -400,9 +400,15 @@ void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>&
         std::vector<Op> sorted(ops.size());
         std::vector<int64_t> pos(start.begin(), start.end() - 1);
         for (const Op& o : ops) sorted[pos[o.stage]++] = o;
+        // small stages one per thread, large ones each with every thread
+        constexpr int64_t BIG = 1 << 18;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : omp_get_max_threads())
         for (int32_t st = 0; st <= maxst; st++)
-            std::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
+            if (start[st + 1] - start[st] < BIG)
+                std::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
+        for (int32_t st = 0; st <= maxst; st++)
+            if (start[st + 1] - start[st] >= BIG)
+                __gnu_parallel::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
         ops.swap(sorted);
     }
     // stages of more than 8000 ops are split (BlockPlanner.cpp:335-354)
