@@ -81,7 +81,16 @@ typedef struct {
     int32_t pipeline_stages; /* SOG_MIXED tensor-core operand stages: 2 (the next product stages while
                                 one computes; 128 KB of shared memory), 1 (64 KB), or 0 = 2, tuned with
                                 SOG_EXEC_AUTO */
-    int32_t reserved[5];
+    int32_t reserved0;
+    double growth_limit;     /* pivot gate (the method does not pivot): the factor call returns SOG_EPIVOT,
+                                with the factors resident and usable, when a system had a pivot clamped, a
+                                diagonal block whose U U^-1 check failed (the reference's inv_check_diag,
+                                MatrixStdDouble.cpp:2871-2937, which it only prints), or a growth
+                                (sog_solve_stats.max_growth) above this limit. 0 = default: 1e8 for SOG_FP64,
+                                1e4 for SOG_MIXED (FP32 factors lose about growth x 6e-8 of relative accuracy;
+                                on SOG_EPIVOT a mixed caller whose refinement does not converge should factor
+                                in SOG_FP64); < 0 = no gate, the reference's clamp-and-continue */
+    int32_t reserved[2];
 } sog_options;
 
 typedef struct {
@@ -90,9 +99,15 @@ typedef struct {
     double rel_resid;        /* ||b - A x||_2 / ||b||_2, worst right-hand side */
     double backward_error;   /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), worst rhs */
     int64_t nan_count;
-    double min_pivot;        /* smallest |u_ii| seen by the last factorisation */
-    int32_t clamped_pivots;  /* pivots raised to +-1e-9 (the reference's clamp) */
-    int32_t reserved[5];
+    double min_pivot;        /* smallest |u_ii| seen by the last factorisation (before the clamp) */
+    int32_t clamped_pivots;  /* pivots raised to +-1e-9 (the reference's clamp; LL^T: 1e-20) */
+    int32_t inv_check_failures; /* diagonal blocks whose U U^-1 diagonal is off 1 by more than 1e-3 or not
+                                   finite (inv_check_diag after upperInv, BlockPlanner.cpp:575-577) */
+    double max_growth;       /* max over diagonal blocks of the largest magnitude its factorisation saw
+                                (the Schur-updated block entering ludcmpSimple, or its U; LL^T: |L|^2)
+                                divided by max |a_ij| of the system: a lower bound on the element
+                                growth factor of the unpivoted factorisation */
+    int32_t reserved[2];
 } sog_solve_stats;
 
 /* Last error message of the calling thread ("" if none). */
@@ -182,7 +197,9 @@ int sog_system_create(sog_ctx *ctx, const sog_plan *plan, const sog_options *opt
 /* bytes of pool this plan needs under opt (for admission decisions) */
 int sog_system_bytes(const sog_plan *plan, const sog_options *opt, uint64_t *bytes);
 /* BlockPlanner::calculate (BlockPlanner.cpp:376-651) on values V (host, the
- * triplet order of sog_plan_build). Returns after the factors are resident. */
+ * triplet order of sog_plan_build). Returns after the factors are resident;
+ * SOG_EPIVOT (factors resident, usable) when a system fails the pivot gate
+ * of sog_options.growth_limit. */
 int sog_factor(sog_system *sys, const double *V);
 /* Same with V already on the device (device pointer). */
 int sog_factor_device(sog_system *sys, const double *V_dev);
@@ -227,6 +244,13 @@ int sog_plan_task_graph_info(const sog_plan *plan, int32_t gemm_split, int64_t *
  * tile-product pairs, GEMM, LU, LINV, UINV, SUB tasks, persistent grid,
  * kernel launches issued by this system so far}. */
 int sog_system_task_info(const sog_system *sys, int64_t *counts);
+/* Pivot statistics of the last factorisation, one entry per system of the
+ * plan (sog_plan_segments): min_pivot, clamped_pivots, inv_check_failures,
+ * max_growth, and status = SOG_EPIVOT for a system that failed the pivot gate
+ * (sog_options.growth_limit), else SOG_OK; the other fields are 0. No
+ * reference counterpart: ludcmpSimple clamps silently
+ * (MatrixStdDouble.cpp:2751-2761) and inv_check_diag only prints. */
+int sog_system_pivots(const sog_system *sys, sog_solve_stats *stats);
 /* Executor configuration in use (after autotuning, the chosen one):
  * SOG_EXEC_*, tensor-core operand stages (mixed), and whether products start
  * before their last producer finished (mixed, static order: 1). */

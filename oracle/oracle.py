@@ -38,6 +38,9 @@ def lib() -> C.CDLL:
         L.oracle_calculate.restype = C.c_int
         L.oracle_solve.argtypes = [C.c_int32, C.c_int64, P, C.c_int64, P, P, P, P]
         L.oracle_solve.restype = C.c_int64
+        L.oracle_solve_lean.argtypes = [C.c_int64, P, C.c_int32, C.c_int32, P, C.c_int32, C.c_int64, P, C.c_int64,
+                                        P, C.c_int32, P, P, C.c_int, P]
+        L.oracle_solve_lean.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -93,17 +96,30 @@ def solve_system(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, stor
 
 
 def solve_system_multi(perm_new_to_old: np.ndarray, n: int, block_rows: int, ops, storage_count, input_tiles, L, U,
-                       B: np.ndarray, threads: int = 0) -> np.ndarray:
+                       B: np.ndarray, threads: int = 0, stats: dict | None = None) -> np.ndarray:
     """One calculate, then one substitution per right-hand side (rows of B,
-    original ordering): the reference's factor-once, solve-each path."""
-    tiles = calculate(ops, storage_count, input_tiles, threads)
-    if len(U) == 0:
-        tiles, U = transposed_upper(L, tiles)
+    original ordering, solved in parallel): the reference's factor-once,
+    solve-each path, with its block lifetime (allocate on first write, free
+    after the last stage that reads a block), so the host memory it needs is
+    the reference's. stats (optional) receives the peak live block count."""
+    ops = np.ascontiguousarray(ops, dtype=np.int32).reshape(-1, 6)
+    L = np.ascontiguousarray(L, dtype=np.int32).reshape(-1, 3)
+    U = np.ascontiguousarray(U, dtype=np.int32).reshape(-1, 3)
+    tin = np.ascontiguousarray(input_tiles, dtype=np.float64)
     B = np.atleast_2d(np.asarray(B, dtype=np.float64))
+    nrhs, n_ext = B.shape[0], block_rows * 64
+    b_ext = np.ones((nrhs, n_ext))
+    b_ext[:, :n] = B[:, perm_new_to_old]
+    x_ext = np.zeros((nrhs, n_ext))
+    peak = C.c_int64(0)
+    rc = lib().oracle_solve_lean(ops.shape[0], ops.ctypes.data, storage_count, tin.shape[0], tin.ctypes.data,
+                                 block_rows, L.shape[0], L.ctypes.data, U.shape[0], U.ctypes.data, nrhs,
+                                 b_ext.ctypes.data, x_ext.ctypes.data, threads, C.byref(peak))
+    if rc < 0:
+        raise RuntimeError(f"oracle_solve_lean failed ({rc})")
+    if stats is not None:
+        stats["peak_blocks"] = int(peak.value)
+        stats["nan"] = int(rc)
     X = np.empty_like(B)
-    for r in range(B.shape[0]):
-        b_ext = np.ones(block_rows * 64)
-        b_ext[:n] = B[r][perm_new_to_old]
-        x_ext, _ = solve(block_rows, L, U, tiles, b_ext)
-        X[r][perm_new_to_old] = x_ext[:n]
+    X[:, perm_new_to_old] = x_ext[:, :n]
     return X

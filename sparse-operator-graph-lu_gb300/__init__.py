@@ -48,13 +48,14 @@ class PlanInfo(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
                 ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("pipeline_stages", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("reserved0", C.c_int32), ("growth_limit", C.c_double), ("reserved", C.c_int32 * 2)]
 
 
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_resid", C.c_double),
                 ("backward_error", C.c_double), ("nan_count", C.c_int64), ("min_pivot", C.c_double),
-                ("clamped_pivots", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("clamped_pivots", C.c_int32), ("inv_check_failures", C.c_int32), ("max_growth", C.c_double),
+                ("reserved", C.c_int32 * 2)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -87,7 +88,7 @@ EXPORTS = [
     "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
     "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
-    "sog_server_destroy", "sog_mtx_read", "sog_mtx_info", "sog_mtx_copy", "sog_mtx_destroy",
+    "sog_server_destroy", "sog_mtx_read", "sog_mtx_info", "sog_mtx_copy", "sog_mtx_destroy", "sog_system_pivots",
 ]
 
 _lib = None
@@ -115,7 +116,8 @@ def lib() -> C.CDLL:
         "sog_solve": ([P, I32, P, P, P], I32), "sog_solve_device": ([P, I32, P, P, P], I32),
         "sog_solve_permuted": ([P, P, P], I32), "sog_system_export_factors": ([P, P, P], I32),
         "sog_system_last_times": ([P, P, P], I32), "sog_system_destroy": ([P], None),
-        "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
+        "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32),
+        "sog_system_pivots": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
         "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
@@ -277,29 +279,50 @@ class System:
 
     def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
                  max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0,
-                 pipeline_stages: int = 0):
+                 pipeline_stages: int = 0, growth_limit: float = 0.0):
+        """growth_limit: the pivot gate (0 = default for the precision, < 0 =
+        off, as the reference); a factorisation that fails it raises
+        SOGError(EPIVOT) unless factor(..., allow_epivot=True)."""
         self.ctx, self.plan = ctx, plan
         self.n = plan.info.n
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
                            gemm_split=gemm_split, solve_lookahead=solve_lookahead,
-                           pipeline_stages=pipeline_stages)
+                           pipeline_stages=pipeline_stages, growth_limit=growth_limit)
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
 
-    def factor(self, vals) -> None:
+    @staticmethod
+    def _factor_rc(rc: int, allow_epivot: bool) -> int:
+        if not (rc == SOG_OK or (allow_epivot and rc == SOG_EPIVOT)):
+            _check(rc)
+        return rc
+
+    def factor(self, vals, allow_epivot: bool = False) -> int:
+        """Factor on host values; returns SOG_OK, or SOG_EPIVOT when allowed
+        (the factors are resident either way)."""
         v = np.ascontiguousarray(vals, dtype=np.float64)
         if v.shape != (self.plan.nnz,):
             raise ValueError(f"values must have shape ({self.plan.nnz},)")
-        _check(lib().sog_factor(self._h, _p(v)))
+        return self._factor_rc(lib().sog_factor(self._h, _p(v)), allow_epivot)
 
-    def factor_device(self, vals_ptr: int) -> None:
-        _check(lib().sog_factor_device(self._h, C.c_void_p(vals_ptr)))
+    def factor_device(self, vals_ptr: int, allow_epivot: bool = False) -> int:
+        return self._factor_rc(lib().sog_factor_device(self._h, C.c_void_p(vals_ptr)), allow_epivot)
 
-    def factor_tiles(self, tiles) -> None:
+    def factor_tiles(self, tiles, allow_epivot: bool = False) -> int:
         t = np.ascontiguousarray(tiles, dtype=np.float64)
         if t.shape != (self.plan.info.n_input, 64, 64):
             raise ValueError(f"tiles must have shape ({self.plan.info.n_input}, 64, 64)")
-        _check(lib().sog_factor_tiles(self._h, _p(t)))
+        return self._factor_rc(lib().sog_factor_tiles(self._h, _p(t)), allow_epivot)
+
+    def pivots(self) -> list[dict]:
+        """Per system of the plan: min_pivot, clamped_pivots,
+        inv_check_failures, max_growth and status (SOG_EPIVOT if it failed
+        the pivot gate) of the last factorisation."""
+        ns = len(self.plan.segments())
+        st = (SolveStats * ns)()
+        _check(lib().sog_system_pivots(self._h, st))
+        keys = ("status", "min_pivot", "clamped_pivots", "inv_check_failures", "max_growth")
+        return [{k: getattr(st[i], k) for k in keys} for i in range(ns)]
 
     def solve(self, b, allow_noconv: bool = False):
         """x (same shape as b: (n,) or (k, n)) and the solve statistics."""
@@ -451,15 +474,16 @@ class Server:
         self._n[rid.value] = (n, bb.shape)
         return rid.value
 
-    def wait(self, rid: int, timeout_ms: float = -1.0, allow_noconv: bool = False):
-        """(x shaped like the submitted b, info dict)."""
+    def wait(self, rid: int, timeout_ms: float = -1.0, allow_noconv: bool = False, allow_epivot: bool = False):
+        """(x shaped like the submitted b, info dict). allow_epivot: return the
+        solution of a system that failed the pivot gate instead of raising."""
         if rid not in self._n:
             raise SOGError(SOG_EINVAL, f"unknown or released request {rid}")
         n, shape = self._n[rid]
         x = np.empty(shape, np.float64)
         info = RequestInfo()
         rc = lib().sog_server_wait(self._h, rid, timeout_ms, _p(x), C.byref(info))
-        if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
+        if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV) or (allow_epivot and rc == SOG_EPIVOT)):
             _check(rc)
         return x, info.as_dict()
 

@@ -216,6 +216,45 @@ __device__ __forceinline__ float rcp_approx(float x) {
 }
 __device__ __forceinline__ double fast_rcp(double x) { return __drcp_rn(x); }
 
+// Pivot statistics of one diagonal-block factorisation, in FP64 off the
+// elimination's critical chain (warp 0, after the CTA barrier that also ORs
+// `bad` over the block): min |pivot| before the clamp, the clamp count, the
+// largest magnitude the task saw (its input block or its factor; LL^T: |L|^2,
+// comparable with the input), and, when the task formed U^-1, the check the
+// reference makes after every upperInv (inv_check_diag, MatrixStdDouble.cpp:
+// 2871-2937, called at BlockPlanner.cpp:575-577): the diagonal of U U^-1
+// within 1e-3 of 1 and no NaN. For triangular U and U^-1 that diagonal is
+// u_ii (U^-1)_ii, and the entries the reference checks below it are exact
+// zeros unless a factor entry is not finite, which `bad` reports. Written to
+// the task's system entry of tk.piv.
+template <typename T, bool CHOL>
+__device__ __forceinline__ void pivot_stats(const DevTasks& tk, int task, const T* raw, const T* piv, const T* rpiv,
+                                            bool check_inv, float maxa, float maxu, bool anybad) {
+    const int lane = threadIdx.x & 31;
+    double mn = 1e300;
+    int cl = 0;
+    bool off = false;
+    for (int k = lane; k < 64; k += 32) {
+        const double v = fabs((double)raw[k]);
+        mn = fmin(mn, v);
+        cl += CHOL ? (double)raw[k] < 1e-20 : v < 1e-9;
+        if (check_inv) off = off || !(fabs((double)piv[k] * (double)rpiv[k] - 1.0) <= 1e-3);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
+        cl += __shfl_xor_sync(FULL, cl, o);
+    }
+    off = __any_sync(FULL, off) || (check_inv && anybad);
+    if (lane == 0) {
+        DevPivot& pv = tk.piv[tk.task_seg ? tk.task_seg[task] : 0];
+        if (cl) atomicAdd(&pv.clamped, cl);
+        if (off) atomicAdd(&pv.inv_fail, 1);
+        atomicMin(&pv.min_pivot_bits, dbits(mn));
+        const double mu = CHOL ? (double)maxu * (double)maxu : (double)maxu;
+        atomicMax(&pv.max_mag_bits, dbits(fmax((double)maxa, mu)));
+    }
+}
+
 // LU task (outputs L, U; L^-1 if tk.b, U^-1 if tk.c); with CHOL the LL^T task
 // of a symmetric tile (lltdcmpSimple, MatrixStdDouble.cpp:2629-2668): the same
 // elimination on the tile symmetrised from its lower triangle, pivots below
@@ -297,8 +336,9 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         }
     }
     T* L = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
-    const int32_t linv = tk.b[task];
+    const int32_t linv = tk.b[task], uinv = CHOL ? 0 : tk.c[task];
     float mu = 0.f;
+    bool bad = false;
     if (CHOL) {
         T* sq = rowbuf;  // sqrt of the pivots (the pivot-row buffers are free now)
         if (tid < 64) sq[tid] = sqrt(piv[tid]);
@@ -326,19 +366,21 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
             const T u = r < c ? a[m] : (r == c ? piv[r] : T(0));
             U[4 * m] = u;
             mu = fmaxf(mu, fabsf((float)u));
+            bad = bad || !isfinite(u);
         }
         if (linv > 0) {
             T* W = tiles + (size_t)linv * 4096 + r * 64 + q;
 #pragma unroll
             for (int m = 0; m < 16; m++) W[4 * m] = q + 4 * m <= r ? y[m] : T(0);
         }
-        const int32_t uinv = tk.c[task];
         if (uinv > 0) {
             T* V = tiles + (size_t)uinv * 4096 + r * 64 + q;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int c = q + 4 * m;
-                V[4 * m] = c >= r ? y[m] * rpiv[c] : T(0);
+                const T v = c >= r ? y[m] * rpiv[c] : T(0);
+                V[4 * m] = v;
+                bad = bad || !isfinite(v);
             }
         }
     }
@@ -350,26 +392,8 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
         atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
         atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
     }
-    __syncthreads();
-    // pivot statistics in FP64, off the elimination's critical chain
-    if (tid < 32) {
-        double mn = 1e300;
-        int cl = 0;
-        for (int k = lane; k < 64; k += 32) {
-            const double v = fabs((double)raw[k]);
-            mn = fmin(mn, v);
-            cl += CHOL ? (double)raw[k] < 1e-20 : v < 1e-9;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
-            cl += __shfl_xor_sync(FULL, cl, o);
-        }
-        if (lane == 0) {
-            if (cl) atomicAdd(&tk.status->clamped, cl);
-            atomicMin(&tk.status->min_pivot_bits, dbits(mn));
-            if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
-        }
-    }
+    const bool anybad = __syncthreads_or(bad) != 0;
+    if (tid < 32) pivot_stats<T, CHOL>(tk, task, raw, piv, rpiv, !CHOL && uinv > 0, s_maxa, s_maxu, anybad);
 }
 
 // FP32 variant of the same elimination with column pairs: thread (r, q) owns
@@ -381,7 +405,7 @@ __device__ void lu_task(const DevTasks& tk, T* __restrict__ tiles, int task, T* 
 // (there is no paired FP64 FMA).
 // blocks: in (source), lo (L), up (U), linv (L^-1, 0 = none), uinv (U^-1, 0 = none)
 template <bool CHOL>
-__device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_t in, int32_t lo, int32_t up,
+__device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int task, int32_t in, int32_t lo, int32_t up,
                            int32_t linv, int32_t uinv, float* sm) {
     float* rowbuf = sm;     // [2][64] published rows
     float* piv = sm + 128;  // [64]
@@ -461,6 +485,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_
     __syncthreads();
     float* L = tiles + (size_t)lo * 4096 + r * 64 + 2 * q;
     float mu = 0.f;
+    bool bad = false;
     if (CHOL) {
         float* sq = rowbuf;
         if (tid < 64) sq[tid] = sqrtf(piv[tid]);
@@ -495,6 +520,7 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_
                                          r < c1 ? a2[m].y : (r == c1 ? piv[r] : 0.f));
             *reinterpret_cast<float2*>(U + 8 * m) = u;
             mu = fmaxf(mu, fmaxf(fabsf(u.x), fabsf(u.y)));
+            bad = bad || !isfinite(u.x) || !isfinite(u.y);
         }
         if (linv > 0) {
             float* W = tiles + (size_t)linv * 4096 + r * 64 + 2 * q;
@@ -509,8 +535,9 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int c0 = 8 * m + 2 * q, c1 = c0 + 1;
-                *reinterpret_cast<float2*>(V + 8 * m) =
-                    make_float2(c0 >= r ? y2[m].x * rpiv[c0] : 0.f, c1 >= r ? y2[m].y * rpiv[c1] : 0.f);
+                const float2 v = make_float2(c0 >= r ? y2[m].x * rpiv[c0] : 0.f, c1 >= r ? y2[m].y * rpiv[c1] : 0.f);
+                *reinterpret_cast<float2*>(V + 8 * m) = v;
+                bad = bad || !isfinite(v.x) || !isfinite(v.y);
             }
         }
     }
@@ -522,25 +549,8 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int32_
         atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
         atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
     }
-    __syncthreads();
-    if (tid < 32) {
-        double mn = 1e300;
-        int cl = 0;
-        for (int k = lane; k < 64; k += 32) {
-            const double v = fabs((double)raw[k]);
-            mn = fmin(mn, v);
-            cl += CHOL ? (double)raw[k] < 1e-20 : v < 1e-9;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            mn = fmin(mn, __shfl_xor_sync(FULL, mn, o));
-            cl += __shfl_xor_sync(FULL, cl, o);
-        }
-        if (lane == 0) {
-            if (cl) atomicAdd(&tk.status->clamped, cl);
-            atomicMin(&tk.status->min_pivot_bits, dbits(mn));
-            if (s_maxa > 0.f) atomicMax(&tk.status->max_growth_bits, dbits((double)s_maxu / (double)s_maxa));
-        }
-    }
+    const bool anybad = __syncthreads_or(bad) != 0;
+    if (tid < 32) pivot_stats<float, CHOL>(tk, task, raw, piv, rpiv, !CHOL && uinv > 0, s_maxa, s_maxu, anybad);
 }
 
 // ---------------------------------------------------------------- triangular inverses
@@ -563,8 +573,6 @@ __device__ void inv_task(const DevTasks& tk, T* __restrict__ tiles, int task, T*
     __syncthreads();
     if (tid < 64) rdiag[tid] = T(1) / M[tid * LD + tid];
     __syncthreads();
-    (void)lane;
-    (void)warp;
 #pragma unroll
     for (int kk = 0; kk < 64; kk++) {
         const int k = LOWER ? kk : 63 - kk;
@@ -588,8 +596,24 @@ __device__ void inv_task(const DevTasks& tk, T* __restrict__ tiles, int task, T*
         }
     }
     T* out = tiles + (size_t)tk.out[task] * 4096 + r * 64 + q;
+    bool bad = false;
 #pragma unroll
-    for (int m = 0; m < 16; m++) out[4 * m] = w[m];
+    for (int m = 0; m < 16; m++) {
+        out[4 * m] = w[m];
+        bad = bad || !isfinite(w[m]);
+    }
+    if (!LOWER) {
+        // inv_check_diag after upperInv (BlockPlanner.cpp:575-577): the
+        // diagonal of U U^-1 is u_kk (U^-1)_kk for triangular factors
+        const bool anybad = __syncthreads_or(bad) != 0;
+        if (warp == 0) {
+            bool off = anybad;
+            for (int k = lane; k < 64; k += 32)
+                off = off || !(fabs((double)M[k * LD + k] * (double)rdiag[k] - 1.0) <= 1e-3);
+            off = __any_sync(FULL, off);
+            if (lane == 0 && off) atomicAdd(&tk.piv[tk.task_seg ? tk.task_seg[task] : 0].inv_fail, 1);
+        }
+    }
 }
 
 // R = A2 - A1; copy / negate when one side is absent (BlockPlanner.cpp:553-572)
@@ -833,12 +857,12 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
             break;
         case K_LU:
             if constexpr (sizeof(T) == 4)
-                lu_task_f2<false>(tk, tiles, tk.a[task], tk.out[task], tk.out2[task], tk.b[task], tk.c[task], sm);
+                lu_task_f2<false>(tk, tiles, task, tk.a[task], tk.out[task], tk.out2[task], tk.b[task], tk.c[task], sm);
             else lu_task<T, false>(tk, tiles, task, sm);
             break;
         case K_LLT:
             if constexpr (sizeof(T) == 4)
-                lu_task_f2<true>(tk, tiles, tk.a[task], tk.out[task], 0, tk.b[task], 0, sm);
+                lu_task_f2<true>(tk, tiles, task, tk.a[task], tk.out[task], 0, tk.b[task], 0, sm);
             else lu_task<T, true>(tk, tiles, task, sm);
             break;
         case K_GEMM_LU:
@@ -846,10 +870,10 @@ __device__ __forceinline__ void run_item(const DevTasks& tk, T* tiles, int task,
             if constexpr (sizeof(T) == 4) {
                 gemm_f32_tc<S>(tk, tiles, task, sm, st, phase, early);  // ends with a CTA barrier
                 if (tk.kind[task] == K_GEMM_LU)
-                    lu_task_f2<false>(tk, tiles, tk.out[task], tk.out3[task], tk.out2[task], tk.b[task], tk.c[task],
-                                      sm);
+                    lu_task_f2<false>(tk, tiles, task, tk.out[task], tk.out3[task], tk.out2[task], tk.b[task],
+                                      tk.c[task], sm);
                 else
-                    lu_task_f2<true>(tk, tiles, tk.out[task], tk.out3[task], 0, tk.b[task], 0, sm);
+                    lu_task_f2<true>(tk, tiles, task, tk.out[task], tk.out3[task], 0, tk.b[task], 0, sm);
             }
             break;
         case K_LINV: inv_task<T, true>(tk, tiles, task, sm); break;

@@ -15,11 +15,17 @@ enum : int32_t {
 
 struct DevStatus {
     int32_t flags;
-    int32_t clamped;                       // pivots clamped to +-1e-9
-    unsigned long long min_pivot_bits;     // min |u_ii| as double bits (non-negative doubles order as integers)
-    unsigned long long max_growth_bits;    // max |u_ij| / max |a_ij| per diagonal block, double bits
     int32_t timeout_where;                 // debugging aid: item index at timeout
-    int32_t pad;
+};
+
+// Pivot statistics of one system's diagonal-block factorisations (one entry
+// per system of a batch). Non-negative doubles order as their bit patterns,
+// so integer atomics keep the minimum / maximum.
+struct DevPivot {
+    unsigned long long min_pivot_bits;  // min |u_ii| before the clamp
+    unsigned long long max_mag_bits;    // max over diagonal blocks of max(|block entering the LU|, |U|) (LL^T: |L|^2)
+    int32_t clamped;                    // pivots raised to the clamp value
+    int32_t inv_fail;                   // blocks whose U U^-1 diagonal is off 1 by more than 1e-3 or not finite
 };
 
 struct DevTasks {
@@ -55,6 +61,9 @@ struct DevTasks {
     // FP64 products skip MMAs of all-zero operand fragments (in-tile sparsity)
     int32_t skip_zero;
     DevStatus* status;
+    // pivot statistics per system; task_seg = system of each task (NULL: one system)
+    DevPivot* piv;
+    const int32_t* task_seg;
     unsigned long long wait_limit_ns;  // bound on any single queue wait
     // optional per-task trace (4 x u64 per task: ready, start, end, sm id), NULL = off
     unsigned long long* trace;
@@ -164,5 +173,11 @@ void residual_seg_launch(const DevCSR& A, const double* b, const double* x, doub
                          double* red, const DevSegs& g, cudaStream_t s);
 // dst = active[system of row] ? (float)src : 0 over n_ext x nc
 void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s);
+
+// max |a| per system over the real rows of the permuted CSR (padding rows
+// skipped) into out[k] as double bits (atomicMax; the caller zeroes out)
+void csr_absmax_seg_launch(const DevCSR& A, const DevSegs& g, unsigned long long* out, cudaStream_t s);
+// max |v[i]| over n values into *out as double bits (atomicMax; the caller zeroes *out)
+void absmax_launch(const double* v, int64_t n, unsigned long long* out, cudaStream_t s);
 
 }  // namespace sog

@@ -157,6 +157,16 @@ struct sog_system {
     int32_t* d_level_items = nullptr;
     int nready = 0;
     DevStatus* d_status0 = nullptr;
+    // pivot statistics per system: working copy, pristine copy, max |a_ij|
+    DevPivot *d_piv = nullptr, *d_piv0 = nullptr;
+    unsigned long long* d_amax = nullptr;
+    bool amax_global = false;  // factored from tiles: one max over all input tiles
+    struct PivotReport {
+        double min_pivot = 0, growth = 0;
+        int32_t clamped = 0, inv_fail = 0;
+        bool tripped = false;
+    };
+    std::vector<PivotReport> piv;
     DevSolve ds{};
     DevCSR csr{};
     double* d_csr_val = nullptr;
@@ -237,9 +247,23 @@ sog_options default_options() {
 DevStatus fresh_status() {
     DevStatus s;
     std::memset(&s, 0, sizeof(s));
-    double inf = INFINITY;
-    std::memcpy(&s.min_pivot_bits, &inf, 8);
     return s;
+}
+
+DevPivot fresh_pivot() {
+    DevPivot p;
+    std::memset(&p, 0, sizeof(p));
+    double inf = INFINITY;
+    std::memcpy(&p.min_pivot_bits, &inf, 8);
+    return p;
+}
+
+// The pivot gate's growth limit: 0 = the default for the precision (FP32
+// factors lose about growth x 6e-8 of relative accuracy, FP64 ones growth x
+// 1.1e-16), < 0 = no gate (the reference's behaviour: clamp and continue).
+double growth_limit(const sog_options& o) {
+    if (o.growth_limit != 0) return o.growth_limit;
+    return o.precision == SOG_FP64 ? 1e8 : 1e4;
 }
 
 double bits_to_double(unsigned long long b) {
@@ -367,6 +391,7 @@ int run_factor_once(sog_system* s) {
         CK(cudaMemcpyAsync(s->dt.queue, s->d_ready0, sizeof(int32_t) * s->nready, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.head, s->d_counters0, sizeof(int32_t) * 3, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.status, s->d_status0, sizeof(DevStatus), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->d_piv, s->d_piv0, sizeof(DevPivot) * s->segs.size(), cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(s->dt.task_done, 0, sizeof(int32_t) * g.ntasks, st));
     (void)fs;
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(unsigned long long) * 4 * g.ntasks, st));
@@ -439,6 +464,59 @@ int run_factor(sog_system* s) {
     s->dt.skip_zero = pick.sparse;
     s->grid_factor = factor_persistent_grid(s->fp64, pick.stages, sms);
     return run_factor_once(s);
+}
+
+// Pivot statistics of the last factorisation per system, and the gate: a
+// system whose pivots were clamped, whose U U^-1 check failed, or whose growth
+// (largest magnitude a diagonal-block factorisation saw / max |a_ij|)
+// exceeded the limit makes the call return SOG_EPIVOT. The factors stay
+// resident and can be used.
+int check_pivots(sog_system* s) {
+    sog_ctx* c = s->ctx;
+    const size_t ns = s->segs.size();
+    std::vector<DevPivot> hp(ns);
+    std::vector<unsigned long long> ha(ns);
+    CK(cudaMemcpyAsync(hp.data(), s->d_piv, sizeof(DevPivot) * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(ha.data(), s->d_amax, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const double lim = growth_limit(s->opt);
+    s->piv.assign(ns, {});
+    int bad = 0;
+    for (size_t k = 0; k < ns; k++) {
+        auto& pr = s->piv[k];
+        pr.min_pivot = bits_to_double(hp[k].min_pivot_bits);
+        if (std::isinf(pr.min_pivot)) pr.min_pivot = 0;  // no diagonal block factored
+        pr.clamped = hp[k].clamped;
+        pr.inv_fail = hp[k].inv_fail;
+        const double mag = bits_to_double(hp[k].max_mag_bits);
+        const double amax = bits_to_double(ha[s->amax_global ? 0 : k]);
+        pr.growth = amax > 0 ? mag / amax : (mag > 0 ? INFINITY : 0.0);
+        pr.tripped = lim > 0 && (pr.clamped > 0 || pr.inv_fail > 0 || !(pr.growth <= lim));
+        bad += pr.tripped;
+    }
+    if (bad) {
+        const auto& p0 = *std::find_if(s->piv.begin(), s->piv.end(), [](const sog_system::PivotReport& r) { return r.tripped; });
+        return fail(SOG_EPIVOT, std::to_string(bad) + " system(s) failed the pivot check (first: " +
+                                    std::to_string(p0.clamped) + " clamped pivots, " + std::to_string(p0.inv_fail) +
+                                    " U*U^-1 check failures, growth " + std::to_string(p0.growth) + " vs limit " +
+                                    std::to_string(lim) + "); the factors are resident");
+    }
+    return SOG_OK;
+}
+
+int factor_checked(sog_system* s) {
+    const int r = run_factor(s);
+    if (r) return r;
+    return check_pivots(s);
+}
+
+void fill_pivot_stats(const sog_system* s, size_t k, sog_solve_stats& st) {
+    if (k >= s->piv.size()) return;
+    const auto& pr = s->piv[k];
+    st.min_pivot = pr.min_pivot;
+    st.clamped_pivots = pr.clamped;
+    st.inv_check_failures = pr.inv_fail;
+    st.max_growth = pr.growth;
 }
 
 int trisolve(sog_system* s, void* vec, int nrhs) {
@@ -566,10 +644,16 @@ int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, d
     }
     sog_solve_stats base;
     std::memset(&base, 0, sizeof(base));
-    base.min_pivot = bits_to_double(s->last.min_pivot_bits);
-    base.clamped_pivots = s->last.clamped;
     std::vector<sog_solve_stats> out(ns, base);
-    s->seg_stats.assign(ns, base);
+    for (size_t k = 0; k < ns; k++) fill_pivot_stats(s, k, out[k]);
+    // the aggregate carries the worst system's pivot figures
+    for (size_t k = 0; k < ns; k++) {
+        if (k == 0 || out[k].min_pivot < base.min_pivot) base.min_pivot = out[k].min_pivot;
+        base.clamped_pivots += out[k].clamped_pivots;
+        base.inv_check_failures += out[k].inv_check_failures;
+        if (!(out[k].max_growth <= base.max_growth)) base.max_growth = out[k].max_growth;
+    }
+    s->seg_stats = out;
     if (agg) *agg = base;
     if (maxr == 0) return SOG_OK;
     int r = ensure_vectors(s, std::min(maxr, 64));
@@ -899,6 +983,24 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (int32_t t = 0; t < g.ntasks; t++) parts32[t] = g.parts[t];
     std::vector<int32_t> counters0 = {0, (int32_t)g.ready_items.size(), 0};
     std::vector<DevStatus> st0 = {fresh_status()};
+    std::vector<DevPivot> piv0(ns, fresh_pivot());
+    // system of each task (batches): through the blocks each op reads, inputs
+    // from their block row; every block of a batch belongs to one system
+    std::vector<int32_t> task_seg;
+    if (ns > 1) {
+        std::vector<int32_t> bseg(storage2, 0);
+        for (int32_t t = 0; t < p.n_input; t++) bseg[t + 1] = seg_brow[p.input_bi[t]];
+        for (const Op& o : ops2) {
+            const int32_t from = o.src > 0 ? bseg[o.src] : (o.src2 > 0 ? bseg[o.src2] : 0);
+            if (o.res > 0) bseg[o.res] = from;
+            if (o.res2 > 0) bseg[o.res2] = from;
+        }
+        task_seg.resize(g.ntasks);
+        for (int32_t t = 0; t < g.ntasks; t++) {
+            const int32_t b = g.kind[t] == K_GEMM_LU || g.kind[t] == K_GEMM_LLT ? g.out3[t] : g.out[t];
+            task_seg[t] = b > 0 && b < storage2 ? bseg[b] : 0;
+        }
+    }
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),
              o_out2 = L.add<int32_t>(g.ntasks), o_a = L.add<int32_t>(g.ntasks), o_b = L.add<int32_t>(g.ntasks),
@@ -925,7 +1027,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()),
              o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
              o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
-             o_done = L.add<int32_t>(g.ntasks),
+             o_done = L.add<int32_t>(g.ntasks), o_piv = L.add<DevPivot>(ns), o_piv0 = L.add<DevPivot>(ns),
+             o_amax = L.add<unsigned long long>(ns), o_tseg = L.add<int32_t>(task_seg.size()),
              o_V = L.add<double>(s->nval), o_vidx = L.add<int32_t>(p.mirror_src.size());
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
@@ -981,6 +1084,12 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     dt.task_done = reinterpret_cast<int32_t*>(A + o_done);
     s->d_status0 = put(A, o_st0, st0, st);
     dt.status = reinterpret_cast<DevStatus*>(A + o_st);
+    s->d_piv0 = put(A, o_piv0, piv0, st);
+    s->d_piv = reinterpret_cast<DevPivot*>(A + o_piv);
+    dt.piv = s->d_piv;
+    s->d_amax = reinterpret_cast<unsigned long long*>(A + o_amax);
+    cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * ns, st);
+    dt.task_seg = task_seg.empty() ? nullptr : put(A, o_tseg, task_seg, st);
     dt.wait_limit_ns = 10ull * 1000 * 1000 * 1000;
     DevSolve& ds = s->ds;
     ds.block_rows = s->R;
@@ -1085,7 +1194,11 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
                           st);
     s->launches++;
     scatter_csr_launch(V_dev, s->d_vidx, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
-    return run_factor(s);
+    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), st));
+    s->launches++;
+    csr_absmax_seg_launch(s->csr, seg_view(s), s->d_amax, st);
+    s->amax_global = false;
+    return factor_checked(s);
 }
 
 int sog_factor(sog_system* s, const double* V) {
@@ -1103,18 +1216,25 @@ int sog_factor_tiles(sog_system* s, const double* tiles) {
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
     const uint64_t n = (uint64_t)s->n_input * 4096;
+    // max |a| over the given tiles, one figure for every system of the plan
+    // (it includes the unit diagonal the planner puts on padding rows)
+    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), c->stream));
+    s->amax_global = true;
     if (s->fp64) {
         CK(cudaMemcpyAsync((double*)s->tiles + 4096, tiles, n * 8, cudaMemcpyHostToDevice, c->stream));
+        s->launches++;
+        absmax_launch((double*)s->tiles + 4096, (int64_t)n, s->d_amax, c->stream);
     } else {
         double* stage = static_cast<double*>(c->pool.alloc(n * 8));
         if (!stage) return fail(SOG_ENOMEM, "block pool exhausted (staging)");
         CK(cudaMemcpyAsync(stage, tiles, n * 8, cudaMemcpyHostToDevice, c->stream));
-        s->launches++;
+        s->launches += 2;
+        absmax_launch(stage, (int64_t)n, s->d_amax, c->stream);
         convert_tiles_launch(stage, (float*)s->tiles + 4096, (int64_t)n, c->stream);
         CK(cudaStreamSynchronize(c->stream));
         c->pool.release(stage, n * 8);
     }
-    return run_factor(s);
+    return factor_checked(s);
 }
 
 int sog_solve_device(sog_system* s, int32_t nrhs, const double* b_dev, double* x_dev, sog_solve_stats* stats) {
@@ -1316,6 +1436,17 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
     return SOG_OK;
 }
 
+int sog_system_pivots(const sog_system* s, sog_solve_stats* stats) {
+    if (!s || !stats) return fail(SOG_EINVAL, "NULL argument");
+    if (!s->factored) return fail(SOG_ESTATE, "no factors");
+    for (size_t k = 0; k < s->segs.size(); k++) {
+        std::memset(&stats[k], 0, sizeof(sog_solve_stats));
+        fill_pivot_stats(s, k, stats[k]);
+        stats[k].status = k < s->piv.size() && s->piv[k].tripped ? SOG_EPIVOT : SOG_OK;
+    }
+    return SOG_OK;
+}
+
 int sog_system_executor(const sog_system* s, int32_t* executor, int32_t* stages, int32_t* early) {
     if (!s || !executor || !stages || !early) return fail(SOG_EINVAL, "bad argument");
     *executor = s->opt.executor;
@@ -1352,6 +1483,7 @@ int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_
     if (r) { sog_plan_destroy(plan); return r; }
     sog_options o = default_options();
     o.precision = precision;
+    o.growth_limit = -1;  // solveLU clamps and continues, as the reference does
     sog_system* s = nullptr;
     r = sog_system_create(c, plan, &o, &s);
     if (!r) {

@@ -203,6 +203,13 @@ int sog_server::run_batch(std::vector<Request*>& group) {
     std::string err;
     const Clock::time_point t0 = Clock::now();
     if (!rc) rc = sog_factor(bt->sys, V.data());
+    // a system that failed the pivot gate is answered with SOG_EPIVOT (and its
+    // solution); the batch's other systems are not affected
+    std::vector<sog_solve_stats> piv;
+    if (rc == SOG_EPIVOT) {
+        piv.resize(group.size());
+        rc = sog_system_pivots(bt->sys, piv.data());
+    }
     if (!rc || rc == SOG_ENOCONV) {
         const int r2 = sog_solve_batch(bt->sys, cnt.data(), B.data(), X.data(), st.data());
         if (!rc) rc = r2;
@@ -226,7 +233,14 @@ int sog_server::run_batch(std::vector<Request*>& group) {
         r->status = (rc == SOG_OK || rc == SOG_ENOCONV || rc == SOG_ENAN) ? st[k].status : rc;
         if (rc && rc != SOG_ENOCONV && rc != SOG_ENAN) r->err = err;
         else if (r->status) r->err = "refinement did not reach the tolerance or the solution is not finite";
-        r->state = r->status == SOG_OK || r->status == SOG_ENOCONV || r->status == SOG_ENAN ? R_DONE : R_FAILED;
+        else if (!piv.empty() && piv[k].status == SOG_EPIVOT) {
+            r->status = SOG_EPIVOT;
+            r->err = "pivot check failed (clamped pivot, U*U^-1 check or growth above the limit); solution returned";
+        }
+        r->state = r->status == SOG_OK || r->status == SOG_ENOCONV || r->status == SOG_ENAN ||
+                           r->status == SOG_EPIVOT
+                       ? R_DONE
+                       : R_FAILED;
         r->seg = (int)k;
         sog_plan_destroy(r->plan);
         r->plan = nullptr;

@@ -393,6 +393,25 @@ __global__ void residual_seg_kernel(DevCSR A, const double* __restrict__ b, cons
         }
     }
 }
+// max |a_ij| per system: one thread per permuted row, a warp's 32 rows lie in
+// one 64-row block row (one system); padding rows skipped
+__global__ void csr_absmax_seg_kernel(DevCSR A, DevSegs g, unsigned long long* out) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row - (threadIdx.x & 31) >= A.n) return;  // whole warp past the end (A.n is a multiple of 64)
+    double m = 0;
+    if (row < A.n && g.n2o[row] >= 0)
+        for (int q = A.ptr[row]; q < A.ptr[row + 1]; q++) m = fmax(m, fabs(A.val[q]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0)
+        atomicMax(out + g.of_brow[row >> 6], (unsigned long long)__double_as_longlong(m));
+}
+__global__ void absmax_kernel(const double* __restrict__ v, int64_t n, unsigned long long* out) {
+    double m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(v[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
 __global__ void cast_seg_kernel(const double* __restrict__ src, float* __restrict__ dst, int n_ext, int nc,
                                 DevSegs g) {
     const int64_t tot = (int64_t)n_ext * nc;
@@ -462,6 +481,12 @@ void residual_seg_launch(const DevCSR& A, const double* b, const double* x, doub
 void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s) {
     if ((int64_t)n_ext * nc > 0) cast_seg_kernel<<<608, 256, 0, s>>>(src, dst, n_ext, nc, g);
 }
+void csr_absmax_seg_launch(const DevCSR& A, const DevSegs& g, unsigned long long* out, cudaStream_t s) {
+    if (A.n > 0) csr_absmax_seg_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A, g, out);
+}
+void absmax_launch(const double* v, int64_t n, unsigned long long* out, cudaStream_t s) {
+    if (n > 0) absmax_kernel<<<608, 256, 0, s>>>(v, n, out);
+}
 
 // ---------------------------------------------------------------- allocation-free residual check
 // The residual kernel's reduction buffer normally comes from the block pool.
@@ -482,6 +507,17 @@ double* g_noalloc_addr[256] = {};  // device address of g_noalloc_red, per devic
 int noalloc_scratch(int dev, double** out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (dev < 0 || dev >= 256) return SOG_EINVAL;
+    if (g_noalloc_addr[dev]) {
+        // a device reset (or a released and recreated primary context) reloads
+        // the module at another address: look it up again when the cached one
+        // is no longer device memory of this context
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, g_noalloc_addr[dev]) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+            at.device != dev) {
+            cudaGetLastError();
+            g_noalloc_addr[dev] = nullptr;
+        }
+    }
     if (!g_noalloc_addr[dev]) {
         double* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_red);
@@ -518,12 +554,18 @@ extern "C" int sog_residual_noalloc(int32_t n, const int32_t* row_ptr, const int
     cudaStream_t s = (cudaStream_t)stream;
     DevCSR A{n, row_ptr, col, val};
     // the array keeps the previous call's sums: clear the part this call accumulates into
-    cudaMemsetAsync(red, 0, sizeof(double) * RED * nrhs, s);
-    residual_kernel<<<(n + 255) / 256, 256, 0, s>>>(A, b, x, r, nrhs, red, n);
+    cudaError_t e = cudaMemsetAsync(red, 0, sizeof(double) * RED * nrhs, s);
+    if (e == cudaSuccess) {
+        residual_kernel<<<(n + 255) / 256, 256, 0, s>>>(A, b, x, r, nrhs, red, n);
+        e = cudaGetLastError();  // a launch that did not start would leave the zeros: a silent perfect residual
+    }
     double host[RED * NOALLOC_MAX_RHS];
-    cudaMemcpyAsync(host, red, sizeof(double) * RED * nrhs, cudaMemcpyDeviceToHost, s);
-    const cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return sog_internal::fail(SOG_ECUDA, std::string("sog_residual_noalloc: ") + cudaGetErrorString(e));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, red, sizeof(double) * RED * nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return sog_internal::fail(SOG_ECUDA, std::string("sog_residual_noalloc: ") + cudaGetErrorString(e));
+    }
     for (int c = 0; c < nrhs; c++) {
         const double* q = host + RED * c;
         rel_resid[c] = q[1] > 0 ? std::sqrt(q[0]) / std::sqrt(q[1]) : std::sqrt(q[0]);

@@ -10,7 +10,8 @@ and stores, per case, in <case>.npz:
   tiles  (small cases) dense L/U tiles in lleaf/uleaf order
   stats  the reference's key=value summary (op counts, stages, phase times)
   ahash  sha256 of the generated triplets, to detect generator drift
-For the 48^3 bench configuration only hashes, counts and x are stored.
+For the large cases (48^3 var-coef, 64^3 Laplacian) only hashes, counts and x
+are stored.
 
 usage: python tests/golden/make_golden.py [case ...]
 """
@@ -61,6 +62,9 @@ def zero_diag_case(wl):
     return s
 
 
+LARGE = ("var3d_48", "lap3d_64")
+
+
 def cases(wl):
     c = {
         "lap2d_32": (lambda: wl.lap2d(32), True),
@@ -73,6 +77,9 @@ def cases(wl):
         "lap2d_8": (lambda: wl.lap2d(8), True),
         "zdiag_600": (lambda: zero_diag_case(wl), False),
         "var3d_48": (lambda: wl.varcoef3d(48), False),
+        # 3D 7-point Laplacian 64^3 (7.1M ops): x for the first right-hand side
+        # of the 64-RHS bench system (same x_true stream, seed 0)
+        "lap3d_64": (lambda: wl.lap3d(64), False),
         # symmetric input: lower triangle given, the reference factors L L^T
         "spd_lap2d_32": (lambda: wl.spd_lower(wl.lap2d(32)), True),
         "spd_var3d_16": (lambda: wl.spd_lower(wl.varcoef3d(16)), False),
@@ -98,7 +105,7 @@ def run_case(wl, name, make, with_tiles, ref_bin, tmp):
                 uleaf=rd("ublk.i32", np.int32).reshape(-1, 3), x=rd("x.f64", np.float64),
                 stats=np.array(stats), ahash=np.array(triplet_hash(s)),
                 daghash=np.array(hashlib.sha256(dag.tobytes()).hexdigest()))
-    if name == "var3d_48":  # large: keep x, hash the structure
+    if name in LARGE:  # keep x, hash the structure
         for k in ("perm", "lleaf", "uleaf"):
             a = arrs.pop(k)
             if k != "perm":  # leaves hashed in (block row, block col) order

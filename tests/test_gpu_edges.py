@@ -9,10 +9,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _solve(sg, n, r, c, v, b, precision, symmetric=False):
+def _solve(sg, n, r, c, v, b, precision, symmetric=False, growth_limit=0.0):
     ctx = sg.Context()
     p = sg.Plan(n, r, c, v, symmetric=symmetric)
-    s = sg.System(ctx, p, precision=precision, max_refine=20, tol=1e-10)
+    s = sg.System(ctx, p, precision=precision, max_refine=20, tol=1e-10, growth_limit=growth_limit)
     s.factor(v)
     x, st = s.solve(b, allow_noconv=True)
     s.close()
@@ -57,9 +57,11 @@ def test_zero_pivot_is_clamped_and_counted(sg):
     1e-9 as ludcmpSimple does; the clamp is reported and b = (2, 2) gives the
     clamped system's solution: 2 for the row ordered first, 0 for the other
     (the ordering may swap them). (A zero leading diagonal would instead be
-    moved by the in-block diagonal sort of the ordering.)"""
+    moved by the in-block diagonal sort of the ordering.) With the pivot gate
+    off (growth_limit < 0) the factorisation is the reference's
+    clamp-and-continue."""
     r = np.array([0, 0, 1, 1]); c = np.array([0, 1, 0, 1]); v = np.ones(4)
-    x, st = _solve(sg, 2, r, c, v, np.array([2.0, 2.0]), sg.FP64)
+    x, st = _solve(sg, 2, r, c, v, np.array([2.0, 2.0]), sg.FP64, growth_limit=-1.0)
     assert st["clamped_pivots"] >= 1 and st["min_pivot"] == 0.0
     assert sorted(x.tolist()) == [0.0, 2.0]
 
@@ -88,7 +90,12 @@ def test_nonfinite_input_is_reported(sg, wl):
     ctx = sg.Context()
     p = sg.Plan(s.n, s.rows, s.cols, v)
     sys_ = sg.System(ctx, p, precision=sg.FP64)
-    sys_.factor(v)
+    # the pivot gate sees the non-finite factor (U U^-1 check) ...
+    with pytest.raises(sg.SOGError, match="EPIVOT"):
+        sys_.factor(v)
+    assert sys_.pivots()[0]["inv_check_failures"] >= 1
+    # ... and a caller that goes on anyway gets the NaNs reported by the solve
+    assert sys_.factor(v, allow_epivot=True) == sg.SOG_EPIVOT
     with pytest.raises(sg.SOGError, match="ENAN"):
         sys_.solve(s.b)
     sys_.close()

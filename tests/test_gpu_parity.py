@@ -151,6 +151,30 @@ def test_bench_config_fp64_vs_reference(sg, wl, ctx):
     sys_.close()
 
 
+def test_north_star_config_64cube(sg, wl, ctx):
+    """3D 7-point Laplacian 64^3 with 64 right-hand sides (the headline
+    configuration, 7.1M unit ops): plain FP64 against the compiled
+    reference's x for the first right-hand side (<= 1e-10; the reference
+    solves one right-hand side) and every column against x_true; mixed +
+    FP64 refinement to a 1e-10 relative residual on every column."""
+    s = wl.lap3d(64, nrhs=64)
+    g = golden("lap3d_64")
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    sys_ = sg.System(ctx, p, precision=sg.FP64)
+    sys_.factor(s.vals)
+    x, st = sys_.solve(s.b)
+    assert st["nan_count"] == 0 and st["backward_error"] < 1e-14
+    assert rel(x[0], g["x"]) <= 1e-10
+    assert max(rel(x[k], s.x_true[k]) for k in range(64)) <= 1e-10
+    sys_.close()
+    sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20)
+    sys_.factor(s.vals)
+    x, st = sys_.solve(s.b)
+    assert st["rel_resid"] <= 1e-10 and st["iterations"] >= 1
+    assert rel(x[0], g["x"]) <= 1e-8
+    sys_.close()
+
+
 @pytest.mark.parametrize("cfg", [(0, 1), (0, 2), (3, 0)], ids=["one-stage", "two-stage", "autotuned"])
 @pytest.mark.parametrize("name", ["lap2d_32", "var3d_16"])
 def test_mixed_pipeline_and_autotune(sg, wl, ctx, name, cfg):

@@ -57,3 +57,30 @@ def test_oracle_detects_planted_error(sg, wl, oracle):
     x, _, _ = oracle.solve_system(g["perm"], s.n, int(stats["block_rows"]), dag, int(stats["storage_count"]),
                                   p.input_tiles(s.vals), g["lleaf"], g["uleaf"], s.b)
     assert np.linalg.norm(x - g["x"]) / np.linalg.norm(g["x"]) > 1e-6
+
+
+@pytest.mark.parametrize("name", ["lap2d_32", "var3d_16", "cd_17", "band_3000", "zdiag_600", "spd_lap2d_32",
+                                  "spd_var3d_16"])
+def test_oracle_lean_path_matches_flat_and_reference(sg, wl, oracle, name):
+    """The reference's block lifetime in the oracle (lazy allocation, free
+    after the last reading stage; solve_system_multi) gives bit for bit the
+    flat-array result on the reference's own DAG, and holds fewer blocks than
+    the DAG names."""
+    s = golden_cases(wl)[name]()
+    g = golden(name)
+    plan = sg.Plan(s.n, s.rows, s.cols, s.vals, symmetric=s.symmetric)
+    tiles_in = plan.input_tiles(s.vals)
+    stats = dict(l.split("=") for l in str(g["stats"]).split())
+    R, sc = int(stats["block_rows"]), int(stats["storage_count"])
+    b = rhs_of(s)
+    x_flat, _, _ = oracle.solve_system(g["perm"], s.n, R, g["dag"], sc, tiles_in, g["lleaf"], g["uleaf"], b)
+    st = {}
+    B = np.stack([b, 2.0 * b, -b])
+    X = oracle.solve_system_multi(g["perm"], s.n, R, g["dag"], sc, tiles_in, g["lleaf"], g["uleaf"], B, stats=st)
+    assert st["nan"] == 0
+    np.testing.assert_array_equal(X[0], x_flat)
+    assert np.linalg.norm(X[0] - g["x"]) / np.linalg.norm(g["x"]) <= 1e-12
+    # columns are independent solves: a scaled right-hand side scales x (up to rounding)
+    np.testing.assert_allclose(X[1], 2.0 * X[0], rtol=0, atol=1e-12 * np.abs(X[0]).max())
+    np.testing.assert_allclose(X[2], -X[0], rtol=0, atol=1e-12 * np.abs(X[0]).max())
+    assert 0 < st["peak_blocks"] < sc

@@ -57,6 +57,23 @@ def test_plan_48cube_matches_reference_hashes(sg, wl):
                            "mulneg": 160873}
 
 
+def test_plan_64cube_matches_reference_hashes(sg, wl):
+    """The headline configuration (3D 7-point Laplacian 64^3, 7.1M ops):
+    full-size DAG identity with the reference's."""
+    s = wl.lap3d(64)
+    g = golden("lap3d_64")
+    assert triplet_hash(s) == str(g["ahash"])
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    assert _sha(perm) == str(g["permhash"])
+    assert _sha(ops) == str(g["daghash"])
+    assert _sha(L) == str(g["lleafhash"]) and _sha(U) == str(g["uleafhash"])
+    info = p.info_dict()
+    stats = dict(l.split("=") for l in str(g["stats"]).split())
+    assert info["nops"] == 7106089 and info["stages"] == int(stats["stages"])
+    assert info["block_rows"] == int(stats["block_rows"]) and info["storage_count"] == int(stats["storage_count"])
+
+
 def test_config_rounding(sg, wl):
     # block rows = next power of two strictly above n/64 (config.cpp:30-49)
     for side, br in ((8, 2), (16, 8), (32, 32), (128, 512)):
