@@ -81,7 +81,9 @@ typedef struct {
     int32_t pipeline_stages; /* SOG_MIXED tensor-core operand stages: 2 (the next product stages while
                                 one computes; 128 KB of shared memory), 1 (64 KB), or 0 = 2, tuned with
                                 SOG_EXEC_AUTO */
-    int32_t reserved0;
+    int32_t max_ctas;        /* 0 = the whole GPU; else at most this many CTAs for the persistent factor and
+                                the substitution launches, so that systems running on other streams
+                                (sog_system_set_stream) share the SMs */
     double growth_limit;     /* pivot gate (the method does not pivot): the factor call returns SOG_EPIVOT,
                                 with the factors resident and usable, when a system had a pivot clamped, a
                                 diagonal block whose U U^-1 check failed (the reference's inv_check_diag,
@@ -206,6 +208,13 @@ int sog_factor_device(sog_system *sys, const double *V_dev);
 /* BlockPlanner::calculate with input tiles given directly (host,
  * n_input x 64 x 64 row-major FP64, block id k+1 at index k). */
 int sog_factor_tiles(sog_system *sys, const double *tiles);
+/* Run this system's kernels and copies on the caller's stream (a
+ * cudaStream_t; NULL = the context's stream again), e.g. several systems of
+ * one context factored concurrently from different host threads, each on its
+ * own stream (the block pool is shared and locked). Waits for the system's
+ * work on its previous stream first. No reference counterpart (one system per
+ * process, main.cpp). */
+int sog_system_set_stream(sog_system *sys, void *stream);
 /* Solve with the resident factors. b and x are host arrays of nrhs right-hand
  * sides, each of length n, in the ORIGINAL ordering (rhs-major: b[r*n + i]).
  * Replaces BlockPlanner::solve + GOrder::reOrderResult (BlockPlanner.cpp:834,
@@ -310,13 +319,18 @@ int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_
  * No counterpart in the reference (one system per process, main.cpp). A
  * request loop with continuous batching: sog_server_submit copies a request
  * (COO system as for sog_plan_build, nrhs right-hand sides rhs-major) and
- * returns at once; host worker threads plan it; one scheduler thread owns the
- * context and, whenever the GPU is free, admits every planned request that
- * the block pool can hold (first come, first served, sog_system_bytes as the
- * estimate), merges them into one batch plan, factors them in one executor
- * launch and solves all their right-hand sides together. Requests that arrive
- * while a batch runs join the next one. A request larger than the whole pool
- * fails with SOG_ENOMEM; one that fits once others are released waits.
+ * returns at once; host worker threads plan it; a scheduler thread admits
+ * the planned requests that the block pool can hold (first come, first
+ * served, sog_system_bytes as the estimate) to the first free lane, merged
+ * into one batch plan. A lane (a host thread and a CUDA stream) factors its
+ * batch in one executor launch and solves all its right-hand sides together.
+ * Lanes run concurrently: a request that arrives while another batch is on
+ * the GPU starts at once on a free lane, its kernels beside the other batch's
+ * (each batch's persistent grid is sized to its parallelism, at most three
+ * quarters of the GPU while there are other lanes). A request larger than the
+ * whole pool fails with SOG_ENOMEM; one that fits once others are released
+ * waits. A system that fails the pivot gate (sog_options.growth_limit) is
+ * answered with SOG_EPIVOT and its solution.
  * Factors stay resident after the answer (sog_server_solve for further
  * right-hand sides) until sog_server_release. The context must not be used
  * directly while a server runs on it. */
@@ -325,7 +339,7 @@ typedef struct {
     int32_t planner_threads;      /* host planning workers (0 = 2) */
     int32_t planner_omp_threads;  /* OpenMP threads per plan (0 = default) */
     int32_t max_batch;            /* requests merged into one launch at most (0 = 256) */
-    int32_t reserved0;
+    int32_t lanes;                /* batches on the GPU at the same time, each on its own stream (0 = 2) */
     double batch_window_ms;       /* once a request is planned, wait up to this long for requests
                                      still being planned to join its launch (0 = launch at once) */
     int32_t reserved[2];

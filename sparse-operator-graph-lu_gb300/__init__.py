@@ -48,7 +48,7 @@ class PlanInfo(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
                 ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("pipeline_stages", C.c_int32),
-                ("reserved0", C.c_int32), ("growth_limit", C.c_double), ("reserved", C.c_int32 * 2)]
+                ("max_ctas", C.c_int32), ("growth_limit", C.c_double), ("reserved", C.c_int32 * 2)]
 
 
 class SolveStats(C.Structure):
@@ -63,7 +63,7 @@ class SolveStats(C.Structure):
 
 class ServerOptions(C.Structure):
     _fields_ = [("planner_threads", C.c_int32), ("planner_omp_threads", C.c_int32), ("max_batch", C.c_int32),
-                ("reserved0", C.c_int32), ("batch_window_ms", C.c_double), ("reserved", C.c_int32 * 2)]
+                ("lanes", C.c_int32), ("batch_window_ms", C.c_double), ("reserved", C.c_int32 * 2)]
 
 
 class RequestInfo(C.Structure):
@@ -89,6 +89,7 @@ EXPORTS = [
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
     "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
     "sog_server_destroy", "sog_mtx_read", "sog_mtx_info", "sog_mtx_copy", "sog_mtx_destroy", "sog_system_pivots",
+    "sog_system_set_stream",
 ]
 
 _lib = None
@@ -117,7 +118,7 @@ def lib() -> C.CDLL:
         "sog_solve_permuted": ([P, P, P], I32), "sog_system_export_factors": ([P, P, P], I32),
         "sog_system_last_times": ([P, P, P], I32), "sog_system_destroy": ([P], None),
         "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32),
-        "sog_system_pivots": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
+        "sog_system_pivots": ([P, P], I32), "sog_system_set_stream": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
         "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
@@ -279,7 +280,7 @@ class System:
 
     def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
                  max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0,
-                 pipeline_stages: int = 0, growth_limit: float = 0.0):
+                 pipeline_stages: int = 0, growth_limit: float = 0.0, max_ctas: int = 0):
         """growth_limit: the pivot gate (0 = default for the precision, < 0 =
         off, as the reference); a factorisation that fails it raises
         SOGError(EPIVOT) unless factor(..., allow_epivot=True)."""
@@ -288,7 +289,7 @@ class System:
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
                            gemm_split=gemm_split, solve_lookahead=solve_lookahead,
-                           pipeline_stages=pipeline_stages, growth_limit=growth_limit)
+                           pipeline_stages=pipeline_stages, growth_limit=growth_limit, max_ctas=max_ctas)
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
 
     @staticmethod
@@ -313,6 +314,10 @@ class System:
         if t.shape != (self.plan.info.n_input, 64, 64):
             raise ValueError(f"tiles must have shape ({self.plan.info.n_input}, 64, 64)")
         return self._factor_rc(lib().sog_factor_tiles(self._h, _p(t)), allow_epivot)
+
+    def set_stream(self, stream: int) -> None:
+        """Run this system on the given cudaStream_t (0 = the context's)."""
+        _check(lib().sog_system_set_stream(self._h, C.c_void_p(stream or None)))
 
     def pivots(self) -> list[dict]:
         """Per system of the plan: min_pivot, clamped_pivots,
@@ -451,12 +456,13 @@ class Server:
     resident until release."""
 
     def __init__(self, ctx: Context, precision: int = MIXED, max_refine: int = 10, tol: float = 1e-10,
-                 planners: int = 2, omp_threads: int = 0, max_batch: int = 0, batch_window_ms: float = 0.0):
+                 planners: int = 2, omp_threads: int = 0, max_batch: int = 0, batch_window_ms: float = 0.0,
+                 lanes: int = 0):
         self.ctx = ctx
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=EXEC_PERSISTENT, max_refine=max_refine, tol=tol)
         self.sopt = ServerOptions(planner_threads=planners, planner_omp_threads=omp_threads, max_batch=max_batch,
-                                  batch_window_ms=batch_window_ms)
+                                  batch_window_ms=batch_window_ms, lanes=lanes)
         self._n = {}
         _check(lib().sog_server_create(ctx._h, C.byref(self.opt), C.byref(self.sopt), C.byref(self._h)))
 

@@ -32,6 +32,9 @@ uint64_t round256(uint64_t b) { return (b + 255) & ~255ull; }
 
 // Chunked first-fit arena over cudaMalloc'd chunks; freed ranges coalesce.
 struct Pool {
+    // systems of one context may run on several host threads (each on its own
+    // stream), so the arena is locked
+    std::mutex mu;
     struct Chunk {
         char* base;
         uint64_t size;
@@ -41,6 +44,7 @@ struct Pool {
     std::vector<Chunk> chunks;
 
     void* alloc(uint64_t bytes) {
+        std::lock_guard<std::mutex> lk(mu);
         bytes = round256(std::max<uint64_t>(bytes, 256));
         for (auto& c : chunks)
             for (auto it = c.free_.begin(); it != c.free_.end(); ++it)
@@ -69,6 +73,7 @@ struct Pool {
     }
     void release(void* ptr, uint64_t bytes) {
         if (!ptr) return;
+        std::lock_guard<std::mutex> lk(mu);
         bytes = round256(std::max<uint64_t>(bytes, 256));
         char* p = static_cast<char*>(ptr);
         for (auto& c : chunks) {
@@ -93,6 +98,7 @@ struct Pool {
     }
     // give chunks without allocations back to the device
     void trim() {
+        std::lock_guard<std::mutex> lk(mu);
         std::vector<Chunk> keep;
         for (auto& c : chunks) {
             if (c.free_.size() == 1 && c.free_.begin()->first == 0 && c.free_.begin()->second == c.size) {
@@ -105,6 +111,7 @@ struct Pool {
         chunks.swap(keep);
     }
     void destroy() {
+        std::lock_guard<std::mutex> lk(mu);
         for (auto& c : chunks) cudaFree(c.base);
         chunks.clear();
         reserved = used = 0;
@@ -134,6 +141,10 @@ struct sog_ctx {
 
 struct sog_system {
     sog_ctx* ctx = nullptr;
+    // every kernel and copy of this system: the context's stream unless the
+    // caller gave the system one of its own (sog_system_set_stream)
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     sog_options opt{};
     bool fp64 = true, imported = false, symmetric = false;
     int n = 0, n_ext = 0, R = 0, n_input = 0;
@@ -378,9 +389,17 @@ int check_status(sog_system* s, bool factor) {
     return SOG_OK;
 }
 
+// persistent factor grid: every co-resident CTA, or at most sog_options.max_ctas
+// (a system sharing the GPU with others; the executors need no particular
+// residency: the claimant of the smallest unfinished position always runs)
+int factor_grid(const sog_system* s, int stages) {
+    const int g = factor_persistent_grid(s->fp64, stages, s->ctx->num_sms);
+    return s->opt.max_ctas > 0 ? std::min(g, s->opt.max_ctas) : g;
+}
+
 int run_factor_once(sog_system* s) {
     sog_ctx* c = s->ctx;
-    cudaStream_t st = c->stream;
+    cudaStream_t st = s->stream;
     const TaskGraph& g = s->tg;
     DevStatus fs = fresh_status();
     // reset working state from pristine copies
@@ -395,7 +414,7 @@ int run_factor_once(sog_system* s) {
     CK(cudaMemsetAsync(s->dt.task_done, 0, sizeof(int32_t) * g.ntasks, st));
     (void)fs;
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(unsigned long long) * 4 * g.ntasks, st));
-    CK(cudaEventRecord(c->e0, st));
+    CK(cudaEventRecord(s->e0, st));
     int rc = 0;
     if (s->opt.executor == SOG_EXEC_LEVELS) {
         for (int l = 0; l < g.nlevels && rc == 0; l++) {
@@ -414,9 +433,9 @@ int run_factor_once(sog_system* s) {
         s->launches++;
     }
     if (rc) return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
-    CK(cudaEventRecord(c->e1, st));
+    CK(cudaEventRecord(s->e1, st));
     CK(cudaStreamSynchronize(st));
-    CK(cudaEventElapsedTime(&s->t_factor, c->e0, c->e1));
+    CK(cudaEventElapsedTime(&s->t_factor, s->e0, s->e1));
     int r = check_status(s, true);
     if (r) return r;
     s->factored = true;
@@ -446,7 +465,7 @@ int run_factor(sog_system* s) {
         s->stages = c.stages;
         s->dt.early = !s->fp64 && c.early && !s->poisoned;
         s->dt.skip_zero = c.sparse;
-        s->grid_factor = factor_persistent_grid(s->fp64, c.stages, sms);
+        s->grid_factor = factor_grid(s, c.stages);
         for (int rep = 0; rep < 2; rep++) {
             const int r = run_factor_once(s);
             if (r) return r;
@@ -462,7 +481,7 @@ int run_factor(sog_system* s) {
     s->early = pick.early;
     s->dt.early = !s->fp64 && pick.early && !s->poisoned;
     s->dt.skip_zero = pick.sparse;
-    s->grid_factor = factor_persistent_grid(s->fp64, pick.stages, sms);
+    s->grid_factor = factor_grid(s, pick.stages);
     return run_factor_once(s);
 }
 
@@ -476,9 +495,9 @@ int check_pivots(sog_system* s) {
     const size_t ns = s->segs.size();
     std::vector<DevPivot> hp(ns);
     std::vector<unsigned long long> ha(ns);
-    CK(cudaMemcpyAsync(hp.data(), s->d_piv, sizeof(DevPivot) * ns, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(ha.data(), s->d_amax, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpyAsync(hp.data(), s->d_piv, sizeof(DevPivot) * ns, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(ha.data(), s->d_amax, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     const double lim = growth_limit(s->opt);
     s->piv.assign(ns, {});
     int bad = 0;
@@ -522,10 +541,11 @@ void fill_pivot_stats(const sog_system* s, size_t k, sog_solve_stats& st) {
 int trisolve(sog_system* s, void* vec, int nrhs) {
     sog_ctx* c = s->ctx;
     const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));  // positions per row
-    const int grid = std::min(s->R * nch, trisolve_grid(s->fp64, nrhs, c->num_sms));
+    int grid = std::min(s->R * nch, trisolve_grid(s->fp64, nrhs, c->num_sms));
+    if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
     int nl = 0;
-    int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, c->stream, nl)
-                     : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, c->stream, nl);
+    int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, s->stream, nl)
+                     : trisolve_launch(s->ds, (const float*)s->tiles, (float*)vec, nrhs, s->epoch, grid, s->stream, nl);
     s->launches += nl;
     if (rc) return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     return SOG_OK;
@@ -537,8 +557,8 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
 int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
     sog_ctx* c = s->ctx;
     const size_t ns = s->segs.size();
-    CK(cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED * nc * ns, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED * nc * ns, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     rel.assign(ns, 0.0);
     for (size_t k = 0; k < ns; k++) {
         sog_solve_stats& ss = s->seg_stats[k];
@@ -563,7 +583,7 @@ int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
 // leaves their iterates bit for bit unchanged.
 int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chunk_stats) {
     sog_ctx* c = s->ctx;
-    cudaStream_t st = c->stream;
+    cudaStream_t st = s->stream;
     const int64_t ne = (int64_t)s->n_ext * nc;
     const size_t ns = s->segs.size();
     const DevSegs g = seg_view(s);
@@ -631,7 +651,7 @@ int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chu
 int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, double* x_dev,
                       sog_solve_stats* agg) {
     sog_ctx* c = s->ctx;
-    cudaStream_t st = c->stream;
+    cudaStream_t st = s->stream;
     const size_t ns = s->segs.size();
     int maxr = 0;
     int64_t off = 0;
@@ -662,7 +682,7 @@ int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, d
     CK(cudaMemcpyAsync(s->d_seg_voff, s->h_voff, sizeof(int64_t) * ns, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->d_cnt, 0, sizeof(unsigned long long) * ns, st));
     const DevSegs g = seg_view(s);
-    CK(cudaEventRecord(c->e0, st));
+    CK(cudaEventRecord(s->e0, st));
     for (int c0 = 0; c0 < maxr; c0 += 64) {
         const int nc = std::min(64, maxr - c0);
         s->launches++;
@@ -672,10 +692,10 @@ int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, d
         s->launches++;
         scatter_seg_launch(s->d_xext, g, s->n_ext, c0, nc, x_dev, s->d_cnt, st);
     }
-    CK(cudaEventRecord(c->e1, st));
+    CK(cudaEventRecord(s->e1, st));
     CK(cudaMemcpyAsync(s->h_cnt, s->d_cnt, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    CK(cudaEventElapsedTime(&s->t_solve, c->e0, c->e1));
+    CK(cudaEventElapsedTime(&s->t_solve, s->e0, s->e1));
     int worst = SOG_OK;
     for (size_t k = 0; k < ns; k++) {
         out[k].nan_count = (int64_t)s->h_cnt[k];
@@ -715,13 +735,13 @@ int solve_host(sog_system* s, const int32_t* nrhs, const double* b, double* x, s
         return fail(SOG_ENOMEM, "block pool exhausted (rhs)");
     }
     int r = SOG_OK;
-    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
         r = fail(SOG_ECUDA, "rhs upload failed");
     if (!r) {
         r = solve_device_impl(s, nrhs, db, dx, agg);
         if (!r || r == SOG_ENOCONV || r == SOG_ENAN) {
-            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-                cudaStreamSynchronize(c->stream) != cudaSuccess)
+            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+                cudaStreamSynchronize(s->stream) != cudaSuccess)
                 r = fail(SOG_ECUDA, "download failed");
         }
     }
@@ -731,6 +751,16 @@ int solve_host(sog_system* s, const int32_t* nrhs, const double* b, double* x, s
 }
 
 }  // namespace
+
+double sog_internal::system_parallelism(const sog_system* s, int* full_grid) {
+    if (full_grid) *full_grid = factor_persistent_grid(s->fp64, s->stages, s->ctx->num_sms);
+    return (double)s->tg.ntasks / std::max(1, s->tg.nlevels);
+}
+
+void sog_internal::system_set_grid_cap(sog_system* s, int cap) {
+    s->opt.max_ctas = cap > 0 ? cap : 0;
+    s->grid_factor = factor_grid(s, s->stages);
+}
 
 extern "C" {
 
@@ -821,6 +851,12 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     const Plan& p = plan->p;
     sog_system* s = new sog_system();
     s->ctx = c;
+    s->stream = c->stream;
+    if (cudaEventCreate(&s->e0) != cudaSuccess || cudaEventCreate(&s->e1) != cudaSuccess) {
+        cudaGetLastError();
+        sog_system_destroy(s);
+        return fail(SOG_ECUDA, "system events");
+    }
     s->opt = o;
     s->fp64 = o.precision == SOG_FP64;
     s->imported = plan->imported;
@@ -1043,7 +1079,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         delete s;
         return fail(SOG_ENOMEM, "block pool exhausted (task tables)");
     }
-    cudaStream_t st = c->stream;
+    cudaStream_t st = s->stream;
     char* A = s->aux;
     DevTasks& dt = s->dt;
     dt.ntasks = g.ntasks;
@@ -1151,7 +1187,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
             s->tune_pending = true;
         }
     }
-    s->grid_factor = factor_persistent_grid(s->fp64, s->stages, c->num_sms);
+    s->grid_factor = factor_grid(s, s->stages);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         std::string m = cudaGetErrorString(cudaGetLastError());
         sog_system_destroy(s);
@@ -1165,7 +1201,7 @@ void sog_system_destroy(sog_system* s) {
     if (!s) return;
     sog_ctx* c = s->ctx;
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(s->stream);
     c->pool.release(s->tiles, s->tiles_bytes);
     c->pool.release(s->aux, s->aux_bytes);
     c->pool.release(s->vecs, s->vec_bytes);
@@ -1175,7 +1211,17 @@ void sog_system_destroy(sog_system* s) {
     if (s->h_active) cudaFreeHost(s->h_active);
     if (s->h_voff) cudaFreeHost(s->h_voff);
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
+    if (s->e0) cudaEventDestroy(s->e0);
+    if (s->e1) cudaEventDestroy(s->e1);
     delete s;
+}
+
+int sog_system_set_stream(sog_system* s, void* stream) {
+    if (!s) return fail(SOG_EINVAL, "NULL system");
+    CK(cudaSetDevice(s->ctx->device));
+    CK(cudaStreamSynchronize(s->stream));  // the system's work so far, on the stream it was issued to
+    s->stream = stream ? (cudaStream_t)stream : s->ctx->stream;
+    return SOG_OK;
 }
 
 int sog_factor_device(sog_system* s, const double* V_dev) {
@@ -1184,7 +1230,7 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
     if (!V_dev && s->ntrip) return fail(SOG_EINVAL, "NULL values");
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
+    cudaStream_t st = s->stream;
     const uint64_t eb = elem_bytes(s->opt);
     CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
     // input tile k (0-based, as the scatter map counts) is block id k+1
@@ -1207,7 +1253,7 @@ int sog_factor(sog_system* s, const double* V) {
     if (!V && s->nval) return fail(SOG_EINVAL, "NULL values");
     CK(cudaSetDevice(s->ctx->device));
     if (s->nval)
-        CK(cudaMemcpyAsync(s->d_V, V, sizeof(double) * s->nval, cudaMemcpyHostToDevice, s->ctx->stream));
+        CK(cudaMemcpyAsync(s->d_V, V, sizeof(double) * s->nval, cudaMemcpyHostToDevice, s->stream));
     return sog_factor_device(s, s->d_V);
 }
 
@@ -1218,20 +1264,20 @@ int sog_factor_tiles(sog_system* s, const double* tiles) {
     const uint64_t n = (uint64_t)s->n_input * 4096;
     // max |a| over the given tiles, one figure for every system of the plan
     // (it includes the unit diagonal the planner puts on padding rows)
-    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), c->stream));
+    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), s->stream));
     s->amax_global = true;
     if (s->fp64) {
-        CK(cudaMemcpyAsync((double*)s->tiles + 4096, tiles, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync((double*)s->tiles + 4096, tiles, n * 8, cudaMemcpyHostToDevice, s->stream));
         s->launches++;
-        absmax_launch((double*)s->tiles + 4096, (int64_t)n, s->d_amax, c->stream);
+        absmax_launch((double*)s->tiles + 4096, (int64_t)n, s->d_amax, s->stream);
     } else {
         double* stage = static_cast<double*>(c->pool.alloc(n * 8));
         if (!stage) return fail(SOG_ENOMEM, "block pool exhausted (staging)");
-        CK(cudaMemcpyAsync(stage, tiles, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(stage, tiles, n * 8, cudaMemcpyHostToDevice, s->stream));
         s->launches += 2;
-        absmax_launch(stage, (int64_t)n, s->d_amax, c->stream);
-        convert_tiles_launch(stage, (float*)s->tiles + 4096, (int64_t)n, c->stream);
-        CK(cudaStreamSynchronize(c->stream));
+        absmax_launch(stage, (int64_t)n, s->d_amax, s->stream);
+        convert_tiles_launch(stage, (float*)s->tiles + 4096, (int64_t)n, s->stream);
+        CK(cudaStreamSynchronize(s->stream));
         c->pool.release(stage, n * 8);
     }
     return factor_checked(s);
@@ -1284,21 +1330,21 @@ int sog_solve_permuted(sog_system* s, const double* b_ext, double* x_ext) {
     int r = ensure_vectors(s, 1);
     if (r) return r;
     const uint64_t ne = (uint64_t)s->n_ext;
-    CK(cudaMemcpyAsync(s->d_xext, b_ext, ne * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaEventRecord(c->e0, c->stream));
+    CK(cudaMemcpyAsync(s->d_xext, b_ext, ne * 8, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaEventRecord(s->e0, s->stream));
     if (s->fp64) {
         if ((r = trisolve(s, s->d_xext, 1))) return r;
     } else {
         s->launches++;
-        cast_f64_to_f32_launch(s->d_xext, s->d_v32, ne, c->stream);
+        cast_f64_to_f32_launch(s->d_xext, s->d_v32, ne, s->stream);
         if ((r = trisolve(s, s->d_v32, 1))) return r;
         s->launches++;
-        axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 1, c->stream);
+        axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 1, s->stream);
     }
-    CK(cudaEventRecord(c->e1, c->stream));
-    CK(cudaMemcpyAsync(x_ext, s->d_xext, ne * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    CK(cudaEventElapsedTime(&s->t_solve, c->e0, c->e1));
+    CK(cudaEventRecord(s->e1, s->stream));
+    CK(cudaMemcpyAsync(x_ext, s->d_xext, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaEventElapsedTime(&s->t_solve, s->e0, s->e1));
     return check_status(s, false);
 }
 
@@ -1363,7 +1409,7 @@ int sog_system_trace_enable(sog_system* s, int32_t on) {
     if (!s) return fail(SOG_EINVAL, "NULL system");
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaStreamSynchronize(s->stream));
     if (!on) {
         c->pool.release(s->trace, s->trace_bytes);
         s->trace = nullptr;
@@ -1384,7 +1430,7 @@ int sog_system_trace_enable(sog_system* s, int32_t on) {
 int sog_system_trace_get(sog_system* s, uint64_t* task_trace, uint64_t* row_trace, int32_t* task_kind) {
     if (!s || !s->trace) return fail(SOG_ESTATE, "trace not enabled");
     CK(cudaSetDevice(s->ctx->device));
-    CK(cudaStreamSynchronize(s->ctx->stream));
+    CK(cudaStreamSynchronize(s->stream));
     if (task_trace)
         CK(cudaMemcpy(task_trace, s->trace, sizeof(uint64_t) * 4 * s->tg.ntasks, cudaMemcpyDeviceToHost));
     if (row_trace)

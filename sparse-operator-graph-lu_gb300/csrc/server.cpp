@@ -2,15 +2,19 @@
 //
 // No counterpart in the reference, which solves one system per process
 // (main.cpp, solver.cpp:121). Requests (a sparse system and its right-hand
-// sides) are planned on host worker threads as they arrive; one scheduler
-// thread owns the device context and, whenever the GPU is free, admits every
-// planned request that the block pool can hold (first come, first served),
-// merges their plans into one batch plan, factors them in one executor launch
-// and solves all their right-hand sides in shared substitution launches.
-// Requests that arrive while a batch is on the GPU are planned meanwhile and
-// join the next batch as soon as the GPU and pool memory free up. Factors stay
-// resident after the answer, for further right-hand sides, until the request
-// is released; a batch's pool memory returns when all its requests are.
+// sides) are planned on host worker threads as they arrive. A scheduler
+// thread admits planned requests (first come, first served, as far as the
+// block pool can hold them) to the first free lane, merging those that are
+// waiting into one batch plan. Each lane is a host thread with its own CUDA
+// stream: it factors its batch in one executor launch and solves all the
+// batch's right-hand sides in shared substitution launches. Lanes run at the
+// same time, so a request that arrives while another batch is on the GPU
+// starts on a free lane at once and its kernels run beside the other
+// batch's; each batch's persistent grid is sized to its task graph's
+// parallelism and, while other lanes exist, leaves a quarter of the GPU to
+// them. Factors stay resident after the answer, for further right-hand sides,
+// until the request is released; a batch's pool memory returns when all its
+// requests are.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -22,6 +26,8 @@
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "api_internal.h"
 
@@ -85,6 +91,14 @@ struct SolveJob {
 }  // namespace
 
 struct sog_server {
+    // a host thread and stream that run one batch at a time
+    struct Lane {
+        std::thread th;
+        cudaStream_t stream = nullptr;
+        std::vector<Request*> group;  // assigned by the scheduler, taken by the lane
+        bool busy = false;
+        uint64_t reserved = 0;  // pool bytes promised to its group until its system exists
+    };
     sog_ctx* ctx = nullptr;
     sog_options opt{};
     sog_server_options sopt{};
@@ -99,6 +113,10 @@ struct sog_server {
     std::vector<std::shared_ptr<Batch>> dead;  // batches whose requests are all released
     std::vector<std::thread> planners;
     std::thread sched;
+    std::vector<Lane> lanes;
+    std::condition_variable cv_lane;  // lanes wait here for a group
+    uint64_t reserved_total = 0;      // sum of the lanes' reservations
+    bool mem_blocked = false;         // a lone request waits for pool memory held by resident requests
     // counters
     int64_t batches = 0, admitted = 0, completed = 0, rejected = 0;
     int64_t max_batch_seen = 0;
@@ -106,10 +124,11 @@ struct sog_server {
 
     void planner_loop();
     void scheduler_loop();
+    void lane_loop(int k);
     // 0 = ran (or failed for good); 1 = too little pool memory: retry with the
     // group shrunk to its first half; 2 = single request blocked on memory
     // held by resident requests: wait for a release
-    int run_batch(std::vector<Request*>& group);
+    int run_batch(std::vector<Request*>& group, int lane);
     bool any_resident() const {
         for (auto& kv : reqs)
             if (kv.second->batch) return true;
@@ -159,15 +178,30 @@ void sog_server::planner_loop() {
     }
 }
 
-int sog_server::run_batch(std::vector<Request*>& group) {
+int sog_server::run_batch(std::vector<Request*>& group, int lane) {
     auto bt = std::make_shared<Batch>();
     std::vector<const sog_plan*> plans;
     for (Request* r : group) plans.push_back(r->plan);
     int rc = sog_plan_merge(plans.data(), (int32_t)plans.size(), &bt->plan);
     if (!rc) rc = sog_system_create(ctx, bt->plan, &opt, &bt->sys);
-    if (rc == SOG_ENOMEM) {
+    if (rc == SOG_ENOMEM) {  // chunks left empty by released batches go back to the device first
         sog_ctx_trim(ctx);
         rc = sog_system_create(ctx, bt->plan, &opt, &bt->sys);
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu);  // the system exists (or failed): its pool use is counted now
+        reserved_total -= lanes[lane].reserved;
+        lanes[lane].reserved = 0;
+    }
+    if (!rc) {
+        // this lane's stream; a grid for the batch's parallelism, leaving a
+        // quarter of the GPU to the other lanes
+        rc = sog_system_set_stream(bt->sys, lanes[lane].stream);
+        int full = 0;
+        const double par = sog_internal::system_parallelism(bt->sys, &full);
+        int cap = std::max(16, (int)(3.0 * par));
+        if (lanes.size() > 1) cap = std::min(cap, std::max(1, 3 * full / 4));
+        sog_internal::system_set_grid_cap(bt->sys, cap < full ? cap : 0);
     }
     if (rc == SOG_ENOMEM) {
         std::lock_guard<std::mutex> lk(mu);
@@ -182,12 +216,16 @@ int sog_server::run_batch(std::vector<Request*>& group) {
             group.resize(keep);
             return 1;
         }
-        // memory still held by resident requests, or by released batches the
-        // scheduler has not freed yet: wait for it instead of failing
-        if (any_resident() || !dead.empty()) {
+        // memory still held by resident requests, by released batches the
+        // scheduler has not freed yet, or by other lanes' batches: wait for it
+        // instead of failing
+        bool others = false;
+        for (size_t k = 0; k < lanes.size(); k++) others = others || ((int)k != lane && lanes[k].busy);
+        if (any_resident() || !dead.empty() || others) {
             group[0]->state = R_PLANNED;
             planned.push_front(group[0]);
             group.clear();
+            mem_blocked = true;
             return 2;
         }
     }
@@ -213,6 +251,12 @@ int sog_server::run_batch(std::vector<Request*>& group) {
     if (!rc || rc == SOG_ENOCONV) {
         const int r2 = sog_solve_batch(bt->sys, cnt.data(), B.data(), X.data(), st.data());
         if (!rc) rc = r2;
+    }
+    // further solves on these factors (sog_server_solve, scheduler thread) run
+    // on the context's stream, beside the lanes
+    if (bt->sys) {
+        sog_internal::system_set_grid_cap(bt->sys, 0);
+        sog_system_set_stream(bt->sys, nullptr);
     }
     if (rc) err = sog_last_error();
     const Clock::time_point t1 = Clock::now();
@@ -259,22 +303,56 @@ int sog_server::run_batch(std::vector<Request*>& group) {
     return 0;
 }
 
-void sog_server::scheduler_loop() {
+void sog_server::lane_loop(int k) {
     for (;;) {
         std::vector<Request*> group;
-        std::vector<std::shared_ptr<Batch>> to_free;
-        SolveJob* job = nullptr;
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return stop || !planned.empty() || !jobs.empty() || !dead.empty(); });
+            cv_lane.wait(lk, [&] { return stop || !lanes[k].group.empty(); });
+            if (stop) return;
+            group.swap(lanes[k].group);
+        }
+        int rb;
+        while ((rb = run_batch(group, k)) == 1) {
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            reserved_total -= lanes[k].reserved;
+            lanes[k].reserved = 0;
+            lanes[k].busy = false;
+            if (rb != 2) mem_blocked = false;  // this lane's memory use is settled: a blocked request may fit
+        }
+        cv_work.notify_all();
+    }
+}
+
+void sog_server::scheduler_loop() {
+    for (;;) {
+        std::vector<std::shared_ptr<Batch>> to_free;
+        SolveJob* job = nullptr;
+        int lane = -1;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            auto free_lane = [&] {
+                for (size_t k = 0; k < lanes.size(); k++)
+                    if (!lanes[k].busy) return (int)k;
+                return -1;
+            };
+            cv_work.wait(lk, [&] {
+                return stop || !jobs.empty() || !dead.empty() ||
+                       (!planned.empty() && !mem_blocked && free_lane() >= 0);
+            });
             if (stop) return;
             to_free.swap(dead);
+            if (!to_free.empty()) mem_blocked = false;  // memory returns: a blocked request may fit now
             if (!jobs.empty()) {
                 job = jobs.front();
                 jobs.pop_front();
+            } else if (!planned.empty() && !mem_blocked) {
+                lane = free_lane();
             }
         }
-        to_free.clear();  // destroys systems: only this thread touches the context
+        to_free.clear();  // destroys systems (on the context's stream)
         if (job) {
             Request* r = job->r;
             int32_t ns = 0;
@@ -293,62 +371,63 @@ void sog_server::scheduler_loop() {
             cv_done.notify_all();
             continue;
         }
-        {
-            std::unique_lock<std::mutex> lk(mu);
+        if (lane < 0) continue;
+        std::unique_lock<std::mutex> lk(mu);
+        if (planned.empty() || lanes[lane].busy) continue;
+        // batching window: give requests still being planned a chance to
+        // join this launch
+        if (sopt.batch_window_ms > 0) {
+            const Clock::time_point until =
+                planned.front()->t_planned +
+                std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double, std::milli>(
+                    sopt.batch_window_ms));
+            cv_work.wait_until(lk, until, [&] { return stop || (to_plan.empty() && planning == 0); });
+            if (stop) return;
             if (planned.empty()) continue;
-            // batching window: give requests still being planned a chance to
-            // join this launch
-            if (sopt.batch_window_ms > 0) {
-                const Clock::time_point until =
-                    planned.front()->t_planned +
-                    std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double, std::milli>(
-                        sopt.batch_window_ms));
-                cv_work.wait_until(lk, until, [&] { return stop || (to_plan.empty() && planning == 0); });
-                if (stop) return;
-            }
-            uint64_t used = 0, total = 0;
-            sog_ctx_pool_usage(ctx, &used, &total);
-            uint64_t avail = total > used ? total - used : 0, need = 0;
-            const int cap = sopt.max_batch > 0 ? sopt.max_batch : 256;
-            while (!planned.empty() && (int)group.size() < cap) {
-                Request* r = planned.front();
-                if (need + r->bytes > avail) break;
-                need += r->bytes;
-                group.push_back(r);
+        }
+        uint64_t used = 0, total = 0;
+        sog_ctx_pool_usage(ctx, &used, &total);
+        const uint64_t taken = used + reserved_total;
+        uint64_t avail = total > taken ? total - taken : 0, need = 0;
+        const int cap = sopt.max_batch > 0 ? sopt.max_batch : 256;
+        std::vector<Request*> group;
+        while (!planned.empty() && (int)group.size() < cap) {
+            Request* r = planned.front();
+            if (need + r->bytes > avail) break;
+            need += r->bytes;
+            group.push_back(r);
+            planned.pop_front();
+        }
+        if (group.empty()) {
+            Request* r = planned.front();
+            bool others = false;
+            for (auto& ln : lanes) others = others || ln.busy;
+            if (!any_resident() && dead.empty() && !others) {
+                // larger than the whole pool: refuse it rather than wait forever
                 planned.pop_front();
+                r->state = R_FAILED;
+                r->status = SOG_ENOMEM;
+                r->err = "request does not fit in the block pool";
+                r->t_done = Clock::now();
+                sog_plan_destroy(r->plan);
+                r->plan = nullptr;
+                rejected++;
+                cv_done.notify_all();
+            } else {
+                mem_blocked = true;  // until a batch is freed or a lane finishes
             }
-            if (group.empty()) {
-                Request* r = planned.front();
-                if (!any_resident() && dead.empty()) {
-                    // larger than the whole pool: refuse it rather than wait forever
-                    planned.pop_front();
-                    r->state = R_FAILED;
-                    r->status = SOG_ENOMEM;
-                    r->err = "request does not fit in the block pool";
-                    r->t_done = Clock::now();
-                    sog_plan_destroy(r->plan);
-                    r->plan = nullptr;
-                    rejected++;
-                    cv_done.notify_all();
-                } else {
-                    // wait for a release to free pool memory
-                    cv_work.wait(lk, [&] { return stop || !dead.empty() || !jobs.empty(); });
-                }
-                continue;
-            }
-            for (Request* r : group) {
-                r->state = R_RUNNING;
-                r->t_start = Clock::now();
-            }
-            admitted += (int64_t)group.size();
+            continue;
         }
-        int rb;
-        while ((rb = run_batch(group)) == 1) {
+        for (Request* r : group) {
+            r->state = R_RUNNING;
+            r->t_start = Clock::now();
         }
-        if (rb == 2) {
-            std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return stop || !dead.empty() || !jobs.empty(); });
-        }
+        admitted += (int64_t)group.size();
+        lanes[lane].busy = true;
+        lanes[lane].reserved = need;
+        reserved_total += need;
+        lanes[lane].group.swap(group);
+        cv_lane.notify_all();
     }
 }
 
@@ -368,8 +447,19 @@ int sog_server_create(sog_ctx* ctx, const sog_options* opt, const sog_server_opt
     }
     if (sopt) s->sopt = *sopt;
     const int np = s->sopt.planner_threads > 0 ? s->sopt.planner_threads : 2;
+    const int nl = s->sopt.lanes > 0 ? s->sopt.lanes : 2;
+    s->lanes.resize(nl);
+    for (auto& ln : s->lanes)
+        if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto& l2 : s->lanes)
+                if (l2.stream) cudaStreamDestroy(l2.stream);
+            delete s;
+            return fail(SOG_ECUDA, "server lane streams");
+        }
     try {
         for (int k = 0; k < np; k++) s->planners.emplace_back([s] { s->planner_loop(); });
+        for (int k = 0; k < nl; k++) s->lanes[k].th = std::thread([s, k] { s->lane_loop(k); });
         s->sched = std::thread([s] { s->scheduler_loop(); });
     } catch (const std::exception& e) {
         {
@@ -377,7 +467,11 @@ int sog_server_create(sog_ctx* ctx, const sog_options* opt, const sog_server_opt
             s->stop = true;
         }
         s->cv_work.notify_all();
+        s->cv_lane.notify_all();
         for (auto& t : s->planners) t.join();
+        for (auto& ln : s->lanes)
+            if (ln.th.joinable()) ln.th.join();
+        for (auto& ln : s->lanes) cudaStreamDestroy(ln.stream);
         delete s;
         return fail(SOG_EINVAL, std::string("server threads: ") + e.what());
     }
@@ -498,8 +592,16 @@ void sog_server_destroy(sog_server* s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
+    s->cv_lane.notify_all();
     for (auto& t : s->planners) t.join();
     if (s->sched.joinable()) s->sched.join();
+    // a lane finishes the batch it is running (its requests are answered)
+    for (auto& ln : s->lanes)
+        if (ln.th.joinable()) ln.th.join();
+    for (auto& ln : s->lanes) {
+        cudaStreamSynchronize(ln.stream);
+        cudaStreamDestroy(ln.stream);
+    }
     // in-flight work ends with the scheduler; drop the resident batches
     s->dead.clear();
     for (auto& kv : s->reqs) {

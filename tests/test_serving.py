@@ -131,3 +131,45 @@ def test_symmetric_request_in_a_mixed_batch(sg, wl):
     srv.release(g)
     srv.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_arrival_overlaps_running_batch(sg, wl, precision):
+    """A small request that arrives while a large batch is already on the GPU
+    starts on a free lane and is answered before the large one, with the
+    same result it gets alone (FP64 bit for bit, mixed within the refinement
+    tolerance)."""
+    import time
+    prec = sg.FP64 if precision == "fp64" else sg.MIXED
+    big = wl.varcoef3d(40)
+    small = wl.random_band(2400, seed=5, nrhs=2)
+    ctx = sg.Context()
+    alone = {}
+    for name, s in (("big", big), ("small", small)):
+        p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+        sysm = sg.System(ctx, p, precision=prec, max_refine=10)
+        sysm.factor(s.vals)
+        alone[name], _ = sysm.solve(s.b)
+        sysm.close()
+    srv = sg.Server(ctx, precision=prec, planners=2, lanes=2)
+    rb = srv.submit(big.n, big.rows, big.cols, big.vals, big.b)
+    t0 = time.time()
+    while srv.counters()["admitted"] < 1:  # the big request has been handed to a lane
+        assert time.time() - t0 < 60
+        time.sleep(0.001)
+    rs = srv.submit(small.n, small.rows, small.cols, small.vals, small.b)
+    xs, info_s = srv.wait(rs)
+    # the small one is answered while the big one is still running
+    with pytest.raises(sg.SOGError, match="ETIMEOUT"):
+        srv.wait(rb, timeout_ms=0)
+    xb, info_b = srv.wait(rb)
+    assert info_s["batch_id"] != info_b["batch_id"] and info_s["batch_size"] == 1
+    for x, key in ((xs, "small"), (xb, "big")):
+        if precision == "fp64":
+            np.testing.assert_array_equal(x, alone[key])
+        else:
+            assert np.linalg.norm(x - alone[key]) <= 1e-9 * np.linalg.norm(alone[key])
+    srv.release(rs)
+    srv.release(rb)
+    srv.close()
+    ctx.close()
