@@ -154,15 +154,43 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         __syncwarp();
         return !*(volatile int*)&s_stop;
     };
-    // this warp's share of a row's early blocks (all but those left to the
-    // look-ahead products): partial sums for output rows 2 lane, 2 lane + 1
-    auto early = [&](int i, int first_warp, int skip1, int skip2, int skip3, int c0, T (&pa)[NR], T (&pb)[NR]) -> bool {
+    // pa/pb += the lane's two rows of block B times the staged slice
+    auto block_product = [&](const T* B, T (&pa)[NR], T (&pb)[NR]) {
+#pragma unroll 4
+        for (int c = 0; c < 64; c += VW) {
+            const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
 #pragma unroll
-        for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
-        const int q0 = ptr[i], q1 = ptr[i + 1];
-        for (int q = q0 + ((warp - first_warp) & 7); q < q1; q += 8) {
+            for (int v = 0; v < VW; v++)
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    const T y = yw[(c + v) * NR + r];
+                    pa[r] += b0.v[v] * y;
+                    pb[r] += b1.v[v] * y;
+                }
+        }
+    };
+    // this warp's share of the position's early blocks (all but those left to
+    // the look-ahead products): both rows' blocks in one walk, in the order
+    // their operands become ready (lower: ascending column, upper:
+    // descending), every 8th to this warp, so the blocks that depend on the
+    // most recent rows come last for both rows. Partial sums for output rows
+    // 2 lane, 2 lane + 1 of row a (xa, za) and of row b (xb, zb).
+    auto early = [&](int ia, int ib, int sa1, int sa2, int sb1, int sb2, int sb3, int c0, T (&xa)[NR], T (&za)[NR],
+                     T (&xb)[NR], T (&zb)[NR]) -> bool {
+#pragma unroll
+        for (int r = 0; r < NR; r++) xa[r] = za[r] = xb[r] = zb[r] = T(0);
+        int qa = ptr[ia], qb = ib >= 0 ? ptr[ib] : 0;
+        const int qa1 = ptr[ia + 1], qb1 = ib >= 0 ? ptr[ib + 1] : 0;
+        int idx = 0;
+        while (qa < qa1 || qb < qb1) {
+            bool from_a;
+            if (qa >= qa1) from_a = false;
+            else if (qb >= qb1) from_a = true;
+            else from_a = lower ? col[qa] <= col[qb] : col[qa] >= col[qb];
+            const int q = from_a ? qa++ : qb++;
             const int j = col[q];
-            if (j == skip1 || j == skip2 || j == skip3) continue;
+            if (from_a ? (j == sa1 || j == sa2) : (j == sb1 || j == sb2 || j == sb3)) continue;
+            if ((idx++ & 7) != warp) continue;
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
             // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
 #pragma unroll
@@ -180,18 +208,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 }
             }
             __syncwarp();
-#pragma unroll 4
-            for (int c = 0; c < 64; c += VW) {
-                const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
-#pragma unroll
-                for (int v = 0; v < VW; v++)
-#pragma unroll
-                    for (int r = 0; r < NR; r++) {
-                        const T y = yw[(c + v) * NR + r];
-                        pa[r] += b0.v[v] * y;
-                        pb[r] += b1.v[v] * y;
-                    }
-            }
+            if (from_a) block_product(B, xa, za);
+            else block_product(B, xb, zb);
             __syncwarp();
         }
         return true;
@@ -216,26 +234,20 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         const int n1 = ia + dir, n2 = ia + 2 * dir;  // the previous rows: a's first and second neighbours
         bool stop = false;
         {
-            T pa[NR], pb[NR];
-            // row a: all but its first two neighbours (when they have products)
-            if (!early(ia, 0, m1a ? n1 : -2, m2a ? n2 : -2, -2, c0, pa, pb)) stop = true;
+            T xa[NR], za[NR], xb[NR], zb[NR];
+            // row a: all but its first two neighbours (when they have
+            // products); row b: all but a and a's first two neighbours
+            if (!early(ia, ib, m1a ? n1 : -2, m2a ? n2 : -2, m1b ? ia : -2, m2b ? n1 : -2, m3b ? n2 : -2, c0, xa, za, xb,
+                       zb))
+                stop = true;
             T* pw = part + warp * NV;
+            T* pw2 = part + (8 + warp) * NV;
 #pragma unroll
             for (int r = 0; r < NR; r++) {
-                pw[(2 * lane) * NR + r] = pa[r];
-                pw[(2 * lane + 1) * NR + r] = pb[r];
-            }
-            if (ib >= 0 && !stop) {
-                // row b: all but a, a's first and second neighbours; its warps
-                // continue where row a's blocks ended
-                const int nqa = ptr[ia + 1] - ptr[ia];
-                if (!early(ib, nqa & 7, m1b ? ia : -2, m2b ? n1 : -2, m3b ? n2 : -2, c0, pa, pb)) stop = true;
-                pw = part + (8 + warp) * NV;
-#pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    pw[(2 * lane) * NR + r] = pa[r];
-                    pw[(2 * lane + 1) * NR + r] = pb[r];
-                }
+                pw[(2 * lane) * NR + r] = xa[r];
+                pw[(2 * lane + 1) * NR + r] = za[r];
+                pw2[(2 * lane) * NR + r] = xb[r];
+                pw2[(2 * lane + 1) * NR + r] = zb[r];
             }
         }
         __syncthreads();
@@ -281,19 +293,26 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 }
             }
         }
-        // y -= M y_n over this lane's 16 columns of M's row and of y_n's slice
-        auto apply = [&](int m, int n, T (&yp)[NR]) {
-            const T* M = tiles + (size_t)m * 4096 + row * 64 + cb;
+        // ypa -= Ma y_n, ypb -= Mb y_n over this lane's 16 columns of the
+        // products' rows and of y_n's slice, loaded once for both
+        auto apply = [&](int ma, int mb, int n) {
+            const T* Ma = tiles + (size_t)ma * 4096 + row * 64 + cb;
+            const T* Mb = tiles + (size_t)mb * 4096 + row * 64 + cb;
             const T* vn = vec + ((size_t)n * 64 + cb) * ld + c0;
 #pragma unroll
             for (int c = 0; c < 16; c += VW) {
-                const Vec16<T> mv = ldg16(M + c);
+                Vec16<T> va, vb;
+                if (ma) va = ldg16(Ma + c);
+                if (mb) vb = ldg16(Mb + c);
 #pragma unroll
                 for (int v = 0; v < VW; v++) {
                     T yn[NR];
                     load_row<T, NR>(vn + (size_t)(c + v) * ld, vec16, yn);
 #pragma unroll
-                    for (int r = 0; r < NR; r++) yp[r] -= mv.v[v] * yn[r];
+                    for (int r = 0; r < NR; r++) {
+                        if (ma) ypa[r] -= va.v[v] * yn[r];
+                        if (mb) ypb[r] -= vb.v[v] * yn[r];
+                    }
                 }
             }
         };
@@ -305,10 +324,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         bool ok = !(m1a || m2b) || wait_row(n1);
         ok = ok && (!(m2a || m3b) || wait_row(n2));
         if (ok) {
-            if (m1a) apply(m1a, n1, ypa);
-            if (m2a) apply(m2a, n2, ypa);
-            if (m2b) apply(m2b, n1, ypb);
-            if (m3b) apply(m3b, n2, ypb);
+            if (m1a || m2b) apply(m1a, m2b, n1);
+            if (m2a || m3b) apply(m2a, m3b, n2);
         }
 #pragma unroll
         for (int r = 0; r < NR; r++) {
