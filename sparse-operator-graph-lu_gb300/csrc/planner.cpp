@@ -408,7 +408,8 @@ void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>&
                 std::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
         for (int32_t st = 0; st <= maxst; st++)
             if (start[st + 1] - start[st] >= BIG)
-                __gnu_parallel::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
+                __gnu_parallel::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder(),
+                                     __gnu_parallel::default_parallel_tag(threads > 0 ? threads : omp_get_max_threads()));
         ops.swap(sorted);
     }
     // stages of more than 8000 ops are split (BlockPlanner.cpp:335-354)
@@ -500,7 +501,8 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < (int64_t)I.size(); k++) keys[k] = (int64_t)(I[k] >> 6) * R + (J[k] >> 6);
         std::vector<int64_t> uk(keys);
-        __gnu_parallel::sort(uk.begin(), uk.end());
+        __gnu_parallel::sort(uk.begin(), uk.end(), std::less<int64_t>(),
+                             __gnu_parallel::default_parallel_tag(threads > 0 ? threads : omp_get_max_threads()));
         uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
         for (int64_t key : uk) {
             int32_t lf = fz.leaf_at(froot, (int)(key / R), (int)(key % R));
@@ -537,7 +539,8 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
             p.scatter_off[k] = (int16_t)((I[k] & 63) * 64 + (J[k] & 63));
             slot[k] = {(int64_t)p.scatter_tile[k] * 4096 + p.scatter_off[k], (int32_t)k};
         }
-        __gnu_parallel::sort(slot.begin(), slot.end());
+        __gnu_parallel::sort(slot.begin(), slot.end(), std::less<std::pair<int64_t, int32_t>>(),
+                             __gnu_parallel::default_parallel_tag(threads > 0 ? threads : omp_get_max_threads()));
         for (int64_t k = 0; k + 1 < nt; k++)
             if (slot[k].first == slot[k + 1].first) p.scatter_tile[slot[k].second] = -1;
     }

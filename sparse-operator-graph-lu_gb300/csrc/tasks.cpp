@@ -280,6 +280,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     // tasks are independent here: their predecessor lists in parallel (the
     // first malformed read found is reported after the loop)
     std::string bad;
+    int32_t bad_task = -1;  // the smallest task with a malformed input (deterministic report)
 #pragma omp parallel for schedule(dynamic, 4096)
     for (int32_t t = 0; t < g.ntasks; t++) {
         int32_t* p = preds.data() + pptr[t];
@@ -296,7 +297,10 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
             }
         } catch (const std::exception& e) {
 #pragma omp critical(sog_tasks_bad)
-            if (bad.empty()) bad = e.what();
+            if (bad_task < 0 || t < bad_task) {
+                bad = e.what();
+                bad_task = t;
+            }
             n = 0;
         }
         std::sort(p, p + n);
