@@ -109,20 +109,19 @@ struct DevSolve {
     unsigned long long wait_limit_ns;
     // optional trace (4 x u64 per block row: lower start/end, upper start/end), NULL = off
     unsigned long long* trace;
-    // positions dealt to CTAs for the lower / upper solve, in order: each one
-    // block row, or two consecutive rows of one system (x = the first, y = the
-    // second in solve order, -1 = none), solved by the same CTA. Every row's
-    // dependencies come at earlier positions. Batches interleave their
+    // optional dealing order of block rows to CTAs (position -> block row) for
+    // the lower / upper solve; NULL = ascending / descending rows. Every row's
+    // dependencies must come at earlier positions. Batches interleave their
     // systems so that consecutive positions are independent rows.
-    const int2 *pos_l, *pos_u;
-    int32_t npos_l, npos_u;
+    const int32_t *order_l, *order_u;
+    // optional look-ahead products per block row (block id of Dinv_i L_{i,i-1}
+    // / Dinv_i U_{i,i+1}, 0 = none); NULL = none
+    const int32_t *l_la, *u_la;
     // position claim counters of the lower and upper launch (zeroed before
-    // each launch pair): CTAs claim positions in order as they become
-    // resident, so the launch needs no co-residency of all its CTAs
+    // each launch pair): CTAs claim positions in dealing order as they become
+    // resident, so a launch needs no co-residency of all its CTAs (systems on
+    // other streams may hold part of the GPU)
     int32_t* claim;
-    // look-ahead products per block row, depth d = 1..3 (block id of
-    // Dinv_i L_{i,i-d} / Dinv_i U_{i,i+d}, 0 = none); NULL = none
-    const int32_t *l_la[3], *u_la[3];
 };
 // Column chunks of 8 right-hand sides solved together in one launch pair
 constexpr int TRISOLVE_MAX_CHUNKS = 8;

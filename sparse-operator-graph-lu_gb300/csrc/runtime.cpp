@@ -541,7 +541,7 @@ void fill_pivot_stats(const sog_system* s, size_t k, sog_solve_stats& st) {
 int trisolve(sog_system* s, void* vec, int nrhs) {
     sog_ctx* c = s->ctx;
     const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));  // positions per row
-    int grid = std::min(s->ds.npos_l * nch, trisolve_grid(s->fp64, nrhs, c->num_sms));
+    int grid = std::min(s->R * nch, trisolve_grid(s->fp64, nrhs, c->num_sms));
     if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
     int nl = 0;
     int rc = s->fp64 ? trisolve_launch(s->ds, (const double*)s->tiles, (double*)vec, nrhs, s->epoch, grid, s->stream, nl)
@@ -829,7 +829,7 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     // + the transposed L leaves of an LL^T plan
     bool any_sym = p.symmetric;
     for (const Segment& sg : p.segs) any_sym = any_sym || sg.symmetric;
-    uint64_t tiles = ((uint64_t)p.storage_count + 8ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
+    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
                      elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
@@ -878,7 +878,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // below (inverses, look-ahead products, transposed leaves), so the op
     // records are copied once.
     std::vector<Op> ops2;
-    ops2.reserve(p.ops.size() + 8 * (size_t)p.cfg.block_rows + p.L.size());
+    ops2.reserve(p.ops.size() + 4 * (size_t)p.cfg.block_rows + p.L.size());
     ops2.assign(p.ops.begin(), p.ops.end());
     int32_t storage2 = p.storage_count;
     // LL^T systems: the upper factor of the substitution is L^T (upperSolverT,
@@ -906,48 +906,16 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     }
     std::vector<int32_t> ldinv, udinv;
     add_diag_inverses(ops2, storage2, s->R, s->L, s->U, ldinv, udinv);
-    // substitution positions: two consecutive rows of one system (the second
-    // after the first in solve order), solved by one CTA; a single row where a
-    // system has an odd row count or the look-ahead is off. Batches interleave
-    // their systems: every system's first position, then every second one, ...
-    std::vector<int32_t> pos_l, pos_u;  // (first row, second row or -1) per position
-    std::vector<char> second_l(s->R, 0), second_u(s->R, 0);
-    {
-        std::vector<std::pair<int, int>> sysr;  // first block row, block rows
-        if (p.segs.empty()) sysr.push_back({0, p.cfg.block_rows});
-        else
-            for (const Segment& sg : p.segs) sysr.push_back({sg.row0 / 64, sg.R});
-        const int step = o.solve_lookahead >= 0 ? 2 : 1;
-        int maxp = 0;
-        for (auto& q : sysr) maxp = std::max(maxp, (q.second + step - 1) / step);
-        for (int P = 0; P < maxp; P++)
-            for (auto& q : sysr) {
-                const int b0 = q.first, Rs = q.second, r = step * P;
-                if (r >= Rs) continue;
-                const bool two = step == 2 && r + 1 < Rs;
-                pos_l.push_back(b0 + r);
-                pos_l.push_back(two ? b0 + r + 1 : -1);
-                pos_u.push_back(b0 + Rs - 1 - r);
-                pos_u.push_back(two ? b0 + Rs - 2 - r : -1);
-                if (two) {
-                    second_l[b0 + r + 1] = 1;
-                    second_u[b0 + Rs - 2 - r] = 1;
-                }
-            }
-    }
-    std::vector<int32_t> lla[3], ula[3];
-    if (o.solve_lookahead >= 0)
-        add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, second_l, second_u, lla, ula);
+    std::vector<int32_t> lla, ula;
+    if (o.solve_lookahead >= 0) add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla, ula);
     s->storage = storage2;
     std::vector<int32_t> outputs;
     for (const Leaf& lf : s->L) outputs.push_back(lf.id);
     for (const Leaf& lf : s->U) outputs.push_back(lf.id);
     for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
-    for (int d = 0; d < 3; d++) {
-        for (int32_t id : lla[d]) if (id > 0) outputs.push_back(id);
-        for (int32_t id : ula[d]) if (id > 0) outputs.push_back(id);
-    }
+    for (int32_t id : lla) if (id > 0) outputs.push_back(id);
+    for (int32_t id : ula) if (id > 0) outputs.push_back(id);
     try {
         s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts, true, !s->fp64);
         if (!s->fp64) order_pairs_by_ready(s->tg, false);
@@ -960,7 +928,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // value lives in its source's tile
     for (Leaf& lf : s->L) lf.id = g.alias[lf.id];
     for (Leaf& lf : s->U) lf.id = g.alias[lf.id];
-    for (auto* v : {&ldinv, &udinv, &lla[0], &ula[0], &lla[1], &ula[1], &lla[2], &ula[2]})
+    for (auto* v : {&ldinv, &udinv, &lla, &ula})
         for (int32_t& id : *v)
             if (id > 0) id = g.alias[id];
     // solve structure
@@ -1031,6 +999,21 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
         for (int i = 0; i < p.cfg.n; i++) n2o[i] = p.ord.new_to_old[i];
     else
         n2o = p.ord.new_to_old;
+    // substitution dealing order of a batch: by row within its system (from
+    // the top for L, from the bottom for U), then by system
+    std::vector<int32_t> ord_l, ord_u;
+    if (ns > 1) {
+        int maxR = 0;
+        for (const Segment& sg : s->segs) maxR = std::max(maxR, sg.R);
+        ord_l.reserve(s->R);
+        ord_u.reserve(s->R);
+        for (int r = 0; r < maxR; r++)
+            for (const Segment& sg : s->segs)
+                if (r < sg.R) {
+                    ord_l.push_back(sg.row0 / 64 + r);
+                    ord_u.push_back(sg.row0 / 64 + sg.R - 1 - r);
+                }
+    }
     // task arrays
     std::vector<int32_t> parts32(g.ntasks);
     for (int32_t t = 0; t < g.ntasks; t++) parts32[t] = g.parts[t];
@@ -1076,10 +1059,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_sco = L.add<int16_t>(p.scatter_off.size()), o_pdt = L.add<int32_t>(p.pad_tile.size()),
              o_pdo = L.add<int16_t>(p.pad_off.size()), o_n2o = L.add<int32_t>(n2o.size()),
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
-             o_posl = L.add<int32_t>(pos_l.size()), o_posu = L.add<int32_t>(pos_u.size()), o_claim = L.add<int32_t>(2),
-             o_lla0 = L.add<int32_t>(lla[0].size()), o_ula0 = L.add<int32_t>(ula[0].size()),
-             o_lla1 = L.add<int32_t>(lla[1].size()), o_ula1 = L.add<int32_t>(ula[1].size()),
-             o_lla2 = L.add<int32_t>(lla[2].size()), o_ula2 = L.add<int32_t>(ula[2].size()),
+             o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
+             o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()), o_claim = L.add<int32_t>(2),
              o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
              o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
              o_done = L.add<int32_t>(g.ntasks), o_piv = L.add<DevPivot>(ns), o_piv0 = L.add<DevPivot>(ns),
@@ -1177,16 +1158,11 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->d_n2o = put(A, o_n2o, n2o, st);
     s->d_seg_brow = put(A, o_sbr, seg_brow, st);
     s->d_seg_n = put(A, o_sn, seg_n, st);
-    ds.pos_l = reinterpret_cast<const int2*>(put(A, o_posl, pos_l, st));
-    ds.pos_u = reinterpret_cast<const int2*>(put(A, o_posu, pos_u, st));
-    ds.npos_l = (int32_t)(pos_l.size() / 2);
-    ds.npos_u = (int32_t)(pos_u.size() / 2);
+    ds.order_l = ord_l.empty() ? nullptr : put(A, o_ordl, ord_l, st);
+    ds.order_u = ord_u.empty() ? nullptr : put(A, o_ordu, ord_u, st);
+    ds.l_la = lla.empty() ? nullptr : put(A, o_lla, lla, st);
+    ds.u_la = ula.empty() ? nullptr : put(A, o_ula, ula, st);
     ds.claim = reinterpret_cast<int32_t*>(A + o_claim);
-    const uint64_t o_lla[3] = {o_lla0, o_lla1, o_lla2}, o_ula[3] = {o_ula0, o_ula1, o_ula2};
-    for (int d = 0; d < 3; d++) {
-        ds.l_la[d] = lla[d].empty() ? nullptr : put(A, o_lla[d], lla[d], st);
-        ds.u_la[d] = ula[d].empty() ? nullptr : put(A, o_ula[d], ula[d], st);
-    }
     if (cudaMallocHost(&s->h_red, sizeof(double) * RED * 64 * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_nrhs, sizeof(int32_t) * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_active, sizeof(int32_t) * ns) != cudaSuccess ||

@@ -4,7 +4,7 @@
 // matrix for iterative refinement, and the permutation gathers.
 //
 // Substitution runs as one persistent launch per triangle. Block rows are
-// dealt round-robin to co-resident CTAs; a CTA folds in each off-diagonal
+// claimed in a fixed dealing order by resident CTAs; a CTA folds in each off-diagonal
 // block as soon as the block row it multiplies is published (a per-row
 // readiness flag), then solves its diagonal block and publishes its own row.
 // Rows only wait on rows dealt earlier, so the smallest unfinished row can
@@ -68,43 +68,18 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// NR consecutive values of one row of vec, with 16-byte loads where the row
-// segment is 16-byte aligned (vec is written by other CTAs of this launch:
-// L2 loads)
-template <typename T, int NR>
-__device__ __forceinline__ void load_row(const T* p, bool vec16, T (&o)[NR]) {
-    constexpr int PER = 16 / (int)sizeof(T);
-    if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
-        if (vec16) {
-#pragma unroll
-            for (int q = 0; q < NR / PER; q++) {
-                const int4 r = __ldcg(reinterpret_cast<const int4*>(p) + q);
-                memcpy(&o[q * PER], &r, 16);
-            }
-            return;
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < NR; r++) o[r] = __ldcg(p + r);
-}
-
 // One launch per triangle and per chunk of NR right-hand-side columns
-// [c0, c0+NR) of vec (n_ext x ld, row-major). A position is one block row or
-// two consecutive ones (a, then b = the row after a in solve order). Its
-// off-diagonal blocks are split over the warps: each warp waits (bounded)
-// only for the row its block multiplies, stages that row's NR-column slice in
-// shared memory and accumulates block * slice in registers (lane l: rows 2l,
-// 2l+1). The sums are combined with b and multiplied by the precomputed
-// inverses of the diagonal blocks. The blocks next to the position's rows
-// are left out of those sums and applied as look-ahead products
-// M_d = Dinv_i * B_{i,i-d} (d = 1, 2 for a; 1, 2, 3 for b, whose first
-// neighbour is a) once the previous position has published its rows:
-//   y_a = Dinv_a acc_a - M1_a y_{a-1} - M2_a y_{a-2}
-//   y_b = Dinv_b acc_b - M2_b y_{a-1} - M3_b y_{a-2} - M1_b y_a
-// so each hop between CTAs is followed by two products in shared memory and
-// only every second block row crosses between CTAs. (Signs for U: a+1, a+2.)
-// The rows are then published with release stores of their flags.
-// smem: part[2][8][NV] | ybuf[8][NV] | acc[2][NV] | ya[NV]
+// [c0, c0+NR) of vec (n_ext x ld, row-major). For block row i the warps split
+// its off-diagonal blocks: each warp waits (bounded) only for the row its
+// block multiplies, stages that row's NR-column slice in shared memory and
+// accumulates block * slice in registers (lane l: rows 2l, 2l+1). The warp
+// partials and b_i are combined and multiplied by the precomputed inverse of
+// the diagonal block. With a look-ahead product M = Dinv_i * B_{i,j} for the
+// neighbouring row j (i-1 for L, i+1 for U), block B_{i,j} is left out of the
+// sum and y_i = Dinv_i (b_i - sum) - M y_j is finished after row j is
+// published: the row's critical path is one 64x64 product. The row is then
+// published with a release store.
+// smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR]
 template <typename T, int NR>
 __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
                                                       int cbase, int nch, int epoch, int lower) {
@@ -112,28 +87,18 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     constexpr int NV = 64 * NR;
     constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte load
     T* part = reinterpret_cast<T*>(smem_raw);
-    T* ybuf = part + 16 * NV;
+    T* ybuf = part + 8 * NV;
     T* acc = ybuf + 8 * NV;
-    T* ya = acc + 2 * NV;
     __shared__ int s_stop, s_next;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int R = s.block_rows;
-    int* claim = s.claim + (lower ? 0 : 1);
     const int* ptr = lower ? s.l_ptr : s.u_ptr;
     const int* col = lower ? s.l_col : s.u_col;
     const int* ids = lower ? s.l_id : s.u_id;
     const int* dinv = lower ? s.l_dinv : s.u_dinv;
-    const int* la1 = lower ? s.l_la[0] : s.u_la[0];
-    const int* la2 = lower ? s.l_la[1] : s.u_la[1];
-    const int* la3 = lower ? s.l_la[2] : s.u_la[2];
-    const int2* pos = lower ? s.pos_l : s.pos_u;
-    const int npos = lower ? s.npos_l : s.npos_u;
-    const int dir = lower ? -1 : 1;  // a row's neighbour on the solved side
-    const bool vec16 = ((size_t)ld * sizeof(T)) % 16 == 0;
-    if (tid == 0) {
-        s_stop = 0;
-        s_next = atomicAdd(claim, 1);
-    }
+    const int* lookahead = lower ? s.l_la : s.u_la;
+    const int* order = lower ? s.order_l : s.order_u;
+    if (tid == 0) { s_stop = 0; s_next = atomicAdd(s.claim + (lower ? 0 : 1), 1); }
     __syncthreads();
     T* yw = ybuf + warp * NV;
     // bounded wait of lane 0 for row j's flag; the warp's later reads of row j
@@ -154,224 +119,117 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         __syncwarp();
         return !*(volatile int*)&s_stop;
     };
-    // pa/pb += the lane's two rows of block B times the staged slice
-    auto block_product = [&](const T* B, T (&pa)[NR], T (&pb)[NR]) {
-#pragma unroll 4
-        for (int c = 0; c < 64; c += VW) {
-            const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
+    // positions: nch column chunks of each row in turn, rows in dealing order
+    // positions claimed in dealing order (the next one while this one runs):
+    // a row only waits on rows dealt earlier, which resident CTAs hold
+    for (int k = s_next; k < R * nch; k = s_next) {
+        __syncthreads();  // every thread has read s_next
+        if (tid == 0) s_next = atomicAdd(s.claim + (lower ? 0 : 1), 1);
+        const int kk = k / nch, ch = k - kk * nch, c0 = cbase + ch * NR;
+        const int i = order ? order[kk] : (lower ? kk : R - 1 - kk);
+        fl = s.flags + (size_t)ch * R;
+        if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
+        const T* Dm = tiles + (size_t)dinv[i] * 4096;
+        const int la = lookahead ? lookahead[i] : 0;
+        // warm L1 with this lane's slice of the diagonal inverse
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
+        T pa[NR], pb[NR];
 #pragma unroll
-            for (int v = 0; v < VW; v++)
-#pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    const T y = yw[(c + v) * NR + r];
-                    pa[r] += b0.v[v] * y;
-                    pb[r] += b1.v[v] * y;
-                }
-        }
-    };
-    // this warp's share of the position's early blocks (all but those left to
-    // the look-ahead products): both rows' blocks in one walk, in the order
-    // their operands become ready (lower: ascending column, upper:
-    // descending), every 8th to this warp, so the blocks that depend on the
-    // most recent rows come last for both rows. Partial sums for output rows
-    // 2 lane, 2 lane + 1 of row a (xa, za) and of row b (xb, zb).
-    auto early = [&](int ia, int ib, int sa1, int sa2, int sb1, int sb2, int sb3, int c0, T (&xa)[NR], T (&za)[NR],
-                     T (&xb)[NR], T (&zb)[NR]) -> bool {
-#pragma unroll
-        for (int r = 0; r < NR; r++) xa[r] = za[r] = xb[r] = zb[r] = T(0);
-        int qa = ptr[ia], qb = ib >= 0 ? ptr[ib] : 0;
-        const int qa1 = ptr[ia + 1], qb1 = ib >= 0 ? ptr[ib + 1] : 0;
-        int idx = 0;
-        while (qa < qa1 || qb < qb1) {
-            bool from_a;
-            if (qa >= qa1) from_a = false;
-            else if (qb >= qb1) from_a = true;
-            else from_a = lower ? col[qa] <= col[qb] : col[qa] >= col[qb];
-            const int q = from_a ? qa++ : qb++;
+        for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
+        bool stop = false;
+        // with a look-ahead product the last block (the neighbouring row) is left out
+        const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0);
+        for (int q = ptr[i] + warp; q < q1; q += 8) {
             const int j = col[q];
-            if (from_a ? (j == sa1 || j == sa2) : (j == sb1 || j == sb2 || j == sb3)) continue;
-            if ((idx++ & 7) != warp) continue;
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
             // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
 #pragma unroll
             for (int o = 0; o < 128; o += 128 / (int)sizeof(T)) asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
-            if (!wait_row(j)) return false;
-            const T* vj = vec + (size_t)j * 64 * ld + c0;
-            {
-                T t0[NR], t1[NR];
-                load_row<T, NR>(vj + (size_t)(2 * lane) * ld, vec16, t0);
-                load_row<T, NR>(vj + (size_t)(2 * lane + 1) * ld, vec16, t1);
-#pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    yw[(2 * lane) * NR + r] = t0[r];
-                    yw[(2 * lane + 1) * NR + r] = t1[r];
-                }
-            }
-            __syncwarp();
-            if (from_a) block_product(B, xa, za);
-            else block_product(B, xb, zb);
-            __syncwarp();
-        }
-        return true;
-    };
-    // positions: nch column chunks of each position in turn, claimed in
-    // order; the next one is claimed while this one runs
-    for (int k = s_next; k < npos * nch; k = s_next) {
-        __syncthreads();  // every thread has read s_next
-        if (tid == 0) s_next = atomicAdd(claim, 1);
-        const int pp = k / nch, ch = k - pp * nch, c0 = cbase + ch * NR;
-        const int2 ab = pos[pp];
-        const int ia = ab.x, ib = ab.y;  // ib < 0: a single row
-        fl = s.flags + (size_t)ch * R;
-        if (s.trace && tid == 0) {
-            s.trace[4 * (size_t)ia + (lower ? 0 : 2)] = globaltimer_ns();
-            if (ib >= 0) s.trace[4 * (size_t)ib + (lower ? 0 : 2)] = globaltimer_ns();
-        }
-        // look-ahead products of this position (0 = none) and the rows they need
-        const int m1a = la1 ? la1[ia] : 0, m2a = la2 ? la2[ia] : 0;
-        const int m1b = (ib >= 0 && la1) ? la1[ib] : 0, m2b = (ib >= 0 && la2) ? la2[ib] : 0,
-                  m3b = (ib >= 0 && la3) ? la3[ib] : 0;
-        const int n1 = ia + dir, n2 = ia + 2 * dir;  // the previous rows: a's first and second neighbours
-        bool stop = false;
-        {
-            T xa[NR], za[NR], xb[NR], zb[NR];
-            // row a: all but its first two neighbours (when they have
-            // products); row b: all but a and a's first two neighbours
-            if (!early(ia, ib, m1a ? n1 : -2, m2a ? n2 : -2, m1b ? ia : -2, m2b ? n1 : -2, m3b ? n2 : -2, c0, xa, za, xb,
-                       zb))
+            if (!wait_row(j)) {
                 stop = true;
-            T* pw = part + warp * NV;
-            T* pw2 = part + (8 + warp) * NV;
-#pragma unroll
-            for (int r = 0; r < NR; r++) {
-                pw[(2 * lane) * NR + r] = xa[r];
-                pw[(2 * lane + 1) * NR + r] = za[r];
-                pw2[(2 * lane) * NR + r] = xb[r];
-                pw2[(2 * lane + 1) * NR + r] = zb[r];
+                break;
             }
+            const T* vj = vec + (size_t)j * 64 * ld + c0;
+            for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
+            __syncwarp();
+#pragma unroll 4
+            for (int c = 0; c < 64; c += VW) {
+                const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
+#pragma unroll
+                for (int v = 0; v < VW; v++)
+#pragma unroll
+                    for (int r = 0; r < NR; r++) {
+                        const T y = yw[(c + v) * NR + r];
+                        pa[r] += b0.v[v] * y;
+                        pb[r] += b1.v[v] * y;
+                    }
+            }
+            __syncwarp();
+        }
+        T* pw = part + warp * NV;
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            pw[(2 * lane) * NR + r] = pa[r];
+            pw[(2 * lane + 1) * NR + r] = pb[r];
         }
         __syncthreads();
         if (s_stop || stop) return;
         for (int e = tid; e < NV; e += NT) {
-            T v = __ldcg(vec + ((size_t)ia * 64 + e / NR) * ld + c0 + (e % NR));
+            T v = __ldcg(vec + ((size_t)i * 64 + e / NR) * ld + c0 + (e % NR));
 #pragma unroll
             for (int w = 0; w < 8; w++) v -= part[w * NV + e];
             acc[e] = v;
-            if (ib >= 0) {
-                T u = __ldcg(vec + ((size_t)ib * 64 + e / NR) * ld + c0 + (e % NR));
-#pragma unroll
-                for (int w = 0; w < 8; w++) u -= part[(8 + w) * NV + e];
-                acc[NV + e] = u;
-            }
         }
         __syncthreads();
-        // warp w rows 8w..8w+7, four lanes per row, each lane 16 columns;
-        // partial sums reduced over the four lanes at the end
-        const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
-        T ypa[NR], ypb[NR];
+        // y_i = inv(D_ii) * acc [- M * y_j]: warp w rows 8w..8w+7, four lanes
+        // per row, each lane 16 columns; partial sums reduced over the four lanes
         {
-            const T* Da = tiles + (size_t)dinv[ia] * 4096 + row * 64 + cb;
+            const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
+            Vec16<T> m[16 / VW];
+            if (la > 0) {  // the look-ahead slice, loaded before the wait
+                const T* M = tiles + (size_t)la * 4096 + row * 64 + cb;
 #pragma unroll
-            for (int r = 0; r < NR; r++) ypa[r] = ypb[r] = T(0);
+                for (int c = 0; c < 16 / VW; c++) m[c] = ldg16(M + c * VW);
+            }
+            T y[NR];
+#pragma unroll
+            for (int r = 0; r < NR; r++) y[r] = T(0);
 #pragma unroll
             for (int c = 0; c < 16; c += VW) {
-                const Vec16<T> d = ldg16(Da + c);
+                const Vec16<T> d = ldg16(Dm + row * 64 + cb + c);
 #pragma unroll
                 for (int v = 0; v < VW; v++)
 #pragma unroll
-                    for (int r = 0; r < NR; r++) ypa[r] += d.v[v] * acc[(cb + c + v) * NR + r];
+                    for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
             }
-            if (ib >= 0) {
-                const T* Db = tiles + (size_t)dinv[ib] * 4096 + row * 64 + cb;
+            // a wait that runs out sets s_stop: the CTA leaves together after
+            // the barrier below, publishing nothing
+            if (la > 0 && wait_row(lower ? i - 1 : i + 1)) {
+                const int j = lower ? i - 1 : i + 1;
+                const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
 #pragma unroll
-                for (int c = 0; c < 16; c += VW) {
-                    const Vec16<T> d = ldg16(Db + c);
+                for (int c = 0; c < 16 / VW; c++)
 #pragma unroll
                     for (int v = 0; v < VW; v++)
 #pragma unroll
-                        for (int r = 0; r < NR; r++) ypb[r] += d.v[v] * acc[NV + (cb + c + v) * NR + r];
-                }
-            }
-        }
-        // ypa -= Ma y_n, ypb -= Mb y_n over this lane's 16 columns of the
-        // products' rows and of y_n's slice, loaded once for both
-        auto apply = [&](int ma, int mb, int n) {
-            const T* Ma = tiles + (size_t)ma * 4096 + row * 64 + cb;
-            const T* Mb = tiles + (size_t)mb * 4096 + row * 64 + cb;
-            const T* vn = vec + ((size_t)n * 64 + cb) * ld + c0;
-#pragma unroll
-            for (int c = 0; c < 16; c += VW) {
-                Vec16<T> va, vb;
-                if (ma) va = ldg16(Ma + c);
-                if (mb) vb = ldg16(Mb + c);
-#pragma unroll
-                for (int v = 0; v < VW; v++) {
-                    T yn[NR];
-                    load_row<T, NR>(vn + (size_t)(c + v) * ld, vec16, yn);
-#pragma unroll
-                    for (int r = 0; r < NR; r++) {
-                        if (ma) ypa[r] -= va.v[v] * yn[r];
-                        if (mb) ypb[r] -= vb.v[v] * yn[r];
-                    }
-                }
-            }
-        };
-        // warm L1 with this lane's slices of the look-ahead products
-        for (int m : {m1a, m2a, m2b, m3b, m1b})
-            if (m > 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + (size_t)m * 4096 + row * 64 + cb));
-        // the previous position's rows (a wait that runs out sets s_stop; the
-        // CTA then leaves together after the barriers below, publishing nothing)
-        bool ok = !(m1a || m2b) || wait_row(n1);
-        ok = ok && (!(m2a || m3b) || wait_row(n2));
-        if (ok) {
-            if (m1a || m2b) apply(m1a, m2b, n1);
-            if (m2a || m3b) apply(m2a, m3b, n2);
-        }
-#pragma unroll
-        for (int r = 0; r < NR; r++) {
-            ypa[r] += __shfl_xor_sync(0xffffffffu, ypa[r], 1);
-            ypa[r] += __shfl_xor_sync(0xffffffffu, ypa[r], 2);
-        }
-        if ((lane & 3) == 0) {
-#pragma unroll
-            for (int r = 0; r < NR; r++) {
-                vec[((size_t)ia * 64 + row) * ld + c0 + r] = ypa[r];
-                ya[row * NR + r] = ypa[r];
-            }
-        }
-        if (ib >= 0) {
-            __syncthreads();
-            if (m1b) {  // y_b -= M1_b y_a, y_a from shared memory
-                const T* M = tiles + (size_t)m1b * 4096 + row * 64 + cb;
-#pragma unroll
-                for (int c = 0; c < 16; c += VW) {
-                    const Vec16<T> mv = ldg16(M + c);
-#pragma unroll
-                    for (int v = 0; v < VW; v++)
-#pragma unroll
-                        for (int r = 0; r < NR; r++) ypb[r] -= mv.v[v] * ya[(cb + c + v) * NR + r];
-                }
+                        for (int r = 0; r < NR; r++) y[r] -= m[c].v[v] * __ldcg(vj + (size_t)(c * VW + v) * ld + r);
             }
 #pragma unroll
             for (int r = 0; r < NR; r++) {
-                ypb[r] += __shfl_xor_sync(0xffffffffu, ypb[r], 1);
-                ypb[r] += __shfl_xor_sync(0xffffffffu, ypb[r], 2);
+                y[r] += __shfl_xor_sync(0xffffffffu, y[r], 1);
+                y[r] += __shfl_xor_sync(0xffffffffu, y[r], 2);
             }
             if ((lane & 3) == 0) {
 #pragma unroll
-                for (int r = 0; r < NR; r++) vec[((size_t)ib * 64 + row) * ld + c0 + r] = ypb[r];
+                for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
             }
         }
         __syncthreads();
         if (s_stop) return;
         if (tid == 0) {
-            fence_acq_rel_gpu();  // the rows written by all threads (ordered by the barrier) before the flags
-            st_release(s.flags + (size_t)ch * R + ia, epoch);
-            if (ib >= 0) st_release(s.flags + (size_t)ch * R + ib, epoch);
-            if (s.trace) {
-                s.trace[4 * (size_t)ia + (lower ? 1 : 3)] = globaltimer_ns();
-                if (ib >= 0) s.trace[4 * (size_t)ib + (lower ? 1 : 3)] = globaltimer_ns();
-            }
+            fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
+            st_release(s.flags + (size_t)ch * R + i, epoch);
+            if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
         }
         __syncthreads();  // thread 0's next claim is visible
     }
@@ -379,7 +237,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
 
 template <typename T, int NR>
 size_t trisolve_smem() {
-    return (size_t)(27 * 64 * NR) * sizeof(T);
+    return (size_t)(17 * 64 * NR) * sizeof(T);
 }
 
 template <typename T, int NR>
@@ -387,7 +245,7 @@ int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, in
                    cudaStream_t st) {
     const size_t smem = trisolve_smem<T, NR>();
     cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaMemsetAsync(s.claim, 0, 2 * sizeof(int32_t), st);
+    cudaMemsetAsync(s.claim, 0, 8, st);
     trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch, 1);
     trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch + 1, 0);
     epoch += 2;

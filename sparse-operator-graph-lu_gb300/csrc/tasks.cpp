@@ -490,30 +490,23 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
 
 void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                            const std::vector<int32_t>& uinv, const std::vector<char>& second_l,
-                            const std::vector<char>& second_u, std::vector<int32_t> (&lla)[3],
-                            std::vector<int32_t> (&ula)[3]) {
-    for (int d = 0; d < 3; d++) {
-        lla[d].assign(block_rows, 0);
-        ula[d].assign(block_rows, 0);
-    }
+                            const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula) {
+    lla.assign(block_rows, 0);
+    ula.assign(block_rows, 0);
     int32_t seq = ops.empty() ? 0 : ops.back().seq;
     const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
-    // depth d = distance from the diagonal; depth 3 only for the second row of a position
-    for (const Leaf& lf : L) {
-        const int d = lf.bi - lf.bj;
-        if (d < 1 || d > 3 || linv[lf.bi] <= 0 || (d == 3 && !second_l[lf.bi])) continue;
-        const int32_t id = storage_count++;
-        ops.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
-        lla[d - 1][lf.bi] = id;
-    }
-    for (const Leaf& lf : U) {
-        const int d = lf.bj - lf.bi;
-        if (d < 1 || d > 3 || uinv[lf.bi] <= 0 || (d == 3 && !second_u[lf.bi])) continue;
-        const int32_t id = storage_count++;
-        ops.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
-        ula[d - 1][lf.bi] = id;
-    }
+    for (const Leaf& lf : L)
+        if (lf.bj == lf.bi - 1 && linv[lf.bi] > 0) {
+            const int32_t id = storage_count++;
+            ops.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            lla[lf.bi] = id;
+        }
+    for (const Leaf& lf : U)
+        if (lf.bj == lf.bi + 1 && uinv[lf.bi] > 0) {
+            const int32_t id = storage_count++;
+            ops.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ula[lf.bi] = id;
+        }
 }
 
 }  // namespace sog

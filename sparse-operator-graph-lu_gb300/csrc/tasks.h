@@ -96,18 +96,13 @@ std::vector<int32_t> static_order(const TaskGraph& g, bool fp64);
 // accumulates the ready pairs first and the late one last.
 void order_pairs_by_ready(TaskGraph& g, bool fp64);
 
-// Look-ahead products for the substitution: lla[d-1][i] = id of a new block
-// Linv_ii * L_{i,i-d} for every L block at distance d = 1, 2 from the diagonal
-// (d = 3 only for rows with second_l[i]: the second row of a substitution
-// position), ula the same with Uinv_ii * U_{i,i+d} (0 = none). A position of
-// rows a, b (b the row after a in solve order) then forms
-//   y_a = Linv_aa (b_a - sum_{j<a-2} L_aj y_j) - lla1_a y_{a-1} - lla2_a y_{a-2}
-//   y_b = Linv_bb (b_b - sum_{j<a-2} L_bj y_j) - lla2_b y_{a-1} - lla3_b y_{a-2} - lla1_b y_a
-// with everything but those products done before rows a-1, a-2 are ready.
+// Look-ahead products for the substitution: for every block row i with an L
+// block at (i, i-1), lla[i] = id of a new block Linv_ii * L_{i,i-1}; for every
+// U block at (i, i+1), ula[i] = id of Uinv_ii * U_{i,i+1} (0 = none). The
+// substitution then forms y_i = Linv_ii (b_i - sum_{j<i-1} L_ij y_j) - lla_i
+// y_{i-1}: everything but one 64x64 product is done before row i-1 is ready.
 void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                            const std::vector<int32_t>& uinv, const std::vector<char>& second_l,
-                            const std::vector<char>& second_u, std::vector<int32_t> (&lla)[3],
-                            std::vector<int32_t> (&ula)[3]);
+                            const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula);
 
 }  // namespace sog
