@@ -92,7 +92,12 @@ typedef struct {
                                 1e4 for SOG_MIXED (FP32 factors lose about growth x 6e-8 of relative accuracy;
                                 on SOG_EPIVOT a mixed caller whose refinement does not converge should factor
                                 in SOG_FP64); < 0 = no gate, the reference's clamp-and-continue */
-    int32_t reserved[2];
+    int32_t resident_compact; /* 1 = after each factorisation keep only the tiles the substitution reads
+                                 (L/U leaves, diagonal inverses, look-ahead products) and return the rest
+                                 of the block pool (the reference frees blocks after their last stage,
+                                 BlockPlanner.cpp:597-648); the next factorisation allocates them again.
+                                 0 = keep every tile (no reallocation between refactorisations) */
+    int32_t reserved;
 } sog_options;
 
 typedef struct {
@@ -330,7 +335,8 @@ int soglu_solveLU(int32_t dim, int64_t valcount, int32_t symmetric, const int32_
  * quarters of the GPU while there are other lanes). A request larger than the
  * whole pool fails with SOG_ENOMEM; one that fits once others are released
  * waits. A system that fails the pivot gate (sog_options.growth_limit) is
- * answered with SOG_EPIVOT and its solution.
+ * answered with SOG_EPIVOT and its solution. Resident factors are compacted
+ * (sog_options.resident_compact is set for the server's systems).
  * Factors stay resident after the answer (sog_server_solve for further
  * right-hand sides) until sog_server_release. The context must not be used
  * directly while a server runs on it. */

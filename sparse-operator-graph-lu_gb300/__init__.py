@@ -48,7 +48,8 @@ class PlanInfo(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("executor", C.c_int32), ("max_refine", C.c_int32), ("tol", C.c_double),
                 ("gemm_split", C.c_int32), ("solve_lookahead", C.c_int32), ("pipeline_stages", C.c_int32),
-                ("max_ctas", C.c_int32), ("growth_limit", C.c_double), ("reserved", C.c_int32 * 2)]
+                ("max_ctas", C.c_int32), ("growth_limit", C.c_double), ("resident_compact", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -280,7 +281,7 @@ class System:
 
     def __init__(self, ctx: Context, plan: Plan, precision: int = FP64, executor: int = EXEC_PERSISTENT,
                  max_refine: int = 10, tol: float = 1e-10, gemm_split: int = 0, solve_lookahead: int = 0,
-                 pipeline_stages: int = 0, growth_limit: float = 0.0, max_ctas: int = 0):
+                 pipeline_stages: int = 0, growth_limit: float = 0.0, max_ctas: int = 0, resident_compact: bool = False):
         """growth_limit: the pivot gate (0 = default for the precision, < 0 =
         off, as the reference); a factorisation that fails it raises
         SOGError(EPIVOT) unless factor(..., allow_epivot=True)."""
@@ -289,7 +290,8 @@ class System:
         self._h = C.c_void_p()
         self.opt = Options(precision=precision, executor=executor, max_refine=max_refine, tol=tol,
                            gemm_split=gemm_split, solve_lookahead=solve_lookahead,
-                           pipeline_stages=pipeline_stages, growth_limit=growth_limit, max_ctas=max_ctas)
+                           pipeline_stages=pipeline_stages, growth_limit=growth_limit, max_ctas=max_ctas,
+                           resident_compact=int(resident_compact))
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
 
     @staticmethod

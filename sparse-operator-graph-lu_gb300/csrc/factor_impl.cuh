@@ -686,66 +686,69 @@ __device__ void lu_task_r4(const DevTasks& tk, float* __restrict__ tiles, int ta
             }
         }
         __syncthreads();
-        // ---- 2: block row and column j
-        {
-            float4 m[4];
-            if (bc == j && br > j) {  // L21 = A21 U_D^-1
+        // ---- 2: block row and column j. Block row j multiplies its own
+        // block from the left by Y_D (U12 right of the diagonal, W's Y left of
+        // it), block column j from the right (L21 = A21 U_D^-1 below, W's
+        // X X_D above): one product per side, the operands chosen by select,
+        // so a warp runs at most two paths
+        if (br == j && bc != j) {
+            const bool right = bc > j;
+            float4 m[4], x[4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) m[i] = reinterpret_cast<const float4*>(Dr + 16)[i];
-                float4 t[4] = {a[0], a[1], a[2], a[3]};
-                mm4(a, t, m, false);
-#pragma unroll
-                for (int i = 0; i < 4; i++) reinterpret_cast<float4*>(Lb)[br * 4 + i] = a[i];
-            } else if (br == j && bc > j) {  // U12 = Y_D A12
-#pragma unroll
-                for (int i = 0; i < 4; i++) m[i] = reinterpret_cast<const float4*>(Dr)[i];
-                float4 t[4] = {a[0], a[1], a[2], a[3]};
-                mm4(a, m, t, false);
-#pragma unroll
-                for (int i = 0; i < 4; i++) reinterpret_cast<float4*>(Ub)[i * 16 + bc] = a[i];
+            for (int i = 0; i < 4; i++) {
+                m[i] = reinterpret_cast<const float4*>(Dr)[i];
+                x[i] = right ? a[i] : w[i];
             }
-            if (br == j && bc < j) {  // W's block row j, left: Y = Y_D Y
+            float4 t[4];
+            mm4(t, m, x, false);
 #pragma unroll
-                for (int i = 0; i < 4; i++) m[i] = reinterpret_cast<const float4*>(Dr)[i];
-                float4 t[4] = {w[0], w[1], w[2], w[3]};
-                mm4(w, m, t, false);
+            for (int i = 0; i < 4; i++) {
+                if (right) a[i] = t[i]; else w[i] = t[i];
+                reinterpret_cast<float4*>(right ? Ub : Yb)[i * 16 + bc] = t[i];
+            }
+        } else if (bc == j && br != j && (br > j || !CHOL)) {
+            const bool below = br > j;
+            float4 m[4], x[4];
+            const float* M = Dr + (below ? 16 : 32);  // U_D^-1 / X_D
 #pragma unroll
-                for (int i = 0; i < 4; i++) reinterpret_cast<float4*>(Yb)[i * 16 + bc] = w[i];
-            } else if (!CHOL && bc == j && br < j) {  // W's block column j, above: X = X X_D
+            for (int i = 0; i < 4; i++) {
+                m[i] = reinterpret_cast<const float4*>(M)[i];
+                x[i] = below ? a[i] : w[i];
+            }
+            float4 t[4];
+            mm4(t, x, m, false);
+            float4 sc = make_float4(1.f, 1.f, 1.f, 1.f);  // X above is published D^-1-scaled
+            if (!below) sc = make_float4(rpiv[4 * j], rpiv[4 * j + 1], rpiv[4 * j + 2], rpiv[4 * j + 3]);
 #pragma unroll
-                for (int i = 0; i < 4; i++) m[i] = reinterpret_cast<const float4*>(Dr + 32)[i];
-                float4 t[4] = {w[0], w[1], w[2], w[3]};
-                mm4(w, t, m, false);
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const float4 v = w[i];
-                    reinterpret_cast<float4*>(Xb)[br * 4 + i] =
-                        make_float4(v.x * rpiv[4 * j], v.y * rpiv[4 * j + 1], v.z * rpiv[4 * j + 2], v.w * rpiv[4 * j + 3]);
-                }
+            for (int i = 0; i < 4; i++) {
+                if (below) a[i] = t[i]; else w[i] = t[i];
+                reinterpret_cast<float4*>(below ? Lb : Xb)[br * 4 + i] =
+                    make_float4(t[i].x * sc.x, t[i].y * sc.y, t[i].z * sc.z, t[i].w * sc.w);
             }
         }
         __syncthreads();
-        // ---- 3: the rest (the next diagonal block's owner then goes on to its step 1)
+        // ---- 3: the rest, one product per thread (L21 or D^-1-scaled X from
+        // the left, U12 or W's Y from the right), applied to A or to W; the
+        // next diagonal block's owner then goes on to its step 1
         {
-            float4 l[4], u[4];
-            if (br > j) {
+            const bool below = br > j, right = bc > j;
+            const bool act = below || (right && !CHOL);
+            if (act) {
+                const float* Lo = below ? Lb + br * 16 : Xb + br * 16;
+                const float* Ro = right ? Ub : Yb;
+                float4 l[4], u[4], t[4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) l[i] = reinterpret_cast<const float4*>(Lb)[br * 4 + i];
-                if (bc > j) {  // A -= L21 U12
-#pragma unroll
-                    for (int i = 0; i < 4; i++) u[i] = reinterpret_cast<const float4*>(Ub)[i * 16 + bc];
-                    mm4(a, l, u, true);
-                } else {  // Y -= L21 Y[j]
-#pragma unroll
-                    for (int i = 0; i < 4; i++) u[i] = reinterpret_cast<const float4*>(Yb)[i * 16 + bc];
-                    mm4(w, l, u, true);
+                for (int i = 0; i < 4; i++) {
+                    l[i] = reinterpret_cast<const float4*>(Lo)[i];
+                    u[i] = reinterpret_cast<const float4*>(Ro)[i * 16 + bc];
                 }
-            } else if (!CHOL && bc > j) {  // X -= X[j] D^-1 U12
+                mm4(t, l, u, false);
+                const bool to_a = below && right;
 #pragma unroll
-                for (int i = 0; i < 4; i++) l[i] = reinterpret_cast<const float4*>(Xb)[br * 4 + i];
-#pragma unroll
-                for (int i = 0; i < 4; i++) u[i] = reinterpret_cast<const float4*>(Ub)[i * 16 + bc];
-                mm4(w, l, u, true);
+                for (int i = 0; i < 4; i++) {
+                    float4& d = to_a ? a[i] : w[i];
+                    d.x -= t[i].x; d.y -= t[i].y; d.z -= t[i].z; d.w -= t[i].w;
+                }
             }
         }
     }

@@ -91,6 +91,9 @@ int factor_persistent_grid(bool fp64, int stages, int num_sms);
 void scatter_values_launch(const double* V, const int32_t* vidx, const int32_t* tile, const int16_t* off, int64_t nnz,
                            const int32_t* pad_tile, const int16_t* pad_off, int64_t npad, double* tiles64,
                            float* tiles32, cudaStream_t s);
+// dst tile k+1 = src tile ids[k] (k < n), tiles of tile_bytes bytes
+void gather_tiles_launch(const void* src, void* dst, const int32_t* ids, int64_t n, uint64_t tile_bytes,
+                         cudaStream_t s);
 // FP64 input tiles -> FP32 input tiles (first n elements)
 void convert_tiles_launch(const double* src, float* dst, int64_t n, cudaStream_t s);
 void widen_tiles_launch(const float* src, double* dst, int64_t n, cudaStream_t s);

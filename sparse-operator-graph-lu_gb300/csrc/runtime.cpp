@@ -213,6 +213,15 @@ struct sog_system {
     uint64_t trace_bytes = 0;
     DevStatus last{};
     std::vector<Leaf> L, U;
+    // resident compaction (sog_options.resident_compact): after a
+    // factorisation only the tiles the substitution reads stay resident, in
+    // their own allocation; the next factorisation allocates the full set again
+    std::vector<int32_t> sol_ids[8];  // host copies of l_id, u_id, l_diag, u_diag, l_dinv, u_dinv, l_la, u_la
+    bool compacted = false;
+    char* cbuf = nullptr;  // compact tiles (slot 0 unused), then the remapped id arrays
+    uint64_t cbuf_bytes = 0;
+    DevSolve ds_full{};
+    std::vector<int32_t> cmap;  // block id -> compact slot while compacted
 };
 
 namespace {
@@ -523,10 +532,90 @@ int check_pivots(sog_system* s) {
     return SOG_OK;
 }
 
+// Keep only the substitution's tiles (L/U leaves, diagonal inverses,
+// look-ahead products): gathered into a compact allocation, the id arrays of
+// the solve remapped, the full tile set returned to the pool. Without room
+// for the compact copy the system simply stays as it is.
+int compact_tiles(sog_system* s) {
+    sog_ctx* c = s->ctx;
+    const uint64_t tile = 4096 * elem_bytes(s->opt);
+    std::vector<int32_t> need;
+    for (auto& v : s->sol_ids)
+        for (int32_t id : v)
+            if (id > 0) need.push_back(id);
+    for (const Leaf& lf : s->L) need.push_back(lf.id);
+    for (const Leaf& lf : s->U) need.push_back(lf.id);
+    std::sort(need.begin(), need.end());
+    need.erase(std::unique(need.begin(), need.end()), need.end());
+    std::vector<int32_t> cmap(s->storage, 0);
+    for (size_t k = 0; k < need.size(); k++) cmap[need[k]] = (int32_t)k + 1;
+    std::vector<int32_t> remap[8];
+    Layout Lc;
+    const uint64_t o_t = Lc.add<char>((need.size() + 1) * tile), o_need = Lc.add<int32_t>(need.size());
+    uint64_t o_ids[8];
+    for (int a = 0; a < 8; a++) {
+        remap[a].resize(s->sol_ids[a].size());
+        for (size_t k = 0; k < remap[a].size(); k++) remap[a][k] = s->sol_ids[a][k] > 0 ? cmap[s->sol_ids[a][k]] : 0;
+        o_ids[a] = Lc.add<int32_t>(remap[a].size());
+    }
+    char* buf = static_cast<char*>(c->pool.alloc(Lc.off));
+    if (!buf) return SOG_OK;
+    cudaStream_t st = s->stream;
+    int32_t* d_need = put(buf, o_need, need, st);
+    s->launches++;
+    gather_tiles_launch(s->tiles, buf + o_t, d_need, (int64_t)need.size(), tile, st);
+    const int32_t* d_ids[8];
+    for (int a = 0; a < 8; a++) d_ids[a] = remap[a].empty() ? nullptr : put(buf, o_ids[a], remap[a], st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        const std::string m = cudaGetErrorString(cudaGetLastError());
+        c->pool.release(buf, Lc.off);
+        return fail(SOG_ECUDA, "compaction: " + m);
+    }
+    c->pool.release(s->tiles, s->tiles_bytes);
+    s->ds_full = s->ds;
+    s->ds.l_id = d_ids[0];
+    s->ds.u_id = d_ids[1];
+    s->ds.l_diag = d_ids[2];
+    s->ds.u_diag = d_ids[3];
+    s->ds.l_dinv = d_ids[4];
+    s->ds.u_dinv = d_ids[5];
+    s->ds.l_la = d_ids[6];
+    s->ds.u_la = d_ids[7];
+    s->tiles = buf + o_t;
+    s->cbuf = buf;
+    s->cbuf_bytes = Lc.off;
+    s->cmap.swap(cmap);
+    s->compacted = true;
+    return SOG_OK;
+}
+
+// before a factorisation of a compacted system: the full tile set again
+int uncompact_tiles(sog_system* s) {
+    if (!s->compacted) return SOG_OK;
+    sog_ctx* c = s->ctx;
+    CK(cudaStreamSynchronize(s->stream));
+    void* t = c->pool.alloc(s->tiles_bytes);
+    if (!t) return fail(SOG_ENOMEM, "block pool exhausted (tiles for the refactorisation)");
+    c->pool.release(s->cbuf, s->cbuf_bytes);
+    s->cbuf = nullptr;
+    s->cbuf_bytes = 0;
+    s->tiles = t;
+    s->ds = s->ds_full;
+    s->cmap.clear();
+    s->compacted = false;
+    return SOG_OK;
+}
+
 int factor_checked(sog_system* s) {
     const int r = run_factor(s);
     if (r) return r;
-    return check_pivots(s);
+    const int pr = check_pivots(s);
+    if (pr && pr != SOG_EPIVOT) return pr;
+    if (s->opt.resident_compact) {
+        const int cr = compact_tiles(s);
+        if (cr) return cr;
+    }
+    return pr;
 }
 
 void fill_pivot_stats(const sog_system* s, size_t k, sog_solve_stats& st) {
@@ -953,6 +1042,14 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     for (const Leaf& lf : loff) { lptr[lf.bi + 1]++; lcol.push_back(lf.bj); lid.push_back(lf.id); }
     for (const Leaf& lf : uoff) { uptr[lf.bi + 1]++; ucol.push_back(lf.bj); uid.push_back(lf.id); }
     for (int i = 0; i < s->R; i++) { lptr[i + 1] += lptr[i]; uptr[i + 1] += uptr[i]; }
+    s->sol_ids[0] = lid;
+    s->sol_ids[1] = uid;
+    s->sol_ids[2] = ldiag;
+    s->sol_ids[3] = udiag;
+    s->sol_ids[4] = ldinv;
+    s->sol_ids[5] = udinv;
+    s->sol_ids[6] = lla;
+    s->sol_ids[7] = ula;
     std::vector<int32_t> order = static_order(g, s->fp64);
     // mixed path: the ordered executor starts a product before its last
     // producer finished (item bit 3), waiting per operand pair; every pair
@@ -1203,7 +1300,8 @@ void sog_system_destroy(sog_system* s) {
     sog_ctx* c = s->ctx;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(s->stream);
-    c->pool.release(s->tiles, s->tiles_bytes);
+    if (s->compacted) c->pool.release(s->cbuf, s->cbuf_bytes);
+    else c->pool.release(s->tiles, s->tiles_bytes);
     c->pool.release(s->aux, s->aux_bytes);
     c->pool.release(s->vecs, s->vec_bytes);
     c->pool.release(s->trace, s->trace_bytes);
@@ -1231,6 +1329,7 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
     if (!V_dev && s->ntrip) return fail(SOG_EINVAL, "NULL values");
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
+    if (int r = uncompact_tiles(s)) return r;
     cudaStream_t st = s->stream;
     const uint64_t eb = elem_bytes(s->opt);
     CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
@@ -1262,6 +1361,7 @@ int sog_factor_tiles(sog_system* s, const double* tiles) {
     if (!s || !tiles) return fail(SOG_EINVAL, "NULL argument");
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
+    if (int r = uncompact_tiles(s)) return r;
     const uint64_t n = (uint64_t)s->n_input * 4096;
     // max |a| over the given tiles, one figure for every system of the plan
     // (it includes the unit diagonal the planner puts on padding rows)
@@ -1361,7 +1461,8 @@ int sog_system_export_factors(sog_system* s, double* ltiles, double* utiles) {
         double* dst = side == 0 ? ltiles : utiles;
         if (!dst || (side == 1 && s->symmetric)) continue;  // LL^T: the plan has no U leaves
         for (size_t k = 0; k < lv.size(); k++) {
-            const char* src = (const char*)s->tiles + (uint64_t)lv[k].id * 4096 * eb;
+            const int32_t id = s->compacted ? s->cmap[lv[k].id] : lv[k].id;
+            const char* src = (const char*)s->tiles + (uint64_t)id * 4096 * eb;
             if (s->fp64) {
                 CK(cudaMemcpy(dst + k * 4096, src, 4096 * 8, cudaMemcpyDeviceToHost));
             } else {

@@ -445,6 +445,8 @@ int sog_server_create(sog_ctx* ctx, const sog_options* opt, const sog_server_opt
         s->opt.max_refine = 10;
         s->opt.tol = 1e-10;
     }
+    // resident requests keep only what their further solves read
+    s->opt.resident_compact = 1;
     if (sopt) s->sopt = *sopt;
     const int np = s->sopt.planner_threads > 0 ? s->sopt.planner_threads : 2;
     const int nl = s->sopt.lanes > 0 ? s->sopt.lanes : 2;

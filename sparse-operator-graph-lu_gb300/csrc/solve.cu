@@ -420,6 +420,14 @@ __global__ void absmax_kernel(const double* __restrict__ v, int64_t n, unsigned 
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
+__global__ void gather_tiles_kernel(const int4* __restrict__ src, int4* __restrict__ dst, const int32_t* ids,
+                                    int64_t n, int per_tile) {
+    const int64_t tot = n * per_tile;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = e / per_tile, o = e - k * per_tile;
+        dst[(k + 1) * per_tile + o] = __ldcg(src + (int64_t)ids[k] * per_tile + o);
+    }
+}
 __global__ void cast_seg_kernel(const double* __restrict__ src, float* __restrict__ dst, int n_ext, int nc,
                                 DevSegs g) {
     const int64_t tot = (int64_t)n_ext * nc;
@@ -488,6 +496,12 @@ void residual_seg_launch(const DevCSR& A, const double* b, const double* x, doub
 }
 void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s) {
     if ((int64_t)n_ext * nc > 0) cast_seg_kernel<<<608, 256, 0, s>>>(src, dst, n_ext, nc, g);
+}
+void gather_tiles_launch(const void* src, void* dst, const int32_t* ids, int64_t n, uint64_t tile_bytes,
+                         cudaStream_t s) {
+    if (n > 0)
+        gather_tiles_kernel<<<1216, 256, 0, s>>>(static_cast<const int4*>(src), static_cast<int4*>(dst), ids, n,
+                                                 (int)(tile_bytes / 16));
 }
 void csr_absmax_seg_launch(const DevCSR& A, const DevSegs& g, unsigned long long* out, cudaStream_t s) {
     if (A.n > 0) csr_absmax_seg_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A, g, out);

@@ -264,3 +264,34 @@ def test_solveLU_symmetric_matches_reference(sg, wl):
     g = golden("spd_lap2d_32")
     x = sg.solveLU(s.n, s.rows, s.cols, s.vals, rhs_of(s), symmetric=True)
     assert rel(x, g["x"]) <= 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_resident_compaction(sg, wl, ctx, precision):
+    """resident_compact: after the factorisation only the substitution's
+    tiles stay in the block pool (L/U leaves, diagonal inverses, look-ahead
+    products); solutions and exported factors are bit for bit those of the
+    full system, and a refactorisation reallocates and works again."""
+    prec = sg.FP64 if precision == "fp64" else sg.MIXED
+    s = wl.varcoef3d(20)
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    full = sg.System(ctx, p, precision=prec)
+    full.factor(s.vals)
+    xf, _ = full.solve(s.b)
+    Lf, Uf = full.export_factors()
+    comp = sg.System(ctx, p, precision=prec, resident_compact=True)
+    used0, _ = ctx.pool_usage()
+    comp.factor(s.vals)
+    used1, _ = ctx.pool_usage()
+    assert used1 < used0  # the full tile set went back to the pool
+    xc, _ = comp.solve(s.b)
+    np.testing.assert_array_equal(xc, xf)
+    Lc, Uc = comp.export_factors()
+    np.testing.assert_array_equal(Lc, Lf)
+    np.testing.assert_array_equal(Uc, Uf)
+    v2 = s.vals * 1.5
+    full.factor(v2)
+    comp.factor(v2)
+    np.testing.assert_array_equal(comp.solve(s.b)[0], full.solve(s.b)[0])
+    full.close()
+    comp.close()
