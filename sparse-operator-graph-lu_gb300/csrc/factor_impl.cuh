@@ -553,292 +553,6 @@ __device__ void lu_task_f2(const DevTasks& tk, float* __restrict__ tiles, int ta
     if (tid < 32) pivot_stats<float, CHOL>(tk, task, raw, piv, rpiv, !CHOL && uinv > 0, s_maxa, s_maxu, anybad);
 }
 
-// ---------------------------------------------------------------- FP32 LU in 4x4 blocks
-// The mixed path's LU / LL^T task with both triangular inverses, blocked in
-// 4x4 blocks so that the 64 dependent pivot steps run in registers of one
-// thread, 4 at a time, instead of one CTA barrier per pivot. Thread t owns
-// block (t >> 4, t & 15) of the tile A (16 values) and of W (16 values; L^-1
-// on and below the diagonal, X = (D^-1 U)^-1 above, identity at the start:
-// the same fused elimination as ludcmpSimple followed by inv_lower /
-// inv_upper, MatrixStdDouble.cpp:2711-2866). Micro-step j (pivots 4j..4j+3):
-//   1  the owner of the diagonal block factors it alone: L_D U_D with the
-//      clamp, Y_D = L_D^-1, X_D, U_D^-1 = X_D D^-1, and publishes them;
-//   2  block column j below: L21 = A21 U_D^-1; block row j right: U12 = Y_D A12;
-//      W's block row j left: Y = Y_D Y; W's block column j above: X = X X_D
-//      (each owner updates its own block and publishes it);
-//   3  every other block: A -= L21 U12, Y -= L21 Y[j], X -= X[j] D^-1 U12.
-// Step 3 of the next diagonal block's owner is followed at once by its step
-// 1, while the other threads finish step 3: two CTA barriers per 4 pivots.
-// U^-1 = X D^-1 at the end. Pivots below 1e-9 in magnitude are clamped to
-// +-1e-9 (MatrixStdDouble.cpp:2751-2761); LL^T (lltdcmpSimple,
-// MatrixStdDouble.cpp:2629-2668) runs the same elimination on the tile
-// symmetrised from its lower triangle with pivots below 1e-20 raised to it,
-// then L = L_lu diag(sqrt p), L^-1 = diag(1/sqrt p) L_lu^-1.
-constexpr int LU4_ELEMS = 4 * 256 + 3 * 16 + 3 * 64;  // published blocks, the diagonal block's results, pivots
-
-// 4x4 products on float4 rows: c (-)= a b
-__device__ __forceinline__ void mm4(float4 (&c)[4], const float4 (&a)[4], const float4 (&b)[4], bool sub) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float av[4] = {a[i].x, a[i].y, a[i].z, a[i].w};
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            t.x = fmaf(av[k], b[k].x, t.x); t.y = fmaf(av[k], b[k].y, t.y);
-            t.z = fmaf(av[k], b[k].z, t.z); t.w = fmaf(av[k], b[k].w, t.w);
-        }
-        if (sub) { c[i].x -= t.x; c[i].y -= t.y; c[i].z -= t.z; c[i].w -= t.w; }
-        else c[i] = t;
-    }
-}
-__device__ __forceinline__ float& el(float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
-
-template <bool CHOL>
-__device__ void lu_task_r4(const DevTasks& tk, float* __restrict__ tiles, int task, int32_t in, int32_t lo, int32_t up,
-                           int32_t linv, int32_t uinv, float* sm) {
-    float* Lb = sm;          // [16 block rows][4][4]: L21 of block column j / scaled X of W's block column j
-    float* Xb = sm + 256;    //   (Xb: X[r][j] D^-1)
-    float* Ub = sm + 512;    // [4][16 block columns][4]: U12 of block row j / Y of W's block row j
-    float* Yb = sm + 768;
-    float* Dr = sm + 1024;   // the diagonal block's Y_D, U_D^-1, X_D (16 each)
-    float* piv = Dr + 48;    // clamped pivots
-    float* rpiv = piv + 64;  // their reciprocals
-    float* raw = rpiv + 64;  // pivots before the clamp
-    __shared__ float s_maxa, s_maxu;
-    const int tid = threadIdx.x, lane = tid & 31, br = tid >> 4, bc = tid & 15;
-    if (tid == 0) { s_maxa = 0.f; s_maxu = 0.f; }
-    float4 a[4], w[4];
-    float ma = 0.f;
-    {
-        const float* A = tiles + (size_t)in * 4096;
-        if (!CHOL || bc < br) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = __ldcg(reinterpret_cast<const float4*>(A + (4 * br + i) * 64 + 4 * bc));
-        } else if (bc > br) {  // the upper triangle mirrors the lower one
-            float4 t[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) t[i] = __ldcg(reinterpret_cast<const float4*>(A + (4 * bc + i) * 64 + 4 * br));
-#pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = make_float4(el(t[0], i), el(t[1], i), el(t[2], i), el(t[3], i));
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = __ldcg(reinterpret_cast<const float4*>(A + (4 * br + i) * 64 + 4 * bc));
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int k = i + 1; k < 4; k++) el(a[i], k) = el(a[k], i);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            ma = fmaxf(ma, fmaxf(fmaxf(fabsf(a[i].x), fabsf(a[i].y)), fmaxf(fabsf(a[i].z), fabsf(a[i].w))));
-            w[i] = make_float4(br == bc && i == 0 ? 1.f : 0.f, br == bc && i == 1 ? 1.f : 0.f,
-                               br == bc && i == 2 ? 1.f : 0.f, br == bc && i == 3 ? 1.f : 0.f);
-        }
-    }
-    __syncthreads();  // s_maxa / s_maxu initialised
-#pragma unroll 1
-    for (int j = 0; j < 16; j++) {
-        // ---- 1: the diagonal block, by its owner (it has applied its step 3 already)
-        if (br == j && bc == j) {
-            const float tiny = 1e-9f;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const float akk = el(a[k], k);
-                const float pv = CHOL ? (akk < 1e-20f ? 1e-20f : akk)
-                                      : ((akk < tiny && akk > -tiny) ? (akk < 0.f ? -tiny : tiny) : akk);
-                const float rp = rcp_approx(pv);
-                piv[4 * j + k] = pv;
-                rpiv[4 * j + k] = rp;
-                raw[4 * j + k] = akk;
-#pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    if (r > k) {  // eliminate below the pivot; row operations on L^-1
-                        const float l = el(a[r], k) * rp;
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            if (c > k) el(a[r], c) = fmaf(-l, el(a[k], c), el(a[r], c));
-                            else el(w[r], c) = fmaf(-l, el(w[k], c), el(w[r], c));
-                        }
-                        el(a[r], k) = l;
-                    } else {  // column operations on X for rows at or above the pivot
-                        const float xs = el(w[r], k) * rp;
-#pragma unroll
-                        for (int c = 0; c < 4; c++)
-                            if (c > k) el(w[r], c) = fmaf(-xs, el(a[k], c), el(w[r], c));
-                    }
-                }
-                el(a[k], k) = pv;  // U's diagonal: the clamped pivot
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                float4 y = w[i], x = w[i], u;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    if (c > i) el(y, c) = 0.f;
-                    if (c < i) el(x, c) = 0.f;
-                    el(u, c) = el(x, c) * rpiv[4 * j + c];
-                }
-                reinterpret_cast<float4*>(Dr)[i] = y;       // Y_D (unit lower)
-                reinterpret_cast<float4*>(Dr + 16)[i] = u;  // U_D^-1
-                reinterpret_cast<float4*>(Dr + 32)[i] = x;  // X_D (unit upper)
-                reinterpret_cast<float4*>(Yb)[i * 16 + j] = y;
-                reinterpret_cast<float4*>(Xb)[j * 4 + i] = u;
-            }
-        }
-        __syncthreads();
-        // ---- 2: block row and column j. Block row j multiplies its own
-        // block from the left by Y_D (U12 right of the diagonal, W's Y left of
-        // it), block column j from the right (L21 = A21 U_D^-1 below, W's
-        // X X_D above): one product per side, the operands chosen by select,
-        // so a warp runs at most two paths
-        if (br == j && bc != j) {
-            const bool right = bc > j;
-            float4 m[4], x[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                m[i] = reinterpret_cast<const float4*>(Dr)[i];
-                x[i] = right ? a[i] : w[i];
-            }
-            float4 t[4];
-            mm4(t, m, x, false);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                if (right) a[i] = t[i]; else w[i] = t[i];
-                reinterpret_cast<float4*>(right ? Ub : Yb)[i * 16 + bc] = t[i];
-            }
-        } else if (bc == j && br != j && (br > j || !CHOL)) {
-            const bool below = br > j;
-            float4 m[4], x[4];
-            const float* M = Dr + (below ? 16 : 32);  // U_D^-1 / X_D
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                m[i] = reinterpret_cast<const float4*>(M)[i];
-                x[i] = below ? a[i] : w[i];
-            }
-            float4 t[4];
-            mm4(t, x, m, false);
-            float4 sc = make_float4(1.f, 1.f, 1.f, 1.f);  // X above is published D^-1-scaled
-            if (!below) sc = make_float4(rpiv[4 * j], rpiv[4 * j + 1], rpiv[4 * j + 2], rpiv[4 * j + 3]);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                if (below) a[i] = t[i]; else w[i] = t[i];
-                reinterpret_cast<float4*>(below ? Lb : Xb)[br * 4 + i] =
-                    make_float4(t[i].x * sc.x, t[i].y * sc.y, t[i].z * sc.z, t[i].w * sc.w);
-            }
-        }
-        __syncthreads();
-        // ---- 3: the rest, one product per thread (L21 or D^-1-scaled X from
-        // the left, U12 or W's Y from the right), applied to A or to W; the
-        // next diagonal block's owner then goes on to its step 1
-        {
-            const bool below = br > j, right = bc > j;
-            const bool act = below || (right && !CHOL);
-            if (act) {
-                const float* Lo = below ? Lb + br * 16 : Xb + br * 16;
-                const float* Ro = right ? Ub : Yb;
-                float4 l[4], u[4], t[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    l[i] = reinterpret_cast<const float4*>(Lo)[i];
-                    u[i] = reinterpret_cast<const float4*>(Ro)[i * 16 + bc];
-                }
-                mm4(t, l, u, false);
-                const bool to_a = below && right;
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    float4& d = to_a ? a[i] : w[i];
-                    d.x -= t[i].x; d.y -= t[i].y; d.z -= t[i].z; d.w -= t[i].w;
-                }
-            }
-        }
-    }
-    // ---- outputs (each thread its blocks, 16-byte rows: coalesced over the block columns)
-    float mu = 0.f;
-    bool bad = false;
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto row_of = [&](float* base, int i) { return reinterpret_cast<float4*>(base + (4 * br + i) * 64 + 4 * bc); };
-    if (CHOL) {
-        float sc[4], sr[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) sc[c] = sqrtf(piv[4 * bc + c]);
-#pragma unroll
-        for (int i = 0; i < 4; i++) sr[i] = sqrtf(piv[4 * br + i]);
-        float* Lt = tiles + (size_t)lo * 4096;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            float4 v = z4;
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                const int gr = 4 * br + i, gc = 4 * bc + c;
-                el(v, c) = gr > gc ? el(a[i], c) * sc[c] : (gr == gc ? sr[i] : 0.f);
-                mu = fmaxf(mu, fabsf(el(v, c)));
-            }
-            *row_of(Lt, i) = v;
-        }
-        if (linv > 0) {
-            float* Wt = tiles + (size_t)linv * 4096;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                float4 v = z4;
-                const float isr = 1.f / sr[i];
-#pragma unroll
-                for (int c = 0; c < 4; c++) el(v, c) = 4 * bc + c <= 4 * br + i ? el(w[i], c) * isr : 0.f;
-                *row_of(Wt, i) = v;
-            }
-        }
-    } else {
-        float* Lt = tiles + (size_t)lo * 4096;
-        float* Ut = tiles + (size_t)up * 4096;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            float4 lv = z4, uv = z4;
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                const int gr = 4 * br + i, gc = 4 * bc + c;
-                el(lv, c) = gr > gc ? el(a[i], c) : (gr == gc ? 1.f : 0.f);
-                el(uv, c) = gr <= gc ? el(a[i], c) : 0.f;
-                mu = fmaxf(mu, fabsf(el(uv, c)));
-                bad = bad || !isfinite(el(uv, c));
-            }
-            *row_of(Lt, i) = lv;
-            *row_of(Ut, i) = uv;
-        }
-        if (linv > 0) {
-            float* Wt = tiles + (size_t)linv * 4096;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                float4 v = z4;
-#pragma unroll
-                for (int c = 0; c < 4; c++) el(v, c) = 4 * bc + c <= 4 * br + i ? el(w[i], c) : 0.f;
-                *row_of(Wt, i) = v;
-            }
-        }
-        if (uinv > 0) {
-            float* Vt = tiles + (size_t)uinv * 4096;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                float4 v = z4;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    el(v, c) = 4 * bc + c >= 4 * br + i ? el(w[i], c) * rpiv[4 * bc + c] : 0.f;
-                    bad = bad || !isfinite(el(v, c));
-                }
-                *row_of(Vt, i) = v;
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        ma = fmaxf(ma, __shfl_xor_sync(FULL, ma, o));
-        mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
-    }
-    if (lane == 0) {
-        atomicMax(reinterpret_cast<int*>(&s_maxa), __float_as_int(ma));
-        atomicMax(reinterpret_cast<int*>(&s_maxu), __float_as_int(mu));
-    }
-    const bool anybad = __syncthreads_or(bad) != 0;
-    if (tid < 32) pivot_stats<float, CHOL>(tk, task, raw, piv, rpiv, !CHOL && uinv > 0, s_maxa, s_maxu, anybad);
-}
-
 // ---------------------------------------------------------------- triangular inverses
 // Y = L^-1 by forward elimination on the identity, Y = U^-1 by backward
 // elimination, the working rows held in registers (thread t owns row t>>2,
