@@ -186,6 +186,8 @@ int sog_plan_segments(const sog_plan *plan, int32_t *count, int32_t *n);
  * The device block-pool arena that replaces memutil's per-thread block pools
  * (memutil.cpp:74-113). pool_bytes = 0: 90% of free device memory. */
 int sog_ctx_create(int32_t device, uint64_t pool_bytes, sog_ctx **out);
+/* Destroy every system and server of the context first: they use its stream
+ * and pool. */
 void sog_ctx_destroy(sog_ctx *ctx);
 /* bytes of the pool in use / total */
 int sog_ctx_pool_usage(const sog_ctx *ctx, uint64_t *used, uint64_t *total);

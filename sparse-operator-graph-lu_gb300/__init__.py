@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -253,6 +254,9 @@ class Context:
 
     def __init__(self, device: int = 0, pool_bytes: int = 0):
         self._h = C.c_void_p()
+        # systems and servers on this context: closed before the context, in
+        # whatever order the interpreter finalises objects
+        self._children = weakref.WeakSet()
         _check(lib().sog_ctx_create(device, pool_bytes, C.byref(self._h)))
 
     def stream(self) -> int:
@@ -268,6 +272,8 @@ class Context:
 
     def close(self):
         if getattr(self, "_h", None):
+            for child in list(getattr(self, "_children", ())):
+                child.close()
             lib().sog_ctx_destroy(self._h)
             self._h = None
 
@@ -293,6 +299,7 @@ class System:
                            pipeline_stages=pipeline_stages, growth_limit=growth_limit, max_ctas=max_ctas,
                            resident_compact=int(resident_compact))
         _check(lib().sog_system_create(ctx._h, plan._h, C.byref(self.opt), C.byref(self._h)))
+        ctx._children.add(self)
 
     @staticmethod
     def _factor_rc(rc: int, allow_epivot: bool) -> int:
@@ -467,6 +474,7 @@ class Server:
                                   batch_window_ms=batch_window_ms, lanes=lanes)
         self._n = {}
         _check(lib().sog_server_create(ctx._h, C.byref(self.opt), C.byref(self.sopt), C.byref(self._h)))
+        ctx._children.add(self)
 
     def submit(self, n: int, rows, cols, vals, b, symmetric: bool = False) -> int:
         r = np.ascontiguousarray(rows, dtype=np.int32)
