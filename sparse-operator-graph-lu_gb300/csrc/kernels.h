@@ -118,8 +118,9 @@ struct DevSolve {
     // systems so that consecutive positions are independent rows.
     const int32_t *order_l, *order_u;
     // optional look-ahead products per block row (block id of Dinv_i L_{i,i-1}
-    // / Dinv_i U_{i,i+1}, 0 = none); NULL = none
-    const int32_t *l_la, *u_la;
+    // / Dinv_i U_{i,i+1}, 0 = none; l_la2 / u_la2: Dinv_i L_{i,i-2} /
+    // Dinv_i U_{i,i+2}); NULL = none
+    const int32_t *l_la, *u_la, *l_la2, *u_la2;
     // position claim counters of the lower and upper launch (zeroed before
     // each launch pair): CTAs claim positions in dealing order as they become
     // resident, so a launch needs no co-residency of all its CTAs (systems on

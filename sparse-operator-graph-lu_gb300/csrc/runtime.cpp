@@ -216,7 +216,7 @@ struct sog_system {
     // resident compaction (sog_options.resident_compact): after a
     // factorisation only the tiles the substitution reads stay resident, in
     // their own allocation; the next factorisation allocates the full set again
-    std::vector<int32_t> sol_ids[8];  // host copies of l_id, u_id, l_diag, u_diag, l_dinv, u_dinv, l_la, u_la
+    std::vector<int32_t> sol_ids[10];  // host copies of l_id, u_id, l_diag, u_diag, l_dinv, u_dinv, l_la, u_la, l_la2, u_la2
     bool compacted = false;
     char* cbuf = nullptr;  // compact tiles (slot 0 unused), then the remapped id arrays
     uint64_t cbuf_bytes = 0;
@@ -549,11 +549,11 @@ int compact_tiles(sog_system* s) {
     need.erase(std::unique(need.begin(), need.end()), need.end());
     std::vector<int32_t> cmap(s->storage, 0);
     for (size_t k = 0; k < need.size(); k++) cmap[need[k]] = (int32_t)k + 1;
-    std::vector<int32_t> remap[8];
+    std::vector<int32_t> remap[10];
     Layout Lc;
     const uint64_t o_t = Lc.add<char>((need.size() + 1) * tile), o_need = Lc.add<int32_t>(need.size());
-    uint64_t o_ids[8];
-    for (int a = 0; a < 8; a++) {
+    uint64_t o_ids[10];
+    for (int a = 0; a < 10; a++) {
         remap[a].resize(s->sol_ids[a].size());
         for (size_t k = 0; k < remap[a].size(); k++) remap[a][k] = s->sol_ids[a][k] > 0 ? cmap[s->sol_ids[a][k]] : 0;
         o_ids[a] = Lc.add<int32_t>(remap[a].size());
@@ -564,8 +564,8 @@ int compact_tiles(sog_system* s) {
     int32_t* d_need = put(buf, o_need, need, st);
     s->launches++;
     gather_tiles_launch(s->tiles, buf + o_t, d_need, (int64_t)need.size(), tile, st);
-    const int32_t* d_ids[8];
-    for (int a = 0; a < 8; a++) d_ids[a] = remap[a].empty() ? nullptr : put(buf, o_ids[a], remap[a], st);
+    const int32_t* d_ids[10];
+    for (int a = 0; a < 10; a++) d_ids[a] = remap[a].empty() ? nullptr : put(buf, o_ids[a], remap[a], st);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         const std::string m = cudaGetErrorString(cudaGetLastError());
         c->pool.release(buf, Lc.off);
@@ -581,6 +581,8 @@ int compact_tiles(sog_system* s) {
     s->ds.u_dinv = d_ids[5];
     s->ds.l_la = d_ids[6];
     s->ds.u_la = d_ids[7];
+    s->ds.l_la2 = d_ids[8];
+    s->ds.u_la2 = d_ids[9];
     s->tiles = buf + o_t;
     s->cbuf = buf;
     s->cbuf_bytes = Lc.off;
@@ -918,7 +920,7 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     // + the transposed L leaves of an LL^T plan
     bool any_sym = p.symmetric;
     for (const Segment& sg : p.segs) any_sym = any_sym || sg.symmetric;
-    uint64_t tiles = ((uint64_t)p.storage_count + 4ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
+    uint64_t tiles = ((uint64_t)p.storage_count + 6ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
                      elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
@@ -967,7 +969,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // below (inverses, look-ahead products, transposed leaves), so the op
     // records are copied once.
     std::vector<Op> ops2;
-    ops2.reserve(p.ops.size() + 4 * (size_t)p.cfg.block_rows + p.L.size());
+    ops2.reserve(p.ops.size() + 6 * (size_t)p.cfg.block_rows + p.L.size());
     ops2.assign(p.ops.begin(), p.ops.end());
     int32_t storage2 = p.storage_count;
     // LL^T systems: the upper factor of the substitution is L^T (upperSolverT,
@@ -995,16 +997,19 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     }
     std::vector<int32_t> ldinv, udinv;
     add_diag_inverses(ops2, storage2, s->R, s->L, s->U, ldinv, udinv);
-    std::vector<int32_t> lla, ula;
-    if (o.solve_lookahead >= 0) add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla, ula);
+    std::vector<int32_t> lla, ula, lla2, ula2;
+    if (o.solve_lookahead >= 0) {
+        add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla, ula);
+        add_lookahead2_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla2, ula2);
+    }
     s->storage = storage2;
     std::vector<int32_t> outputs;
     for (const Leaf& lf : s->L) outputs.push_back(lf.id);
     for (const Leaf& lf : s->U) outputs.push_back(lf.id);
     for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
-    for (int32_t id : lla) if (id > 0) outputs.push_back(id);
-    for (int32_t id : ula) if (id > 0) outputs.push_back(id);
+    for (auto* v : {&lla, &ula, &lla2, &ula2})
+        for (int32_t id : *v) if (id > 0) outputs.push_back(id);
     try {
         s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts, true, !s->fp64);
         if (!s->fp64) order_pairs_by_ready(s->tg, false);
@@ -1017,7 +1022,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // value lives in its source's tile
     for (Leaf& lf : s->L) lf.id = g.alias[lf.id];
     for (Leaf& lf : s->U) lf.id = g.alias[lf.id];
-    for (auto* v : {&ldinv, &udinv, &lla, &ula})
+    for (auto* v : {&ldinv, &udinv, &lla, &ula, &lla2, &ula2})
         for (int32_t& id : *v)
             if (id > 0) id = g.alias[id];
     // solve structure
@@ -1050,6 +1055,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->sol_ids[5] = udinv;
     s->sol_ids[6] = lla;
     s->sol_ids[7] = ula;
+    s->sol_ids[8] = lla2;
+    s->sol_ids[9] = ula2;
     std::vector<int32_t> order = static_order(g, s->fp64);
     // mixed path: the ordered executor starts a product before its last
     // producer finished (item bit 3), waiting per operand pair; every pair
@@ -1158,6 +1165,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()), o_claim = L.add<int32_t>(2),
+             o_lla2 = L.add<int32_t>(lla2.size()), o_ula2 = L.add<int32_t>(ula2.size()),
              o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
              o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
              o_done = L.add<int32_t>(g.ntasks), o_piv = L.add<DevPivot>(ns), o_piv0 = L.add<DevPivot>(ns),
@@ -1259,6 +1267,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     ds.order_u = ord_u.empty() ? nullptr : put(A, o_ordu, ord_u, st);
     ds.l_la = lla.empty() ? nullptr : put(A, o_lla, lla, st);
     ds.u_la = ula.empty() ? nullptr : put(A, o_ula, ula, st);
+    ds.l_la2 = lla2.empty() ? nullptr : put(A, o_lla2, lla2, st);
+    ds.u_la2 = ula2.empty() ? nullptr : put(A, o_ula2, ula2, st);
     ds.claim = reinterpret_cast<int32_t*>(A + o_claim);
     if (cudaMallocHost(&s->h_red, sizeof(double) * RED * 64 * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_nrhs, sizeof(int32_t) * ns) != cudaSuccess ||

@@ -61,6 +61,26 @@ __device__ __forceinline__ Vec16<T> ldg16(const T* p) {
     return o;
 }
 
+// NR consecutive values of one row of vec, with 16-byte loads where the row
+// segment is 16-byte aligned (vec is written by other CTAs of the launch: L2
+// loads)
+template <typename T, int NR>
+__device__ __forceinline__ void load_row(const T* p, bool vec16, T (&o)[NR]) {
+    constexpr int PER = 16 / (int)sizeof(T);
+    if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
+        if (vec16) {
+#pragma unroll
+            for (int q = 0; q < NR / PER; q++) {
+                const int4 r = __ldcg(reinterpret_cast<const int4*>(p) + q);
+                memcpy(&o[q * PER], &r, 16);
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < NR; r++) o[r] = __ldcg(p + r);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -97,6 +117,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     const int* ids = lower ? s.l_id : s.u_id;
     const int* dinv = lower ? s.l_dinv : s.u_dinv;
     const int* lookahead = lower ? s.l_la : s.u_la;
+    const int* lookahead2 = lower ? s.l_la2 : s.u_la2;
+    const int dir = lower ? -1 : 1;  // the rows a row waits on lie on this side
     const int* order = lower ? s.order_l : s.order_u;
     if (tid == 0) { s_stop = 0; s_next = atomicAdd(s.claim + (lower ? 0 : 1), 1); }
     __syncthreads();
@@ -130,15 +152,16 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         fl = s.flags + (size_t)ch * R;
         if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
         const T* Dm = tiles + (size_t)dinv[i] * 4096;
-        const int la = lookahead ? lookahead[i] : 0;
+        const int la = lookahead ? lookahead[i] : 0, la2 = lookahead2 ? lookahead2[i] : 0;
         // warm L1 with this lane's slice of the diagonal inverse
         asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
         T pa[NR], pb[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
         bool stop = false;
-        // with a look-ahead product the last block (the neighbouring row) is left out
-        const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0);
+        // with look-ahead products the last blocks (the neighbouring rows i-1,
+        // i-2; the lists run in readiness order) are left out
+        const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0) - (la2 > 0 ? 1 : 0);
         for (int q = ptr[i] + warp; q < q1; q += 8) {
             const int j = col[q];
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
@@ -185,12 +208,15 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         // per row, each lane 16 columns; partial sums reduced over the four lanes
         {
             const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
+            const bool vec16 = ((size_t)ld * sizeof(T)) % 16 == 0 && ((size_t)c0 * sizeof(T)) % 16 == 0;
             Vec16<T> m[16 / VW];
             if (la > 0) {  // the look-ahead slice, loaded before the wait
                 const T* M = tiles + (size_t)la * 4096 + row * 64 + cb;
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++) m[c] = ldg16(M + c * VW);
             }
+            if (la2 > 0)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + (size_t)la2 * 4096 + row * 64 + cb));
             T y[NR];
 #pragma unroll
             for (int r = 0; r < NR; r++) y[r] = T(0);
@@ -202,18 +228,35 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
 #pragma unroll
                     for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
             }
-            // a wait that runs out sets s_stop: the CTA leaves together after
-            // the barrier below, publishing nothing
-            if (la > 0 && wait_row(lower ? i - 1 : i + 1)) {
-                const int j = lower ? i - 1 : i + 1;
+            // y -= M y_j over this lane's 16 columns (all warps: a 64x64 product
+            // split over the CTA instead of one warp's block product)
+            auto apply = [&](const Vec16<T>* mm, int j) {
                 const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++)
 #pragma unroll
-                    for (int v = 0; v < VW; v++)
+                    for (int v = 0; v < VW; v++) {
+                        T yj[NR];
+                        load_row<T, NR>(vj + (size_t)(c * VW + v) * ld, vec16, yj);
 #pragma unroll
-                        for (int r = 0; r < NR; r++) y[r] -= m[c].v[v] * __ldcg(vj + (size_t)(c * VW + v) * ld + r);
+                        for (int r = 0; r < NR; r++) y[r] -= mm[c].v[v] * yj[r];
+                    }
+            };
+            // row i-2 first (M2 = Dinv_i B_{i,i-2}), then row i-1 (M1); a wait
+            // that runs out sets s_stop: the CTA leaves together after the
+            // barrier below, publishing nothing
+            bool ok = true;
+            if (la2 > 0) {
+                ok = wait_row(i + 2 * dir);
+                if (ok) {
+                    Vec16<T> m2[16 / VW];
+                    const T* M = tiles + (size_t)la2 * 4096 + row * 64 + cb;
+#pragma unroll
+                    for (int c = 0; c < 16 / VW; c++) m2[c] = ldg16(M + c * VW);
+                    apply(m2, i + 2 * dir);
+                }
             }
+            if (ok && la > 0 && wait_row(i + dir)) apply(m, i + dir);
 #pragma unroll
             for (int r = 0; r < NR; r++) {
                 y[r] += __shfl_xor_sync(0xffffffffu, y[r], 1);

@@ -509,4 +509,25 @@ void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int bl
         }
 }
 
+void add_lookahead2_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows,
+                             const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
+                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2) {
+    lla2.assign(block_rows, 0);
+    ula2.assign(block_rows, 0);
+    int32_t seq = ops.empty() ? 0 : ops.back().seq;
+    const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    for (const Leaf& lf : L)
+        if (lf.bj == lf.bi - 2 && linv[lf.bi] > 0) {
+            const int32_t id = storage_count++;
+            ops.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            lla2[lf.bi] = id;
+        }
+    for (const Leaf& lf : U)
+        if (lf.bj == lf.bi + 2 && uinv[lf.bi] > 0) {
+            const int32_t id = storage_count++;
+            ops.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ula2[lf.bi] = id;
+        }
+}
+
 }  // namespace sog

@@ -104,5 +104,12 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64);
 void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula);
+// The same at distance 2: lla2[i] = Linv_ii * L_{i,i-2}, ula2[i] = Uinv_ii *
+// U_{i,i+2} (0 = none), so the block of row i-2 is applied by the whole
+// substitution CTA as soon as that row is published, and row i waits only on
+// its two neighbours' products.
+void add_lookahead2_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows,
+                             const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
+                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2);
 
 }  // namespace sog
