@@ -115,7 +115,7 @@ Plan merge_plans(const std::vector<const Plan*>& ps) {
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int64_t a, int64_t b) { return m.ops[a].stage < m.ops[b].stage; });
-    std::vector<Op> sorted;
+    OpVec sorted;
     sorted.reserve(m.ops.size());
     for (int64_t i : order) sorted.push_back(m.ops[i]);
     m.ops.swap(sorted);

@@ -9,7 +9,11 @@
 // BlockPlanner::solve on exactly the reference's workload.
 #pragma once
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace sog {
@@ -33,6 +37,23 @@ struct Op {
     int32_t op, src, src2, res, res2, stage;
     int32_t seq, group;
 };
+
+// Allocator that leaves default-constructed elements uninitialised, so that
+// sizing an op list of several hundred MB does not zero it first (the
+// planner fills it from several threads, which also spreads the page faults).
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind { using other = NoInitAlloc<U>; };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) { ::new ((void*)p) U; }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+using OpVec = std::vector<Op, NoInitAlloc<Op>>;
 
 struct Config {
     int n = 0;             // matrix dimension
@@ -73,7 +94,7 @@ struct Segment {
 struct Plan {
     Config cfg;
     Ordering ord;
-    std::vector<Op> ops;         // fine ops, sorted by stage as the reference executes them
+    OpVec ops;                   // fine ops, sorted by stage as the reference executes them
     int32_t storage_count = 0;   // block ids are 1..storage_count-1
     int32_t n_input = 0;         // input tiles carry ids 1..n_input
     std::vector<int32_t> input_bi, input_bj;  // block coordinates of input tiles (index id-1)

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <vector>
 
@@ -30,14 +31,37 @@ struct QNode {
     int32_t ch[4];  // 0 = b11, 1 = b12, 2 = b21, 3 = b22; 0 = absent
 };
 
+// Append-only op list in fixed-size chunks: growing it never moves the ops
+// already emitted (a 64^3 Laplacian emits 10.8M fine ops, 350 MB, which a
+// doubling vector would copy and re-fault at every growth step).
+struct OpLog {
+    static constexpr int SHIFT = 18;  // 256K ops (8 MB) per chunk
+    static constexpr int64_t MASK = (int64_t(1) << SHIFT) - 1;
+    std::vector<std::unique_ptr<Op[]>> chunks;
+    int64_t n = 0;
+    void push_back(const Op& o) {
+        if ((n >> SHIFT) == (int64_t)chunks.size()) chunks.emplace_back(new Op[size_t(1) << SHIFT]);
+        chunks[n >> SHIFT][n & MASK] = o;
+        n++;
+    }
+    int64_t size() const { return n; }
+    Op& operator[](int64_t i) { return chunks[i >> SHIFT][i & MASK]; }
+    const Op& operator[](int64_t i) const { return chunks[i >> SHIFT][i & MASK]; }
+};
+
 // Op emitter over one block-id space (one planning level).
 struct Emitter {
     std::vector<QNode> nodes;  // nodes[0] is the "absent" sentinel
-    std::vector<Op> ops;
+    OpLog ops;
     int32_t storage = 1;  // next block id; id 0 = none
     int32_t* seq;         // op sequence counter shared by both levels (operation.cpp:84-95)
 
-    explicit Emitter(int32_t* s) : seq(s) { nodes.push_back({-1, 0, {0, 0, 0, 0}}); }
+    // node_hint: expected node count, reserved up front (untouched capacity
+    // costs address space only)
+    Emitter(int32_t* s, size_t node_hint) : seq(s) {
+        nodes.reserve(node_hint);
+        nodes.push_back({-1, 0, {0, 0, 0, 0}});
+    }
 
     int32_t node(int level) {
         nodes.push_back({level, 0, {0, 0, 0, 0}});
@@ -332,16 +356,21 @@ struct OpOrder {
 };
 
 // Liveness, dead-op elimination, stage assignment and ordering
-// (BlockPlanner.cpp:103-374). `inputs` / `outputs` are block ids.
-void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>& inputs,
-              const std::vector<int32_t>& outputs, bool always_prune, int threads) {
+// (BlockPlanner.cpp:103-374). `inputs` / `outputs` are block ids. The
+// scheduled ops go to `out`, sorted by OpOrder; `log` gets its stages.
+void schedule(OpLog& log, int32_t storage, const std::vector<int32_t>& inputs, const std::vector<int32_t>& outputs,
+              bool always_prune, int threads, OpVec& out) {
+    const int nthr = threads > 0 ? threads : omp_get_max_threads();
+    const int64_t nops = log.size();
     std::vector<int32_t> lastuse(storage, 0), stage(storage, 0);
     stage[0] = 1;
     for (int32_t id : inputs) { stage[id] = 1; lastuse[id] = 0; }
     for (int32_t id : outputs) lastuse[id] = storage;
-    // backward liveness: a source is live if any op writing a live block reads it
-    for (int64_t i = (int64_t)ops.size() - 1; i >= 0; i--) {
-        const Op& o = ops[i];
+    // backward liveness: a source is live if any op writing a live block reads
+    // it. Every reader of a block comes after its writers, so an op's results
+    // have their final liveness when it is reached.
+    for (int64_t i = nops - 1; i >= 0; i--) {
+        const Op& o = log[i];
         int32_t mark = 0;
         if (o.res > 0) { mark = o.res; if (o.res2 > 0 && o.res2 > mark) mark = o.res2; }
         if (o.res > 0 && o.res2 > 0 && lastuse[o.res] == 0 && lastuse[o.res2] == 0) continue;
@@ -354,67 +383,95 @@ void schedule(std::vector<Op>& ops, int32_t storage, const std::vector<int32_t>&
             }
         }
     }
-    size_t waste = 0;
-    for (const Op& o : ops) {
-        if (lastuse[o.res] > 0) continue;
-        if (o.res2 > 0 && lastuse[o.res2] > 0) continue;
-        waste++;
-    }
-    if (always_prune || waste > ops.size() / 25) {
-        size_t w = 0;
-        for (size_t i = 0; i < ops.size(); i++) {
-            const Op& o = ops[i];
-            if (lastuse[o.res] > 0 || (o.res2 > 0 && lastuse[o.res2] > 0)) ops[w++] = o;
-        }
-        ops.resize(w);
-    }
-    // stage = 1 + max(stage of sources), at least 2 (BlockPlanner.cpp:225-266)
-    for (Op& o : ops) {
-        int32_t s = 0;
+    auto live = [&](const Op& o) { return lastuse[o.res] > 0 || (o.res2 > 0 && lastuse[o.res2] > 0); };
+    // stage = 1 + max(stage of sources), at least 2 (BlockPlanner.cpp:225-266),
+    // in op order. A dead op writes only dead blocks, which no live op reads,
+    // so giving dead ops stages too leaves every live op's stage as it is when
+    // the dead ones are removed first.
+    int64_t waste = 0;
+    for (int64_t i = 0; i < nops; i++) {
+        Op& o = log[i];
+        if (!live(o)) waste++;
+        int32_t st = 0;
         if (o.src > 0) {
-            s = std::max(stage[o.src] + 1, 2);
-            if (o.src2 > 0) s = std::max(s, stage[o.src2] + 1);
+            st = std::max(stage[o.src] + 1, 2);
+            if (o.src2 > 0) st = std::max(st, stage[o.src2] + 1);
         } else {
-            if (o.src2 > 0) s = std::max(s, stage[o.src2] + 1);
-            s = std::max(s, 2);
+            if (o.src2 > 0) st = std::max(st, stage[o.src2] + 1);
+            st = std::max(st, 2);
         }
-        o.stage = s;
-        if (o.res > 0 && stage[o.res] < s) stage[o.res] = s;
-        if (o.res2 > 0 && stage[o.res2] < s) stage[o.res2] = s;
+        o.stage = st;
+        if (o.res > 0 && stage[o.res] < st) stage[o.res] = st;
+        if (o.res2 > 0 && stage[o.res2] < st) stage[o.res2] = st;
     }
-    // every single-result writer of a block moves to that block's last write stage
-    for (int64_t i = (int64_t)ops.size() - 1; i >= 0; i--) {
-        Op& o = ops[i];
-        if (o.res2 > 0) continue;
-        if (o.res > 0 && stage[o.res] > o.stage) o.stage = stage[o.res];
+    const bool prune = always_prune || waste > nops / 25;
+    // kept ops, each single-result writer moved to its block's last write
+    // stage, bucketed by stage: a counting sort over contiguous slices of the
+    // log, one per thread (the order within a stage is fixed by the sort below)
+    const int nslice = (int)std::max<int64_t>(1, std::min<int64_t>(nthr, nops / 65536 + 1));
+    std::vector<int32_t> slice_max(nslice, 0);
+    std::vector<std::vector<int64_t>> cnt(nslice);
+    auto final_stage = [&](const Op& o) {
+        return (o.res2 == 0 && o.res > 0 && stage[o.res] > o.stage) ? stage[o.res] : o.stage;
+    };
+    auto slice_lo = [&](int k) { return nops * k / nslice; };
+#pragma omp parallel for schedule(static, 1) num_threads(nslice)
+    for (int k = 0; k < nslice; k++) {
+        int32_t mx = 0;
+        for (int64_t i = slice_lo(k); i < slice_lo(k + 1); i++) {
+            Op& o = log[i];
+            o.stage = final_stage(o);
+            mx = std::max(mx, o.stage);
+        }
+        slice_max[k] = mx;
     }
-    // sort by OpOrder: bucket by stage (its first key), then order each
-    // stage's ops by the remaining keys, stages in parallel. OpOrder is a
+    int32_t maxst = 0;
+    for (int32_t m : slice_max) maxst = std::max(maxst, m);
+#pragma omp parallel for schedule(static, 1) num_threads(nslice)
+    for (int k = 0; k < nslice; k++) {
+        cnt[k].assign(maxst + 1, 0);
+        for (int64_t i = slice_lo(k); i < slice_lo(k + 1); i++) {
+            const Op& o = log[i];
+            if (!prune || live(o)) cnt[k][o.stage]++;
+        }
+    }
+    std::vector<int64_t> start(maxst + 2, 0);
+    {
+        int64_t run = 0;
+        for (int32_t st = 0; st <= maxst; st++) {
+            start[st] = run;
+            for (int k = 0; k < nslice; k++) {
+                const int64_t c = cnt[k][st];
+                cnt[k][st] = run;  // slice k's first slot in stage st
+                run += c;
+            }
+        }
+        start[maxst + 1] = run;
+    }
+    out.resize(start[maxst + 1]);
+#pragma omp parallel for schedule(static, 1) num_threads(nslice)
+    for (int k = 0; k < nslice; k++)
+        for (int64_t i = slice_lo(k); i < slice_lo(k + 1); i++) {
+            const Op& o = log[i];
+            if (!prune || live(o)) out[cnt[k][o.stage]++] = o;
+        }
+    // order each stage by OpOrder's remaining keys, stages in parallel: small
+    // stages one per thread, large ones each with every thread. OpOrder is a
     // total order (seq is unique), so the result is the single sorted order.
     {
-        int32_t maxst = 0;
-        for (const Op& o : ops) maxst = std::max(maxst, o.stage);
-        std::vector<int64_t> start(maxst + 2, 0);
-        for (const Op& o : ops) start[o.stage + 1]++;
-        for (int32_t st = 0; st <= maxst; st++) start[st + 1] += start[st];
-        std::vector<Op> sorted(ops.size());
-        std::vector<int64_t> pos(start.begin(), start.end() - 1);
-        for (const Op& o : ops) sorted[pos[o.stage]++] = o;
-        // small stages one per thread, large ones each with every thread
         constexpr int64_t BIG = 1 << 18;
-#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : omp_get_max_threads())
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthr)
         for (int32_t st = 0; st <= maxst; st++)
             if (start[st + 1] - start[st] < BIG)
-                std::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder());
+                std::sort(out.begin() + start[st], out.begin() + start[st + 1], OpOrder());
         for (int32_t st = 0; st <= maxst; st++)
             if (start[st + 1] - start[st] >= BIG)
-                __gnu_parallel::sort(sorted.begin() + start[st], sorted.begin() + start[st + 1], OpOrder(),
-                                     __gnu_parallel::default_parallel_tag(threads > 0 ? threads : omp_get_max_threads()));
-        ops.swap(sorted);
+                __gnu_parallel::sort(out.begin() + start[st], out.begin() + start[st + 1], OpOrder(),
+                                     __gnu_parallel::default_parallel_tag(nthr));
     }
     // stages of more than 8000 ops are split (BlockPlanner.cpp:335-354)
     int32_t jump = 0, band = 0, cur = 0;
-    for (Op& o : ops) {
+    for (Op& o : out) {
         if (o.stage > cur) { cur = o.stage; band = 0; }
         if (band > 8000) { jump++; band = 0; }
         o.stage += jump;
@@ -466,7 +523,7 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
     int32_t seq = 0;
 
     // ---- coarse level (PlanL2, BlockPlanner.cpp:1470-1490): blocks in first-touch order
-    Emitter cz(&seq);
+    Emitter cz(&seq, 1024);
     int32_t croot = cz.root_for(R2);
     std::vector<int32_t> cinputs;
     auto ctouch = [&](int bi, int bj) {
@@ -485,16 +542,18 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
     std::vector<Leaf> cL, cU;
     cz.collect(cl, 0, 0, cL);
     if (!symmetric) cz.collect(cu, 0, 0, cU);
+    OpVec cops;
     {
         std::vector<int32_t> outs;
         for (auto& lf : cL) outs.push_back(lf.id);
         for (auto& lf : cU) outs.push_back(lf.id);
-        schedule(cz.ops, cz.storage, cinputs, outs, true, threads);
+        schedule(cz.ops, cz.storage, cinputs, outs, true, threads, cops);
     }
-    p.coarse_ops = (int64_t)cz.ops.size();
+    p.coarse_ops = (int64_t)cops.size();
 
     // ---- fine level: input tiles in (block row, block col) order (BlockPlanner.cpp:1491-1539)
-    Emitter fz(&seq);
+    // a banded 64^3 Laplacian (R = 8192) creates ~260 fine nodes per block row
+    Emitter fz(&seq, (size_t)512 * R + 1024);
     int32_t froot = fz.root_for(R);
     {
         std::vector<int64_t> keys(I.size());
@@ -566,7 +625,7 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
         }
     }
     // expand every coarse op into fine ops (copyOperatorL2, BlockPlanner.cpp:1332-1460)
-    for (const Op& o : cz.ops) {
+    for (const Op& o : cops) {
         if (o.res > 0 && zoom[o.res] == 0) zoom[o.res] = fz.node(levL2);
         if (o.res2 > 0 && zoom[o.res2] == 0) zoom[o.res2] = fz.node(levL2);
         const int32_t g = o.seq;
@@ -607,9 +666,8 @@ Plan build_plan(int n, int64_t nnz, bool symmetric, const int32_t* I0, const int
         std::vector<int32_t> outs;
         for (auto& lf : p.L) outs.push_back(lf.id);
         for (auto& lf : p.U) outs.push_back(lf.id);
-        schedule(fz.ops, fz.storage, finputs, outs, false, threads);
+        schedule(fz.ops, fz.storage, finputs, outs, false, threads, p.ops);
     }
-    p.ops = std::move(fz.ops);
     p.storage_count = fz.storage;
     p.stages = p.ops.empty() ? 0 : p.ops.back().stage;
     p.t_plan = now_s() - t1;

@@ -965,12 +965,11 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     int gemm_parts = o.gemm_split == 1 ? 1 : (o.gemm_split == 4 ? 4 : (s->fp64 ? 4 : 1));
     if (!s->fp64) gemm_parts = 1;
     // inverses of the diagonal factor blocks for the substitution (reused
-    // where the DAG already computes them). Room for everything appended
-    // below (inverses, look-ahead products, transposed leaves), so the op
-    // records are copied once.
-    std::vector<Op> ops2;
-    ops2.reserve(p.ops.size() + 6 * (size_t)p.cfg.block_rows + p.L.size());
-    ops2.assign(p.ops.begin(), p.ops.end());
+    // where the DAG already computes them), look-ahead products and
+    // transposed leaves: appended to a view of the plan's ops, which are not
+    // copied
+    OpSeq ops2(p.ops.data(), (int64_t)p.ops.size());
+    ops2.extra.reserve(6 * (size_t)p.cfg.block_rows + p.L.size());
     int32_t storage2 = p.storage_count;
     // LL^T systems: the upper factor of the substitution is L^T (upperSolverT,
     // BlockPlanner.cpp:752-797), materialised as transposed L leaves (in a
@@ -1130,7 +1129,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     if (ns > 1) {
         std::vector<int32_t> bseg(storage2, 0);
         for (int32_t t = 0; t < p.n_input; t++) bseg[t + 1] = seg_brow[p.input_bi[t]];
-        for (const Op& o : ops2) {
+        for (int64_t i = 0; i < ops2.size(); i++) {
+            const Op& o = ops2[i];
             const int32_t from = o.src > 0 ? bseg[o.src] : (o.src2 > 0 ? bseg[o.src2] : 0);
             if (o.res > 0) bseg[o.res] = from;
             if (o.res2 > 0) bseg[o.res2] = from;
@@ -1567,9 +1567,7 @@ int sog_plan_task_graph_info(const sog_plan* plan, int32_t gemm_split, int64_t* 
     if (!plan || !counts) return fail(SOG_EINVAL, "NULL argument");
     const Plan& p = plan->p;
     try {
-        std::vector<Op> ops2;
-        ops2.reserve(p.ops.size() + 2 * (size_t)p.cfg.block_rows);
-        ops2.assign(p.ops.begin(), p.ops.end());
+        OpSeq ops2(p.ops.data(), (int64_t)p.ops.size());
         int32_t storage2 = p.storage_count;
         std::vector<int32_t> ldinv, udinv, outputs;
         add_diag_inverses(ops2, storage2, p.cfg.block_rows, p.L, p.U, ldinv, udinv);

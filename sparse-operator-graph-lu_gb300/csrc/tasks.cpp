@@ -13,7 +13,7 @@ namespace sog {
 // resolve to the first non-redundant block.
 // Marks in skip the ops replaced by aliasing; readers of the other ops then
 // read alias[src] (a view, not a copy of the op list).
-static void alias_copies(const std::vector<Op>& in, int32_t storage_count, std::vector<int32_t>& alias,
+static void alias_copies(const OpSeq& in, int32_t storage_count, std::vector<int32_t>& alias,
                          std::vector<char>& skip, int64_t& ncopies, int64_t& ndup) {
     alias.resize(storage_count);
     for (int32_t b = 0; b < storage_count; b++) alias[b] = b;
@@ -31,7 +31,7 @@ static void alias_copies(const std::vector<Op>& in, int32_t storage_count, std::
     auto valid = [&](int32_t b) { return b > 0 && b < storage_count; };
     skip.assign(in.size(), 0);
     std::vector<int32_t> first_inv;  // (source root << 1 | upper) -> result, 0 = none yet
-    for (size_t i = 0; i < in.size(); i++) {
+    for (int64_t i = 0; i < in.size(); i++) {
         const Op& o = in[i];
         if (o.op == OP_SUB && o.src == 0 && valid(o.src2) && valid(o.res) && alias[o.res] == o.res) {
             alias[o.res] = o.src2;
@@ -53,14 +53,14 @@ static void alias_copies(const std::vector<Op>& in, int32_t storage_count, std::
     for (int32_t b = 0; b < storage_count; b++) find(b);
 }
 
-TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int32_t n_input,
+TaskGraph build_tasks(const OpSeq& ops_in, int32_t storage_count, int32_t n_input,
                       const std::vector<int32_t>& outputs_in, int gemm_parts, bool fuse_subs, bool fuse_lu) {
     if (gemm_parts != 1 && gemm_parts != 4) throw std::runtime_error("gemm_parts must be 1 or 4");
     std::vector<int32_t> alias;
     int64_t ncopies = 0, ndup = 0;
     std::vector<char> skip;
     alias_copies(ops_in, storage_count, alias, skip, ncopies, ndup);
-    const std::vector<Op>& ops = ops_in;
+    const OpSeq& ops = ops_in;
     // an op that survives aliasing, with its sources read through the aliases
     auto view = [&](int64_t i) {
         Op q = ops[i];
@@ -71,7 +71,7 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     std::vector<int32_t> outputs;
     outputs.reserve(outputs_in.size());
     for (int32_t id : outputs_in) outputs.push_back(id > 0 && id < storage_count ? alias[id] : id);
-    const int64_t nops = (int64_t)ops.size();
+    const int64_t nops = ops.size();
     std::vector<int32_t> producer(storage_count, -1);  // block -> task
     std::vector<int32_t> readers(storage_count, 0);
     auto check_id = [&](int32_t id) {
@@ -358,20 +358,21 @@ TaskGraph build_tasks(const std::vector<Op>& ops_in, int32_t storage_count, int3
     return g;
 }
 
-void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+void add_diag_inverses(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv) {
     // per source block the result of the last lowerInv / upperInv of it (0: none)
     std::vector<int32_t> have_l(storage_count, 0), have_u(storage_count, 0);
-    for (const Op& o : ops) {
+    for (int64_t i = 0; i < ops.size(); i++) {
+        const Op& o = ops[i];
         if (o.src <= 0 || o.src >= storage_count) continue;
         if (o.op == OP_LOWERINV) have_l[o.src] = o.res;
         if (o.op == OP_UPPERINV) have_u[o.src] = o.res;
     }
-    ops.reserve(ops.size() + L.size() + U.size());
+    ops.extra.reserve(ops.extra.size() + L.size() + U.size());
     linv.assign(block_rows, 0);
     uinv.assign(block_rows, 0);
-    int32_t seq = ops.empty() ? 0 : ops.back().seq;
-    int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    int32_t seq = ops.last_seq();
+    int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
     for (int side = 0; side < 2; side++) {
         const std::vector<Leaf>& lv = side == 0 ? L : U;
         auto& have = side == 0 ? have_l : have_u;
@@ -383,20 +384,20 @@ void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_r
                 continue;
             }
             const int32_t id = storage_count++;
-            ops.push_back({side == 0 ? OP_LOWERINV : OP_UPPERINV, lf.id, 0, id, 0, stage, ++seq, 0});
+            ops.extra.push_back({side == 0 ? OP_LOWERINV : OP_UPPERINV, lf.id, 0, id, 0, stage, ++seq, 0});
             dst[lf.bi] = id;
         }
     }
 }
 
-void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const std::vector<Leaf>& L,
+void add_transposed_leaves(OpSeq& ops, int32_t& storage_count, const std::vector<Leaf>& L,
                            std::vector<Leaf>& U) {
     U.clear();
-    int32_t seq = ops.empty() ? 0 : ops.back().seq;
-    const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    int32_t seq = ops.last_seq();
+    const int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
     for (const Leaf& lf : L) {
         const int32_t id = storage_count++;
-        ops.push_back({OP_TRANSPOSE, lf.id, 0, id, 0, stage, ++seq, 0});
+        ops.extra.push_back({OP_TRANSPOSE, lf.id, 0, id, 0, stage, ++seq, 0});
         U.push_back({lf.bj, lf.bi, id});
     }
     std::sort(U.begin(), U.end(), [](const Leaf& a, const Leaf& b) { return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj; });
@@ -421,11 +422,12 @@ static constexpr double HOP_US = 2.4;
 // earliest start of every task with unlimited CTAs (longest weighted path
 // from a source)
 static std::vector<double> estimate_start(const TaskGraph& g, bool fp64) {
-    std::vector<int32_t> by_level(g.ntasks);
-    for (int32_t t = 0; t < g.ntasks; t++) by_level[t] = t;
-    std::stable_sort(by_level.begin(), by_level.end(), [&](int32_t a, int32_t b) { return g.level[a] < g.level[b]; });
     std::vector<double> est(g.ntasks, 0.0);
-    for (int32_t t : by_level) {
+    // level_items lists every task's parts grouped by level: visiting part 0
+    // of each visits the tasks level by level
+    for (int32_t it : g.level_items) {
+        if (it & 15) continue;
+        const int32_t t = it >> 4;
         const double fin = est[t] + task_cost(g, t, fp64) + HOP_US;
         for (int32_t k = g.succ_ptr[t]; k < g.succ_ptr[t + 1]; k++) est[g.succ[k]] = std::max(est[g.succ[k]], fin);
     }
@@ -488,44 +490,44 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
     }
 }
 
-void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula) {
     lla.assign(block_rows, 0);
     ula.assign(block_rows, 0);
-    int32_t seq = ops.empty() ? 0 : ops.back().seq;
-    const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    int32_t seq = ops.last_seq();
+    const int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
     for (const Leaf& lf : L)
         if (lf.bj == lf.bi - 1 && linv[lf.bi] > 0) {
             const int32_t id = storage_count++;
-            ops.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ops.extra.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             lla[lf.bi] = id;
         }
     for (const Leaf& lf : U)
         if (lf.bj == lf.bi + 1 && uinv[lf.bi] > 0) {
             const int32_t id = storage_count++;
-            ops.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ops.extra.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             ula[lf.bi] = id;
         }
 }
 
-void add_lookahead2_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows,
+void add_lookahead2_products(OpSeq& ops, int32_t& storage_count, int block_rows,
                              const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                              const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2) {
     lla2.assign(block_rows, 0);
     ula2.assign(block_rows, 0);
-    int32_t seq = ops.empty() ? 0 : ops.back().seq;
-    const int32_t stage = ops.empty() ? 1 : ops.back().stage + 1;
+    int32_t seq = ops.last_seq();
+    const int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
     for (const Leaf& lf : L)
         if (lf.bj == lf.bi - 2 && linv[lf.bi] > 0) {
             const int32_t id = storage_count++;
-            ops.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ops.extra.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             lla2[lf.bi] = id;
         }
     for (const Leaf& lf : U)
         if (lf.bj == lf.bi + 2 && uinv[lf.bi] > 0) {
             const int32_t id = storage_count++;
-            ops.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
+            ops.extra.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             ula2[lf.bi] = id;
         }
 }

@@ -66,6 +66,22 @@ struct TaskGraph {
     std::vector<int32_t> producer;
 };
 
+// The op list a task graph is built from: a plan's ops (not copied) followed
+// by the ops appended for the substitution and the LL^T path (diagonal
+// inverses, look-ahead products, transposed leaves).
+struct OpSeq {
+    const Op* base = nullptr;
+    int64_t nbase = 0;
+    std::vector<Op> extra;
+    OpSeq() = default;
+    OpSeq(const Op* b, int64_t n) : base(b), nbase(n) {}
+    int64_t size() const { return nbase + (int64_t)extra.size(); }
+    const Op& operator[](int64_t i) const { return i < nbase ? base[i] : extra[i - nbase]; }
+    // sequence number and stage of the last op (0, 0 when empty)
+    int32_t last_seq() const { return size() == 0 ? 0 : (*this)[size() - 1].seq; }
+    int32_t last_stage() const { return size() == 0 ? 0 : (*this)[size() - 1].stage; }
+};
+
 // outputs: block ids that must be materialised (the L/U leaves; a copied
 // output is materialised in its source's tile, see TaskGraph::alias). Throws
 // std::runtime_error on a block written by ops of different kinds, a read of a
@@ -73,18 +89,18 @@ struct TaskGraph {
 // gemm_parts: parts per GEMM task (1 or 4).
 // fuse_lu: merge an LU / LL^T task into the single-part product producing its
 // input block when nothing else reads that block (the mixed path).
-TaskGraph build_tasks(const std::vector<Op>& ops, int32_t storage_count, int32_t n_input,
+TaskGraph build_tasks(const OpSeq& ops, int32_t storage_count, int32_t n_input,
                       const std::vector<int32_t>& outputs, int gemm_parts, bool fuse_subs = true,
                       bool fuse_lu = false);
 
 // Appends, for every diagonal L (U) block without one already in the DAG, a
 // lowerInv (upperInv) op; returns per block row the id of the inverse of the
 // diagonal L and U blocks. storage_count grows by the number of new blocks.
-void add_diag_inverses(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+void add_diag_inverses(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                        const std::vector<Leaf>& U, std::vector<int32_t>& linv, std::vector<int32_t>& uinv);
 // LL^T plans have no U leaves: U = L^T is materialised by one transpose op
 // per L leaf (new blocks), so the back substitution runs as for LU.
-void add_transposed_leaves(std::vector<Op>& ops, int32_t& storage_count, const std::vector<Leaf>& L,
+void add_transposed_leaves(OpSeq& ops, int32_t& storage_count, const std::vector<Leaf>& L,
                            std::vector<Leaf>& U);
 
 // Claim order of the ordered executor: items by estimated start time (longest
@@ -101,14 +117,14 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64);
 // U block at (i, i+1), ula[i] = id of Uinv_ii * U_{i,i+1} (0 = none). The
 // substitution then forms y_i = Linv_ii (b_i - sum_{j<i-1} L_ij y_j) - lla_i
 // y_{i-1}: everything but one 64x64 product is done before row i-1 is ready.
-void add_lookahead_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
+void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula);
 // The same at distance 2: lla2[i] = Linv_ii * L_{i,i-2}, ula2[i] = Uinv_ii *
 // U_{i,i+2} (0 = none), so the block of row i-2 is applied by the whole
 // substitution CTA as soon as that row is published, and row i waits only on
 // its two neighbours' products.
-void add_lookahead2_products(std::vector<Op>& ops, int32_t& storage_count, int block_rows,
+void add_lookahead2_products(OpSeq& ops, int32_t& storage_count, int block_rows,
                              const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                              const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2);
 

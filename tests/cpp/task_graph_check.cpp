@@ -110,7 +110,7 @@ static void check_system(const char* name, int n, const std::vector<int32_t>& I,
         return;
     }
     const Plan& p = plan->p;
-    std::vector<Op> ops = p.ops;
+    OpSeq ops(p.ops.data(), (int64_t)p.ops.size());
     int32_t storage = p.storage_count;
     std::vector<int32_t> linv, uinv, outputs;
     add_diag_inverses(ops, storage, p.cfg.block_rows, p.L, p.U, linv, uinv);
