@@ -139,8 +139,14 @@ MEASURED = _measured_peaks()
 # DRAM bytes (read + write) of one mixed factor launch, NOT measured in the
 # run that prints them: taken from the committed ncu summaries under
 # profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of one launch);
-# None where no capture covers the workload
-TRAFFIC: dict = {"var48": (251.71e6 + 3.45e9, "profiles/launches_var48_bench.md (one-pass ncu, full-size launch)")}
+# None where no capture covers the workload. The 64^3 figure is the 48^3
+# capture scaled by the FP32 tile count (25.06 GB / 5.83 GB of tiles): the
+# factor writes each tile once and reads its operands mostly from L2.
+_T48 = 253.46e6 + 3505.47e6
+TRAFFIC: dict = {
+    "var48": (_T48, "profiles/dram_factor_var48.md (one-pass ncu, full-size launch)"),
+    "lap64": (_T48 * 25.06 / 5.83, "profiles/dram_factor_var48.md, scaled by the tile count (25.06 / 5.83 GB)"),
+}
 
 
 def algorithmic_flops(op_count) -> float:
@@ -456,8 +462,10 @@ def run_ours(args):
         return {"ms": max_over_ranks(ms, world, dev), "lat": lat, "factor_ms": fms, "solve_ms": sms,
                 "iters": iters, "stats": st, "clocks": clocks, "launches": sysm.task_info()["launches"] - l0}
 
+    t_sys = time.perf_counter()
     mixed = sg.System(ctx, plan, precision=sg.MIXED, max_refine=20, tol=1e-10, executor=args.executor,
                       pipeline_stages=args.stages)
+    t_sys = time.perf_counter() - t_sys
     rm = timed(mixed, args.steps, args.warmup)
     grid_mixed = mixed.task_info()["grid"]
     ex = mixed.executor_config()
@@ -561,7 +569,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": rm["clocks"],
             "gpu_launches": int(rm["launches"]),
-            "plan": {"host_plan_s": work.t_plan, "ops": int(info.nops), "stages": int(info.stages),
+            "plan": {"host_plan_s": work.t_plan, "host_system_s": t_sys, "ops": int(info.nops),
+                     "stages": int(info.stages),
                      "tasks": ti["tasks"], "levels": ti["levels"], "algorithmic_gflop": flops / 1e9},
         }
         print(json.dumps(line), flush=True)
