@@ -176,8 +176,9 @@ void gather_seg_launch(const double* b, const DevSegs& g, int n_ext, int c0, int
 // the inverse for real rows and columns; per-system non-finite counts into cnt[k]
 void scatter_seg_launch(const double* xe, const DevSegs& g, int n_ext, int c0, int nc, double* x,
                         unsigned long long* cnt, cudaStream_t s);
-// r = b - A x (n_ext x nc); reductions per (system, column) over the system's
-// real rows and columns: red[(k*nc + c)*6 + {0..5}] as residual_launch
+// r = b - A x (n_ext x nc, 1 <= nc <= 64: the solve's column chunk);
+// reductions per (system, column) over the system's real rows and columns:
+// red[(k*nc + c)*6 + {0..5}] as residual_launch
 void residual_seg_launch(const DevCSR& A, const double* b, const double* x, double* r, int c0, int nc,
                          double* red, const DevSegs& g, cudaStream_t s);
 // dst = active[system of row] ? (float)src : 0 over n_ext x nc

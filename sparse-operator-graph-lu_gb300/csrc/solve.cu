@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -88,6 +89,55 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// ---- thread-block clusters: distributed shared memory hand-over of solved rows
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_rank(uint32_t addr, uint32_t rank) {
+    uint32_t d;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(addr), "r"(rank));
+    return d;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void st_cluster_u32(uint32_t addr, uint32_t v) {
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, int4 v) {
+    asm volatile("st.shared::cluster.v4.s32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w)
+                 : "memory");
+}
+__device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void mbar_init_cta(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// one arrival on the mbarrier at cluster address `addr`, releasing at cluster scope
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+__device__ __forceinline__ bool mbar_test_cluster(const uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
 // One launch per triangle and per chunk of NR right-hand-side columns
 // [c0, c0+NR) of vec (n_ext x ld, row-major). For block row i the warps split
 // its off-diagonal blocks: each warp waits (bounded) only for the row its
@@ -99,8 +149,21 @@ __device__ __forceinline__ T warp_sum(T v) {
 // sum and y_i = Dinv_i (b_i - sum) - M y_j is finished after row j is
 // published: the row's critical path is one 64x64 product. The row is then
 // published with a release store.
-// smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR]
-template <typename T, int NR>
+//
+// CL > 1 (a plain system, no dealing order): the CTAs of a thread-block
+// cluster take CL consecutive rows of one column chunk together (cluster rank
+// r: the r-th row in dealing order). A solved row is also stored straight into
+// the shared memory of every later rank of the cluster, with one mbarrier
+// arrival per receiving rank, so the hand-over between neighbouring rows of a
+// group is a distributed-shared-memory store and an mbarrier wait instead of
+// an L2 round trip behind a GPU-scope fence and a polled flag; rows of earlier
+// groups come through the global flags as before. The ranks finish a group
+// with a cluster barrier (their receive slots are then free), after which
+// rank 0's claim of the next group is read by all. Results are bit-identical
+// to CL = 1: the same products in the same order, only the source of the
+// neighbouring rows' values differs.
+// smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR] | slot[CL][64*NR] (CL > 1)
+template <typename T, int NR, int CL>
 __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
                                                       int cbase, int nch, int epoch, int lower) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -109,7 +172,10 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     T* part = reinterpret_cast<T*>(smem_raw);
     T* ybuf = part + 8 * NV;
     T* acc = ybuf + 8 * NV;
+    T* slot = acc + NV;  // CL > 1: slot[r] holds the row solved by cluster rank r of this group
     __shared__ int s_stop, s_next;
+    __shared__ int s_claim[2], s_cstop;           // CL > 1: rank 0's claims (by group parity), stop flag
+    __shared__ __align__(8) uint64_t s_bar[CL];   // CL > 1: s_bar[r]: rank r's row delivered here
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int R = s.block_rows;
     const int* ptr = lower ? s.l_ptr : s.u_ptr;
@@ -120,7 +186,24 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     const int* lookahead2 = lower ? s.l_la2 : s.u_la2;
     const int dir = lower ? -1 : 1;  // the rows a row waits on lie on this side
     const int* order = lower ? s.order_l : s.order_u;
-    if (tid == 0) { s_stop = 0; s_next = atomicAdd(s.claim + (lower ? 0 : 1), 1); }
+    int* claim = s.claim + (lower ? 0 : 1);
+    const int rank = CL > 1 ? (int)cluster_rank() : 0;
+    const int ngroups = (R + CL - 1) / CL * nch;
+    if (tid == 0) {
+        s_stop = 0;
+        if constexpr (CL > 1) {
+            s_cstop = 0;
+            if (rank == 0) s_claim[0] = atomicAdd(claim, 1);
+        } else {
+            s_next = atomicAdd(claim, 1);
+        }
+    }
+    if constexpr (CL > 1) {
+        if (tid < CL) mbar_init_cta(&s_bar[tid], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        cluster_sync_all();
+        if (tid == 0) s_next = ld_cluster_s32(map_rank(smem_addr(&s_claim[0]), 0));
+    }
     __syncthreads();
     T* yw = ybuf + warp * NV;
     // bounded wait of lane 0 for row j's flag; the warp's later reads of row j
@@ -141,15 +224,49 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         __syncwarp();
         return !*(volatile int*)&s_stop;
     };
+    uint32_t gpar = 0;  // CL > 1: phase parity of s_bar for this group
+    // bounded wait (every lane) for the row of cluster rank `snd` of this group
+    auto wait_rank = [&](int snd) -> bool {
+        if (!mbar_test_cluster(&s_bar[snd], gpar)) {
+            const unsigned long long t0 = globaltimer_ns();
+            while (!mbar_test_cluster(&s_bar[snd], gpar)) {
+                if (globaltimer_ns() - t0 > s.wait_limit_ns) {
+                    if (lane == 0) atomicOr(&s.status->flags, ST_SOLVE_TIMEOUT);
+                    s_stop = 1;
+                    break;
+                }
+            }
+        }
+        __syncwarp();
+        return !*(volatile int*)&s_stop;
+    };
     // positions: nch column chunks of each row in turn, rows in dealing order
-    // positions claimed in dealing order (the next one while this one runs):
-    // a row only waits on rows dealt earlier, which resident CTAs hold
-    for (int k = s_next; k < R * nch; k = s_next) {
+    // (CL > 1: groups of CL rows), claimed in dealing order (the next one
+    // while this one runs): a row only waits on rows dealt earlier, which
+    // resident CTAs hold
+    for (int k = s_next; k < ngroups; k = s_next) {
         __syncthreads();  // every thread has read s_next
-        if (tid == 0) s_next = atomicAdd(s.claim + (lower ? 0 : 1), 1);
-        const int kk = k / nch, ch = k - kk * nch, c0 = cbase + ch * NR;
-        const int i = order ? order[kk] : (lower ? kk : R - 1 - kk);
+        if (tid == 0) {
+            if constexpr (CL > 1) {
+                if (rank == 0) s_claim[gpar ^ 1u] = atomicAdd(claim, 1);
+            } else {
+                s_next = atomicAdd(claim, 1);
+            }
+        }
+        const int kg = k / nch, ch = k - kg * nch, c0 = cbase + ch * NR;
+        const int kk = kg * CL + rank, kk0 = kg * CL;
+        const bool have = kk < R;  // CL > 1: the last group may be short
+        const int i = !have ? 0 : (order ? order[kk] : (lower ? kk : R - 1 - kk));
+        // CL > 1: rows of this group lie on the waiting side of row i, up to
+        // the group's first row: sender rank of row j, -1 = an earlier group
+        auto rank_of = [&](int j) -> int {
+            if constexpr (CL == 1) return -1;
+            const int d = lower ? j - kk0 : (R - 1 - kk0) - j;
+            return d >= 0 && d < rank ? d : -1;
+        };
         fl = s.flags + (size_t)ch * R;
+        bool stop = false;
+        if (have) {
         if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
         const T* Dm = tiles + (size_t)dinv[i] * 4096;
         const int la = lookahead ? lookahead[i] : 0, la2 = lookahead2 ? lookahead2[i] : 0;
@@ -158,7 +275,6 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         T pa[NR], pb[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
-        bool stop = false;
         // with look-ahead products the last blocks (the neighbouring rows i-1,
         // i-2; the lists run in readiness order) are left out
         const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0) - (la2 > 0 ? 1 : 0);
@@ -168,13 +284,23 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
 #pragma unroll
             for (int o = 0; o < 128; o += 128 / (int)sizeof(T)) asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
-            if (!wait_row(j)) {
-                stop = true;
-                break;
+            const int snd = rank_of(j);
+            const T* ys = yw;
+            if (snd >= 0) {
+                if (!wait_rank(snd)) {
+                    stop = true;
+                    break;
+                }
+                ys = slot + snd * NV;
+            } else {
+                if (!wait_row(j)) {
+                    stop = true;
+                    break;
+                }
+                const T* vj = vec + (size_t)j * 64 * ld + c0;
+                for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
+                __syncwarp();
             }
-            const T* vj = vec + (size_t)j * 64 * ld + c0;
-            for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
-            __syncwarp();
 #pragma unroll 4
             for (int c = 0; c < 64; c += VW) {
                 const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
@@ -182,7 +308,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 for (int v = 0; v < VW; v++)
 #pragma unroll
                     for (int r = 0; r < NR; r++) {
-                        const T y = yw[(c + v) * NR + r];
+                        const T y = ys[(c + v) * NR + r];
                         pa[r] += b0.v[v] * y;
                         pb[r] += b1.v[v] * y;
                     }
@@ -196,17 +322,19 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             pw[(2 * lane + 1) * NR + r] = pb[r];
         }
         __syncthreads();
-        if (s_stop || stop) return;
+        stop = stop || s_stop;
+        if (!stop) {
         for (int e = tid; e < NV; e += NT) {
             T v = __ldcg(vec + ((size_t)i * 64 + e / NR) * ld + c0 + (e % NR));
 #pragma unroll
             for (int w = 0; w < 8; w++) v -= part[w * NV + e];
             acc[e] = v;
         }
+        }
         __syncthreads();
         // y_i = inv(D_ii) * acc [- M * y_j]: warp w rows 8w..8w+7, four lanes
         // per row, each lane 16 columns; partial sums reduced over the four lanes
-        {
+        if (!stop) {
             const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
             const bool vec16 = ((size_t)ld * sizeof(T)) % 16 == 0 && ((size_t)c0 * sizeof(T)) % 16 == 0;
             Vec16<T> m[16 / VW];
@@ -229,34 +357,45 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
             }
             // y -= M y_j over this lane's 16 columns (all warps: a 64x64 product
-            // split over the CTA instead of one warp's block product)
-            auto apply = [&](const Vec16<T>* mm, int j) {
+            // split over the CTA instead of one warp's block product); row j
+            // from global memory or, within a cluster group, from its slot
+            auto apply = [&](const Vec16<T>* mm, int j, int snd) {
                 const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
+                const T* sj = slot + (snd >= 0 ? snd : 0) * NV + cb * NR;
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++)
 #pragma unroll
                     for (int v = 0; v < VW; v++) {
                         T yj[NR];
-                        load_row<T, NR>(vj + (size_t)(c * VW + v) * ld, vec16, yj);
+                        if (CL > 1 && snd >= 0) {
+#pragma unroll
+                            for (int r = 0; r < NR; r++) yj[r] = sj[(c * VW + v) * NR + r];
+                        } else {
+                            load_row<T, NR>(vj + (size_t)(c * VW + v) * ld, vec16, yj);
+                        }
 #pragma unroll
                         for (int r = 0; r < NR; r++) y[r] -= mm[c].v[v] * yj[r];
                     }
             };
+            auto wait_any = [&](int j, int snd) { return snd >= 0 ? wait_rank(snd) : wait_row(j); };
             // row i-2 first (M2 = Dinv_i B_{i,i-2}), then row i-1 (M1); a wait
-            // that runs out sets s_stop: the CTA leaves together after the
-            // barrier below, publishing nothing
+            // that runs out sets s_stop: the CTA publishes nothing
             bool ok = true;
             if (la2 > 0) {
-                ok = wait_row(i + 2 * dir);
+                const int j2 = i + 2 * dir, snd2 = rank_of(j2);
+                ok = wait_any(j2, snd2);
                 if (ok) {
                     Vec16<T> m2[16 / VW];
                     const T* M = tiles + (size_t)la2 * 4096 + row * 64 + cb;
 #pragma unroll
                     for (int c = 0; c < 16 / VW; c++) m2[c] = ldg16(M + c * VW);
-                    apply(m2, i + 2 * dir);
+                    apply(m2, j2, snd2);
                 }
             }
-            if (ok && la > 0 && wait_row(i + dir)) apply(m, i + dir);
+            if (ok && la > 0) {
+                const int j1 = i + dir, snd1 = rank_of(j1);
+                if (wait_any(j1, snd1)) apply(m, j1, snd1);
+            }
 #pragma unroll
             for (int r = 0; r < NR; r++) {
                 y[r] += __shfl_xor_sync(0xffffffffu, y[r], 1);
@@ -265,34 +404,159 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             if ((lane & 3) == 0) {
 #pragma unroll
                 for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
+                if constexpr (CL > 1) {
+                    // the row into slot[rank] of every later rank of the group
+                    const uint32_t src = smem_addr(slot + rank * NV + row * NR);
+                    for (int dst = rank + 1; dst < CL; dst++) {
+                        const uint32_t a = map_rank(src, (uint32_t)dst);
+                        if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
+#pragma unroll
+                            for (int q = 0; q < NR * (int)sizeof(T) / 16; q++) {
+                                int4 v;
+                                memcpy(&v, reinterpret_cast<const char*>(y) + 16 * q, 16);
+                                st_cluster_v4(a + 16 * q, v);
+                            }
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < NR * (int)sizeof(T) / 4; q++) {
+                                uint32_t v;
+                                memcpy(&v, reinterpret_cast<const char*>(y) + 4 * q, 4);
+                                st_cluster_u32(a + 4 * q, v);
+                            }
+                        }
+                    }
+                }
             }
         }
+        }  // have
         __syncthreads();
-        if (s_stop) return;
+        stop = stop || s_stop;
         if (tid == 0) {
-            fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
-            st_release(s.flags + (size_t)ch * R + i, epoch);
-            if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
+            if constexpr (CL > 1) {
+                // every later rank's barrier completes one phase per group
+                // (also when this rank has no row or stopped), so that the
+                // parities stay in step
+                asm volatile("fence.acq_rel.cluster;" ::: "memory");
+                for (int dst = rank + 1; dst < CL; dst++)
+                    mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
+                if (stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
+            }
+            if (have && !stop) {
+                fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
+                st_release(s.flags + (size_t)ch * R + i, epoch);
+                if (s.trace) s.trace[4 * (size_t)i + (lower ? 1 : 3)] = globaltimer_ns();
+            }
         }
-        __syncthreads();  // thread 0's next claim is visible
+        if constexpr (CL > 1) {
+            // the group is done in every rank (its slots are free); rank 0's
+            // claim of the next group and any rank's stop are visible
+            cluster_sync_all();
+            gpar ^= 1u;
+            if (tid == 0) {
+                const int st0 = ld_cluster_s32(map_rank(smem_addr(&s_cstop), 0));
+                s_next = st0 ? ngroups : ld_cluster_s32(map_rank(smem_addr(&s_claim[gpar]), 0));
+            }
+            __syncthreads();
+        } else {
+            if (stop) return;
+            __syncthreads();  // thread 0's next claim is visible
+        }
     }
+    if constexpr (CL > 1) cluster_sync_all();  // no rank leaves while another may still store into it
 }
 
-template <typename T, int NR>
+template <typename T, int NR, int CL>
 size_t trisolve_smem() {
-    return (size_t)(17 * 64 * NR) * sizeof(T);
+    return (size_t)((17 + (CL > 1 ? CL : 0)) * 64 * NR) * sizeof(T);
 }
 
+// rows per cluster group of the substitution of a plain system
+constexpr int SOLVE_CLUSTER = 8;
+
+template <typename T, int NR, int CL>
+int trisolve_pair(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int nch, int epoch, int grid,
+                  cudaStream_t st) {
+    const size_t smem = trisolve_smem<T, NR, CL>();
+    auto kern = trisolve_kernel<T, NR, CL>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaMemsetAsync(s.claim, 0, 8, st);
+    if constexpr (CL == 1) {
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch, 1);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch + 1, 0);
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = CL;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, kern, s, tiles, vec, ld, c0, nch, epoch, 1) != cudaSuccess) return -1;
+        if (cudaLaunchKernelEx(&cfg, kern, s, tiles, vec, ld, c0, nch, epoch + 1, 0) != cudaSuccess) return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// resident clusters of CL CTAs of the kernel (0: cannot be launched so)
+template <typename T, int NR, int CL>
+int resident_clusters() {
+    const size_t smem = trisolve_smem<T, NR, CL>();
+    auto kern = trisolve_kernel<T, NR, CL>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CL;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// One launch pair (lower, upper) for nch column chunks of NR columns. A plain
+// system (no dealing order) runs in clusters when at least one cluster fits
+// the grid bound: at most grid CTAs, a multiple of the cluster size.
 template <typename T, int NR>
 int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int nch, int& epoch, int grid,
                    cudaStream_t st) {
-    const size_t smem = trisolve_smem<T, NR>();
-    cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaMemsetAsync(s.claim, 0, 8, st);
-    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch, 1);
-    trisolve_kernel<T, NR><<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch + 1, 0);
+    int rc = 1;
+    if constexpr (NR == 8 || NR == 1) {
+        constexpr int CL = SOLVE_CLUSTER;
+        // the kernel's resident clusters, queried once (every GPU this
+        // library drives is the same model)
+        static std::atomic<int> cached{-1};
+        int clusters = cached.load(std::memory_order_relaxed);
+        if (clusters < 0) {
+            clusters = resident_clusters<T, NR, CL>();
+            cached.store(clusters, std::memory_order_relaxed);
+        }
+        const bool plain = s.order_l == nullptr && s.order_u == nullptr;
+        if (plain && clusters > 0 && grid >= CL) {
+            const int groups = (s.block_rows + CL - 1) / CL * nch;
+            const int ncl = std::max(1, std::min({clusters, groups, grid / CL}));
+            rc = trisolve_pair<T, NR, CL>(s, tiles, vec, ld, c0, nch, epoch, ncl * CL, st);
+        }
+    }
+    if (rc == 1) rc = trisolve_pair<T, NR, 1>(s, tiles, vec, ld, c0, nch, epoch, grid, st);
     epoch += 2;
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return rc;
 }
 
 template <typename T>
@@ -316,9 +580,9 @@ int trisolve_impl(const DevSolve& s, const T* tiles, T* vec, int nrhs, int& epoc
 template <typename T, int NR>
 int occupancy_grid(int num_sms) {
     int per_sm = 0;
-    const size_t smem = trisolve_smem<T, NR>();
-    cudaFuncSetAttribute(trisolve_kernel<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trisolve_kernel<T, NR>, NT, smem);
+    const size_t smem = trisolve_smem<T, NR, 1>();
+    cudaFuncSetAttribute(trisolve_kernel<T, NR, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trisolve_kernel<T, NR, 1>, NT, smem);
     return (per_sm < 1 ? 1 : per_sm) * num_sms;
 }
 
@@ -401,48 +665,92 @@ __global__ void scatter_seg_kernel(const double* __restrict__ xe, DevSegs g, int
     x[g.voff[k] + (int64_t)col * g.n[k] + o] = v;
     if (!isfinite(v)) atomicAdd(cnt + k, 1ull);
 }
-// as residual_kernel, reductions per (system, column): a warp's 32 rows lie
-// in one 64-row block row, so each warp reduces into one system's slots
-__global__ void residual_seg_kernel(DevCSR A, const double* __restrict__ b, const double* __restrict__ x,
-                                    double* __restrict__ r, int c0, int nc, double* red, DevSegs g) {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row - (threadIdx.x & 31) >= A.n) return;  // whole warp past the end (A.n is a multiple of 64)
-    const int lane = threadIdx.x & 31;
-    const int k = g.of_brow[row >> 6];
-    const bool real = g.n2o[row] >= 0;
-    double rowabs = 0;
-    if (real)
-        for (int q = A.ptr[row]; q < A.ptr[row + 1]; q++) rowabs += fabs(A.val[q]);
-    for (int o = 16; o > 0; o >>= 1) rowabs = fmax(rowabs, __shfl_xor_sync(0xffffffffu, rowabs, o));
-    const int creal = min(nc, g.nrhs[k] - c0);  // columns of this chunk that system k has
-    for (int c = 0; c < nc; c++) {
-        double acc = 0;
-        for (int q = A.ptr[row]; q < A.ptr[row + 1]; q++) acc += A.val[q] * x[(size_t)A.col[q] * nc + c];
-        const double bv = b[(size_t)row * nc + c];
-        const double rv = bv - acc;
-        r[(size_t)row * nc + c] = rv;
-        if (c >= creal) continue;  // warp-uniform
-        double rr = 0, bb = 0, ar = 0, ax = 0, ab = 0;
-        if (real) {
-            rr = rv * rv; bb = bv * bv; ar = fabs(rv); ax = fabs(x[(size_t)row * nc + c]); ab = fabs(bv);
+// as residual_kernel, reductions per (system, column). Each CTA walks a
+// contiguous range of 64-row block rows (a block row belongs to one system).
+// Its first nc * (256 / nc) threads each keep one column c = t % nc and rows
+// t / nc, t / nc + 256 / nc, ... of every block row, so the lanes of a warp
+// read consecutive columns of x and b (coalesced for nc >= 32; several rows
+// per warp for fewer columns), and each thread accumulates its column's sums
+// and maxima in registers. Partial results leave once per system the range
+// touches: shared-memory atomics per column, then one global atomic per
+// (column, slot) and CTA, instead of one per (warp, column, slot). r is
+// formed exactly as in residual_kernel (same products in the same order).
+constexpr int RES_THREADS = 256;
+constexpr int RES_CTAS = 4 * 152;  // four per SM of a GB300
+__global__ void __launch_bounds__(RES_THREADS) residual_seg_kernel(DevCSR A, const double* __restrict__ b,
+                                                                 const double* __restrict__ x, double* __restrict__ r,
+                                                                 int c0, int nc, double* red, DevSegs g, int nbr) {
+    __shared__ double s_acc[64 * 5];
+    __shared__ double s_rowabs;
+    const int t = threadIdx.x;
+    const int rpp = RES_THREADS / nc;  // rows per pass over a block row
+    const bool act = t < rpp * nc;
+    const int c = act ? t % nc : 0, roff = act ? t / nc : 0;
+    const int br0 = (int)((int64_t)blockIdx.x * nbr / gridDim.x);
+    const int br1 = (int)((int64_t)(blockIdx.x + 1) * nbr / gridDim.x);
+    for (int i = t; i < 64 * 5; i += RES_THREADS) s_acc[i] = 0.0;
+    if (t == 0) s_rowabs = 0.0;
+    __syncthreads();
+    double rr = 0, bb = 0, ar = 0, ax = 0, ab = 0, rowabs = 0;
+    auto smax = [](double* p, double v) {
+        atomicMax(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double_as_longlong(v));
+    };
+    // this CTA's partial results for system k -> red; uniform across the CTA
+    auto flush = [&](int k) {
+        const int creal = min(nc, g.nrhs[k] - c0);
+        if (act && c < creal) {
+            atomicAdd(&s_acc[c * 5 + 0], rr);
+            atomicAdd(&s_acc[c * 5 + 1], bb);
+            smax(&s_acc[c * 5 + 2], ar);
+            smax(&s_acc[c * 5 + 3], ax);
+            smax(&s_acc[c * 5 + 4], ab);
+            smax(&s_rowabs, rowabs);
         }
-        rr = warp_sum(rr);
-        bb = warp_sum(bb);
-        for (int o = 16; o > 0; o >>= 1) {
-            ar = fmax(ar, __shfl_xor_sync(0xffffffffu, ar, o));
-            ax = fmax(ax, __shfl_xor_sync(0xffffffffu, ax, o));
-            ab = fmax(ab, __shfl_xor_sync(0xffffffffu, ab, o));
+        rr = bb = ar = ax = ab = rowabs = 0;
+        __syncthreads();
+        for (int i = t; i < max(creal, 0) * RED; i += RES_THREADS) {
+            const int cc = i / RED, slot = i % RED;
+            double* rd = red + ((size_t)k * nc + cc) * RED + slot;
+            if (slot < 2) atomicAdd(rd, s_acc[cc * 5 + slot]);
+            else atomic_max_nonneg(rd, slot < 5 ? s_acc[cc * 5 + slot] : s_rowabs);
         }
-        if (lane == 0) {
-            double* rd = red + ((size_t)k * nc + c) * RED;
-            atomicAdd(rd + 0, rr);
-            atomicAdd(rd + 1, bb);
-            atomic_max_nonneg(rd + 2, ar);
-            atomic_max_nonneg(rd + 3, ax);
-            atomic_max_nonneg(rd + 4, ab);
-            atomic_max_nonneg(rd + 5, rowabs);
+        __syncthreads();
+        for (int i = t; i < 64 * 5; i += RES_THREADS) s_acc[i] = 0.0;
+        if (t == 0) s_rowabs = 0.0;
+        __syncthreads();
+    };
+    int k = br0 < br1 ? g.of_brow[br0] : 0;
+    for (int br = br0; br < br1; br++) {
+        const int kb = g.of_brow[br];
+        if (kb != k) {
+            flush(k);
+            k = kb;
+        }
+        const int creal = min(nc, g.nrhs[k] - c0);
+        if (!act) continue;
+        for (int rw = roff; rw < 64; rw += rpp) {
+            const int row = br * 64 + rw;
+            const int q0 = A.ptr[row], q1 = A.ptr[row + 1];
+            double acc = 0, ra = 0;
+            for (int q = q0; q < q1; q++) {
+                const double a = A.val[q];
+                acc += a * x[(size_t)A.col[q] * nc + c];
+                ra += fabs(a);
+            }
+            const double bv = b[(size_t)row * nc + c];
+            const double rv = bv - acc;
+            r[(size_t)row * nc + c] = rv;
+            if (c < creal && g.n2o[row] >= 0) {
+                rr += rv * rv;
+                bb += bv * bv;
+                ar = fmax(ar, fabs(rv));
+                ax = fmax(ax, fabs(x[(size_t)row * nc + c]));
+                ab = fmax(ab, fabs(bv));
+                rowabs = fmax(rowabs, ra);
+            }
         }
     }
+    if (br0 < br1) flush(k);
 }
 // max |a_ij| per system: one thread per permuted row, a warp's 32 rows lie in
 // one 64-row block row (one system); padding rows skipped
@@ -535,7 +843,9 @@ void scatter_seg_launch(const double* xe, const DevSegs& g, int n_ext, int c0, i
 void residual_seg_launch(const DevCSR& A, const double* b, const double* x, double* r, int c0, int nc,
                          double* red, const DevSegs& g, cudaStream_t s) {
     cudaMemsetAsync(red, 0, sizeof(double) * RED * nc * g.nseg, s);
-    residual_seg_kernel<<<(A.n + 255) / 256, 256, 0, s>>>(A, b, x, r, c0, nc, red, g);
+    const int nbr = A.n / 64;  // A.n is a multiple of 64
+    if (nbr > 0 && nc > 0 && nc <= 64)
+        residual_seg_kernel<<<std::min(nbr, RES_CTAS), RES_THREADS, 0, s>>>(A, b, x, r, c0, nc, red, g, nbr);
 }
 void cast_seg_launch(const double* src, float* dst, int n_ext, int nc, const DevSegs& g, cudaStream_t s) {
     if ((int64_t)n_ext * nc > 0) cast_seg_kernel<<<608, 256, 0, s>>>(src, dst, n_ext, nc, g);
