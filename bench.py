@@ -332,9 +332,14 @@ def run_serving(args):
                           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                           "mean_plan_ms": float(np.mean([i["plan_ms"] for i in infos])),
                           "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])),
+                          "mean_setup_ms": float(np.mean([i["setup_ms"] for i in infos])),
                           "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i in infos])),
                           "batches": c["batches"], "largest_batch": c["max_batch"],
-                          "worst_rel_resid": worst, "not_ok": stat_bad})
+                          "worst_rel_resid": worst, "not_ok": stat_bad,
+                          "slowest": (lambda k: {"n": int(systems[k].n), "total_ms": lat[k],
+                                                 "plan_ms": infos[k]["plan_ms"], "queue_ms": infos[k]["queue_ms"],
+                                                 "setup_ms": infos[k]["setup_ms"],
+                                                 "gpu_ms": infos[k]["gpu_ms"]})(int(np.argmax(lat)))})
     ctx.close()
     top = [r for r in sweep if r["precision"] == "mixed"][-1]
     line = {"metric": METRIC, "value": top["throughput_per_s"], "unit": "requests/s", "n_gpus": 1,

@@ -294,6 +294,11 @@ int sog_system_set_wait_limit(sog_system *sys, double ms);
  * (host-side fault injection); sog_debug_unpoison restores the graph. */
 int sog_debug_poison_task(sog_system *sys, int32_t task);
 int sog_debug_unpoison(sog_system *sys);
+/* Testing hook (FP64 systems): on = 0 runs every DMMA of the FP64 products,
+ * on = 1 skips those whose operand fragment is all zero (the default; the
+ * autotuner may pick either). Either way the factors are the same: a skipped
+ * MMA would only add exact zeros. Overrides a pending autotuning choice. */
+int sog_debug_fp64_fragment_skip(sog_system *sys, int32_t on);
 
 /* ---- allocation-free residual check (no counterpart in the reference) ------
  * r = b - A x in FP64 for a CSR matrix on the device, and per right-hand side
@@ -358,6 +363,7 @@ typedef struct {
     int64_t batch_id;
     double plan_ms;       /* host planning */
     double queue_ms;      /* planned -> admitted */
+    double setup_ms;      /* admitted -> the batch's factor starts: plan merge, task graph, device upload */
     double gpu_ms;        /* the batch's factor + solve, host clock */
     double total_ms;      /* submit -> answer */
     sog_solve_stats stats;

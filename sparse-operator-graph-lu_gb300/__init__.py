@@ -70,7 +70,8 @@ class ServerOptions(C.Structure):
 
 class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int32), ("batch_size", C.c_int32), ("batch_id", C.c_int64), ("plan_ms", C.c_double),
-                ("queue_ms", C.c_double), ("gpu_ms", C.c_double), ("total_ms", C.c_double), ("stats", SolveStats)]
+                ("queue_ms", C.c_double), ("setup_ms", C.c_double), ("gpu_ms", C.c_double), ("total_ms", C.c_double),
+                ("stats", SolveStats)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stats"}
@@ -86,7 +87,7 @@ EXPORTS = [
     "sog_system_create", "sog_system_bytes", "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve",
     "sog_solve_device", "sog_solve_permuted", "sog_system_export_factors", "sog_system_last_times",
     "sog_system_destroy", "sog_system_task_info", "sog_system_executor", "sog_system_set_wait_limit", "sog_debug_poison_task",
-    "sog_debug_unpoison", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
+    "sog_debug_unpoison", "sog_debug_fp64_fragment_skip", "soglu_solveLU", "sog_system_trace_enable", "sog_system_trace_get",
     "sog_system_task_graph", "sog_plan_task_graph_info", "sog_residual_noalloc", "sog_plan_merge",
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
     "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
@@ -122,6 +123,7 @@ def lib() -> C.CDLL:
         "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32),
         "sog_system_pivots": ([P, P], I32), "sog_system_set_stream": ([P, P], I32), "sog_system_set_wait_limit": ([P, D], I32),
         "sog_debug_poison_task": ([P, I32], I32), "sog_debug_unpoison": ([P], I32),
+        "sog_debug_fp64_fragment_skip": ([P, I32], I32),
         "soglu_solveLU": ([I32, I64, I32, P, P, P, P, P, I32], I32),
         "sog_system_trace_enable": ([P, I32], I32), "sog_system_trace_get": ([P, P, P, P], I32),
         "sog_system_task_graph": ([P, P, P, P], I32), "sog_plan_task_graph_info": ([P, I32, P], I32),

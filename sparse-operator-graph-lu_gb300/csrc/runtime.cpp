@@ -4,8 +4,12 @@
 // behind the C ABI of include/soglu_gb300.h.
 #include <cuda_runtime.h>
 
+#include <parallel/algorithm>
+
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -302,37 +306,37 @@ struct HostCSR {
 HostCSR build_csr(const Plan& p) {
     HostCSR h;
     const int n_ext = p.cfg.n_ext();
-    const size_t nt = p.scatter_tile.size();
-    std::vector<int64_t> key;
-    std::vector<int32_t> trip;
-    key.reserve(nt + p.pad_tile.size());
-    for (size_t k = 0; k < nt; k++) {
-        int32_t t = p.scatter_tile[k];
-        if (t < 0) continue;
-        int64_t row = (int64_t)p.input_bi[t] * 64 + p.scatter_off[k] / 64;
-        int64_t col = (int64_t)p.input_bj[t] * 64 + p.scatter_off[k] % 64;
-        key.push_back(row * n_ext + col);
-        trip.push_back((int32_t)k);
+    const int64_t nt = (int64_t)p.scatter_tile.size(), np_ = (int64_t)p.pad_tile.size();
+    // (row * n_ext + col, triplet or -1 for a padded row's unit diagonal),
+    // sorted by position: every position occurs once (superseded duplicates
+    // have no tile), so the order is unique
+    std::vector<std::pair<int64_t, int32_t>> e(nt + np_);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nt; k++) {
+        const int32_t t = p.scatter_tile[k];
+        if (t < 0) {
+            e[k] = {INT64_MAX, -2};  // sorts last, dropped below
+            continue;
+        }
+        const int64_t row = (int64_t)p.input_bi[t] * 64 + p.scatter_off[k] / 64;
+        const int64_t col = (int64_t)p.input_bj[t] * 64 + p.scatter_off[k] % 64;
+        e[k] = {row * n_ext + col, (int32_t)k};
     }
-    // padded rows: unit diagonal (one entry per padded row in the pad list)
-    for (size_t q = 0; q < p.pad_tile.size(); q++) {
+    for (int64_t q = 0; q < np_; q++) {
         const int64_t i = (int64_t)p.input_bi[p.pad_tile[q]] * 64 + p.pad_off[q] / 64;
-        key.push_back(i * n_ext + i);
-        trip.push_back(-1);
+        e[nt + q] = {i * n_ext + i, -1};
     }
-    std::vector<int64_t> order(key.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = (int64_t)i;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+    __gnu_parallel::sort(e.begin(), e.end());
+    while (!e.empty() && e.back().second == -2) e.pop_back();
     h.ptr.assign(n_ext + 1, 0);
-    h.col.resize(key.size());
-    h.val.assign(key.size(), 0.0);
+    h.col.resize(e.size());
+    h.val.assign(e.size(), 0.0);
     h.pos.assign(nt, -1);
-    for (size_t q = 0; q < order.size(); q++) {
-        int64_t kk = key[order[q]];
-        int row = (int)(kk / n_ext);
+    for (size_t q = 0; q < e.size(); q++) {
+        const int64_t kk = e[q].first;
         h.col[q] = (int32_t)(kk % n_ext);
-        h.ptr[row + 1]++;
-        if (trip[order[q]] >= 0) h.pos[trip[order[q]]] = (int32_t)q;
+        h.ptr[kk / n_ext + 1]++;
+        if (e[q].second >= 0) h.pos[e[q].second] = (int32_t)q;
         else h.val[q] = 1.0;
     }
     for (int i = 0; i < n_ext; i++) h.ptr[i + 1] += h.ptr[i];
@@ -407,7 +411,6 @@ int factor_grid(const sog_system* s, int stages) {
 }
 
 int run_factor_once(sog_system* s) {
-    sog_ctx* c = s->ctx;
     cudaStream_t st = s->stream;
     const TaskGraph& g = s->tg;
     DevStatus fs = fresh_status();
@@ -500,7 +503,6 @@ int run_factor(sog_system* s) {
 // exceeded the limit makes the call return SOG_EPIVOT. The factors stay
 // resident and can be used.
 int check_pivots(sog_system* s) {
-    sog_ctx* c = s->ctx;
     const size_t ns = s->segs.size();
     std::vector<DevPivot> hp(ns);
     std::vector<unsigned long long> ha(ns);
@@ -646,7 +648,6 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
 // into the systems' statistics; rel[k] = worst relative residual of system k
 // over the chunk's columns it has (0 if none).
 int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
-    sog_ctx* c = s->ctx;
     const size_t ns = s->segs.size();
     CK(cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED * nc * ns, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -673,7 +674,6 @@ int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
 // have not converged yet: the others' corrections are masked to zero, which
 // leaves their iterates bit for bit unchanged.
 int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chunk_stats) {
-    sog_ctx* c = s->ctx;
     cudaStream_t st = s->stream;
     const int64_t ne = (int64_t)s->n_ext * nc;
     const size_t ns = s->segs.size();
@@ -741,7 +741,6 @@ int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chu
 // s->seg_stats; agg (if not NULL) gets the worst over systems.
 int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, double* x_dev,
                       sog_solve_stats* agg) {
-    sog_ctx* c = s->ctx;
     cudaStream_t st = s->stream;
     const size_t ns = s->segs.size();
     int maxr = 0;
@@ -1514,6 +1513,18 @@ int sog_debug_unpoison(sog_system* s) {
     CK(cudaMemcpy(s->d_ndep0, s->tg.ndep.data(), sizeof(int32_t) * s->tg.ntasks, cudaMemcpyHostToDevice));
     s->poisoned = false;
     s->dt.early = !s->fp64 && s->early;
+    return SOG_OK;
+}
+
+int sog_debug_fp64_fragment_skip(sog_system* s, int32_t on) {
+    if (!s) return fail(SOG_EINVAL, "NULL system");
+    if (!s->fp64) return fail(SOG_EINVAL, "not an FP64 system");
+    if (s->tune_pending) {  // keep the tuner's executor choice out of it
+        s->tune_pending = false;
+        s->opt.executor = SOG_EXEC_PERSISTENT;
+        s->grid_factor = factor_grid(s, s->stages);
+    }
+    s->dt.skip_zero = on ? 1 : 0;
     return SOG_OK;
 }
 

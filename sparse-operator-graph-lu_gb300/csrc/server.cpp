@@ -61,7 +61,7 @@ struct Request {
     bool released = false;
     int jobs = 0;  // further solves queued or running
     Clock::time_point t_submit, t_planned, t_start, t_done;
-    double plan_ms = 0, gpu_ms = 0;
+    double plan_ms = 0, setup_ms = 0, gpu_ms = 0;
 };
 
 struct Batch {
@@ -240,6 +240,7 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
     std::vector<sog_solve_stats> st(group.size());
     std::string err;
     const Clock::time_point t0 = Clock::now();
+    for (Request* r : group) r->setup_ms = ms_since(r->t_start, t0);
     if (!rc) rc = sog_factor(bt->sys, V.data());
     // a system that failed the pivot gate is answered with SOG_EPIVOT (and its
     // solution); the batch's other systems are not affected
@@ -522,6 +523,7 @@ int sog_server_wait(sog_server* s, int64_t id, double timeout_ms, double* x, sog
         info->batch_size = r->batch ? (int32_t)r->batch->members.size() : 0;
         info->plan_ms = r->plan_ms;
         info->queue_ms = r->state == R_DONE ? ms_since(r->t_planned, r->t_start) : 0;
+        info->setup_ms = r->setup_ms;
         info->gpu_ms = r->gpu_ms;
         info->total_ms = ms_since(r->t_submit, r->t_done);
     }

@@ -402,11 +402,17 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 y[r] += __shfl_xor_sync(0xffffffffu, y[r], 2);
             }
             if ((lane & 3) == 0) {
+                if constexpr (CL == 1) {
 #pragma unroll
-                for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
-                if constexpr (CL > 1) {
-                    // the row into slot[rank] of every later rank of the group
-                    const uint32_t src = smem_addr(slot + rank * NV + row * NR);
+                    for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
+                } else {
+                    // the row into this CTA's own slot (copied to vec below,
+                    // once the later ranks have it) and into slot[rank] of
+                    // every later rank of the group
+                    T* own = slot + rank * NV + row * NR;
+#pragma unroll
+                    for (int r = 0; r < NR; r++) own[r] = y[r];
+                    const uint32_t src = smem_addr(own);
                     for (int dst = rank + 1; dst < CL; dst++) {
                         const uint32_t a = map_rank(src, (uint32_t)dst);
                         if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
@@ -431,16 +437,25 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         }  // have
         __syncthreads();
         stop = stop || s_stop;
-        if (tid == 0) {
-            if constexpr (CL > 1) {
-                // every later rank's barrier completes one phase per group
-                // (also when this rank has no row or stopped), so that the
-                // parities stay in step
+        if constexpr (CL > 1) {
+            // the later ranks first: their hand-over then waits for no global
+            // store (a fence waits for the stores issued before it). Every
+            // later rank's barrier completes one phase per group (also when
+            // this rank has no row or stopped), so that the parities stay in
+            // step.
+            if (tid == 0) {
                 asm volatile("fence.acq_rel.cluster;" ::: "memory");
                 for (int dst = rank + 1; dst < CL; dst++)
                     mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
                 if (stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
             }
+            __syncthreads();
+            if (have && !stop)
+                for (int e = tid; e < NV; e += NT)
+                    vec[((size_t)i * 64 + e / NR) * ld + c0 + (e % NR)] = slot[rank * NV + e];
+            __syncthreads();
+        }
+        if (tid == 0) {
             if (have && !stop) {
                 fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
                 st_release(s.flags + (size_t)ch * R + i, epoch);
@@ -479,6 +494,7 @@ int trisolve_pair(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int
     const size_t smem = trisolve_smem<T, NR, CL>();
     auto kern = trisolve_kernel<T, NR, CL>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (CL > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     cudaMemsetAsync(s.claim, 0, 8, st);
     if constexpr (CL == 1) {
         kern<<<grid, NT, smem, st>>>(s, tiles, vec, ld, c0, nch, epoch, 1);
@@ -507,7 +523,8 @@ template <typename T, int NR, int CL>
 int resident_clusters() {
     const size_t smem = trisolve_smem<T, NR, CL>();
     auto kern = trisolve_kernel<T, NR, CL>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        (CL > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
         cudaGetLastError();
         return 0;
     }

@@ -59,6 +59,31 @@ def test_fp64_factors_match_oracle(sg, wl, ctx, oracle, name, split):
     sys_.close()
 
 
+@pytest.mark.parametrize("name", SMALL)
+def test_fp64_dense_products_match_fragment_skipping(sg, wl, ctx, oracle, name):
+    """The FP64 products with every DMMA run (the dense variant the autotuner
+    may pick) and with all-zero operand fragments skipped give the same
+    factors (a skipped MMA only adds exact zeros), and both match the oracle."""
+    s = golden_cases(wl)[name]()
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    perm, ops, L, U = p.export()
+    tiles = oracle.calculate(ops, p.info.storage_count, p.input_tiles(s.vals))
+    out = []
+    for skip in (0, 1):
+        sys_ = sg.System(ctx, p, precision=sg.FP64, executor=3)
+        assert sg.lib().sog_debug_fp64_fragment_skip(sys_._h, skip) == 0
+        sys_.factor(s.vals)
+        out.append(sys_.export_factors())
+        sys_.close()
+    (Ld, Ud), (Ls, Us) = out
+    for a, b in ((Ld, Ls), (Ud, Us)):
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))  # -0 == +0
+    for k, (_, _, bid) in enumerate(L):
+        np.testing.assert_allclose(Ld[k], tiles[bid], rtol=0, atol=1e-10 * max(1.0, np.abs(tiles[bid]).max()))
+    for k, (_, _, bid) in enumerate(U):
+        np.testing.assert_allclose(Ud[k], tiles[bid], rtol=0, atol=1e-10 * max(1.0, np.abs(tiles[bid]).max()))
+
+
 @pytest.mark.parametrize("executor", [0, 2], ids=["persistent", "queue"])
 @pytest.mark.parametrize("name", SMALL)
 def test_mixed_refinement_reaches_tolerance(sg, wl, ctx, name, executor):
