@@ -180,9 +180,18 @@ void sog_server::planner_loop() {
 
 int sog_server::run_batch(std::vector<Request*>& group, int lane) {
     auto bt = std::make_shared<Batch>();
-    std::vector<const sog_plan*> plans;
-    for (Request* r : group) plans.push_back(r->plan);
-    int rc = sog_plan_merge(plans.data(), (int32_t)plans.size(), &bt->plan);
+    // a lone request runs on its own plan (a merge would copy it); the plan
+    // goes back to the request if the batch is requeued
+    const bool single = group.size() == 1;
+    int rc = SOG_OK;
+    if (single) {
+        bt->plan = group[0]->plan;
+        group[0]->plan = nullptr;
+    } else {
+        std::vector<const sog_plan*> plans;
+        for (Request* r : group) plans.push_back(r->plan);
+        rc = sog_plan_merge(plans.data(), (int32_t)plans.size(), &bt->plan);
+    }
     if (!rc) rc = sog_system_create(ctx, bt->plan, &opt, &bt->sys);
     if (rc == SOG_ENOMEM) {  // chunks left empty by released batches go back to the device first
         sog_ctx_trim(ctx);
@@ -222,6 +231,10 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
         bool others = false;
         for (size_t k = 0; k < lanes.size(); k++) others = others || ((int)k != lane && lanes[k].busy);
         if (any_resident() || !dead.empty() || others) {
+            if (single) {
+                group[0]->plan = bt->plan;
+                bt->plan = nullptr;
+            }
             group[0]->state = R_PLANNED;
             planned.push_front(group[0]);
             group.clear();

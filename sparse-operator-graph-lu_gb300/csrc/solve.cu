@@ -162,16 +162,23 @@ __device__ __forceinline__ bool mbar_test_cluster(const uint64_t* bar, uint32_t 
 // rank 0's claim of the next group is read by all. Results are bit-identical
 // to CL = 1: the same products in the same order, only the source of the
 // neighbouring rows' values differs.
-// smem: part[8][64*NR] | ybuf[8][64*NR] | acc[64*NR] | slot[CL][64*NR] (CL > 1)
+// smem: part[8][64*NR] | ybuf[8][NVP] | acc[64*NR] | slot[CL][NVP] (CL > 1).
+// A staged row (ybuf, slot) keeps each block row's NR values together, with
+// 16 bytes of padding after every 16 rows: the four lanes of a row quad read
+// rows 16 apart without bank conflicts, 16 bytes at a time.
 template <typename T, int NR, int CL>
 __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
                                                       int cbase, int nch, int epoch, int lower) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NV = 64 * NR;
+    constexpr int PADE = 16 / (int)sizeof(T);  // elements of 16 bytes
+    constexpr int NVP = NV + 4 * PADE;         // a staged row with its padding
+    // element (row, r) of a staged row
+    auto pidx = [](int row, int r) { return row * NR + r + (row >> 4) * PADE; };
     constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte load
     T* part = reinterpret_cast<T*>(smem_raw);
     T* ybuf = part + 8 * NV;
-    T* acc = ybuf + 8 * NV;
+    T* acc = ybuf + 8 * NVP;
     T* slot = acc + NV;  // CL > 1: slot[r] holds the row solved by cluster rank r of this group
     __shared__ int s_stop, s_next;
     __shared__ int s_claim[2], s_cstop;           // CL > 1: rank 0's claims (by group parity), stop flag
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         if (tid == 0) s_next = ld_cluster_s32(map_rank(smem_addr(&s_claim[0]), 0));
     }
     __syncthreads();
-    T* yw = ybuf + warp * NV;
+    T* yw = ybuf + warp * NVP;
     // bounded wait of lane 0 for row j's flag; the warp's later reads of row j
     // are ordered after lane 0's acquire by the __syncwarp that follows
     const int* fl = nullptr;  // this position's chunk of the flags
@@ -291,14 +298,14 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     stop = true;
                     break;
                 }
-                ys = slot + snd * NV;
+                ys = slot + snd * NVP;
             } else {
                 if (!wait_row(j)) {
                     stop = true;
                     break;
                 }
                 const T* vj = vec + (size_t)j * 64 * ld + c0;
-                for (int e = lane; e < NV; e += 32) yw[e] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
+                for (int e = lane; e < NV; e += 32) yw[pidx(e / NR, e % NR)] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
                 __syncwarp();
             }
 #pragma unroll 4
@@ -308,7 +315,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 for (int v = 0; v < VW; v++)
 #pragma unroll
                     for (int r = 0; r < NR; r++) {
-                        const T y = ys[(c + v) * NR + r];
+                        const T y = ys[pidx(c + v, r)];
                         pa[r] += b0.v[v] * y;
                         pb[r] += b1.v[v] * y;
                     }
@@ -361,15 +368,24 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             // from global memory or, within a cluster group, from its slot
             auto apply = [&](const Vec16<T>* mm, int j, int snd) {
                 const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
-                const T* sj = slot + (snd >= 0 ? snd : 0) * NV + cb * NR;
+                const T* sj = slot + (snd >= 0 ? snd : 0) * NVP;
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++)
 #pragma unroll
                     for (int v = 0; v < VW; v++) {
                         T yj[NR];
                         if (CL > 1 && snd >= 0) {
+                            const T* q = sj + pidx(cb + c * VW + v, 0);
+                            if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
 #pragma unroll
-                            for (int r = 0; r < NR; r++) yj[r] = sj[(c * VW + v) * NR + r];
+                                for (int h = 0; h < NR * (int)sizeof(T) / 16; h++) {
+                                    const int4 w4 = reinterpret_cast<const int4*>(q)[h];
+                                    memcpy(&yj[h * PADE], &w4, 16);
+                                }
+                            } else {
+#pragma unroll
+                                for (int r = 0; r < NR; r++) yj[r] = q[r];
+                            }
                         } else {
                             load_row<T, NR>(vj + (size_t)(c * VW + v) * ld, vec16, yj);
                         }
@@ -409,7 +425,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     // the row into this CTA's own slot (copied to vec below,
                     // once the later ranks have it) and into slot[rank] of
                     // every later rank of the group
-                    T* own = slot + rank * NV + row * NR;
+                    T* own = slot + rank * NVP + pidx(row, 0);
 #pragma unroll
                     for (int r = 0; r < NR; r++) own[r] = y[r];
                     const uint32_t src = smem_addr(own);
@@ -452,7 +468,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             __syncthreads();
             if (have && !stop)
                 for (int e = tid; e < NV; e += NT)
-                    vec[((size_t)i * 64 + e / NR) * ld + c0 + (e % NR)] = slot[rank * NV + e];
+                    vec[((size_t)i * 64 + e / NR) * ld + c0 + (e % NR)] = slot[rank * NVP + pidx(e / NR, e % NR)];
             __syncthreads();
         }
         if (tid == 0) {
@@ -482,7 +498,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
 
 template <typename T, int NR, int CL>
 size_t trisolve_smem() {
-    return (size_t)((17 + (CL > 1 ? CL : 0)) * 64 * NR) * sizeof(T);
+    const size_t nv = 64 * NR, nvp = nv + 4 * (16 / sizeof(T));
+    return (9 * nv + (8 + (CL > 1 ? CL : 0)) * nvp) * sizeof(T);
 }
 
 // rows per cluster group of the substitution of a plain system
