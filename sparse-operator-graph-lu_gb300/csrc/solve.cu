@@ -8,9 +8,12 @@
 // block as soon as the block row it multiplies is published (a per-row
 // readiness flag), then solves its diagonal block and publishes its own row.
 // Rows only wait on rows dealt earlier, so the smallest unfinished row can
-// always proceed; every wait is bounded and reports a timeout status. A batch
-// of independent systems deals its rows interleaved (row 0 of every system,
-// then row 1, ...), so that neighbouring CTAs work on different systems.
+// always proceed; every wait is bounded and reports a timeout status. A plain
+// system runs in thread-block clusters that take consecutive rows together and
+// hand each solved row to the cluster's later CTAs through distributed shared
+// memory. A batch of independent systems deals its rows interleaved (row 0 of
+// every system, then row 1, ...), so that neighbouring CTAs work on different
+// systems.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -459,11 +462,12 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             // later rank's barrier completes one phase per group (also when
             // this rank has no row or stopped), so that the parities stay in
             // step.
-            if (tid == 0) {
-                asm volatile("fence.acq_rel.cluster;" ::: "memory");
-                for (int dst = rank + 1; dst < CL; dst++)
-                    mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
-                if (stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
+            if (warp == 0) {  // one lane per later rank: the arrivals go out together
+                if (lane == 0) asm volatile("fence.acq_rel.cluster;" ::: "memory");
+                __syncwarp();
+                const int dst = rank + 1 + lane;
+                if (dst < CL) mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
+                if (lane == 0 && stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
             }
             __syncthreads();
             if (have && !stop)
