@@ -31,7 +31,6 @@ namespace sog {
 namespace {
 
 constexpr int NT = 256;
-constexpr int LD = 65;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;
