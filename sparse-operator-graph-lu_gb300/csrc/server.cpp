@@ -111,6 +111,7 @@ struct sog_server {
     std::deque<Request*> to_plan, planned;
     std::deque<SolveJob*> jobs;
     std::vector<std::shared_ptr<Batch>> dead;  // batches whose requests are all released
+    int freeing = 0;  // batches taken from dead that the scheduler is destroying right now
     std::vector<std::thread> planners;
     std::thread sched;
     std::vector<Lane> lanes;
@@ -230,7 +231,7 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
         // instead of failing
         bool others = false;
         for (size_t k = 0; k < lanes.size(); k++) others = others || ((int)k != lane && lanes[k].busy);
-        if (any_resident() || !dead.empty() || others) {
+        if (any_resident() || !dead.empty() || freeing > 0 || others) {
             if (single) {
                 group[0]->plan = bt->plan;
                 bt->plan = nullptr;
@@ -358,7 +359,7 @@ void sog_server::scheduler_loop() {
             });
             if (stop) return;
             to_free.swap(dead);
-            if (!to_free.empty()) mem_blocked = false;  // memory returns: a blocked request may fit now
+            freeing = (int)to_free.size();  // their memory is on its way back
             if (!jobs.empty()) {
                 job = jobs.front();
                 jobs.pop_front();
@@ -366,7 +367,12 @@ void sog_server::scheduler_loop() {
                 lane = free_lane();
             }
         }
-        to_free.clear();  // destroys systems (on the context's stream)
+        if (!to_free.empty()) {
+            to_free.clear();  // destroys systems (on the context's stream)
+            std::lock_guard<std::mutex> lk(mu);
+            freeing = 0;
+            mem_blocked = false;  // memory returned: a blocked request may fit now
+        }
         if (job) {
             Request* r = job->r;
             int32_t ns = 0;
@@ -416,7 +422,7 @@ void sog_server::scheduler_loop() {
             Request* r = planned.front();
             bool others = false;
             for (auto& ln : lanes) others = others || ln.busy;
-            if (!any_resident() && dead.empty() && !others) {
+            if (!any_resident() && dead.empty() && freeing == 0 && !others) {
                 // larger than the whole pool: refuse it rather than wait forever
                 planned.pop_front();
                 r->state = R_FAILED;
