@@ -420,7 +420,9 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 y[r] += __shfl_xor_sync(0xffffffffu, y[r], 2);
             }
             if ((lane & 3) == 0) {
-                if constexpr (CL == 1) {
+                if (CL == 1 || rank == CL - 1) {
+                    // no later rank: straight to global memory, where the next
+                    // group's first rows wait for it
 #pragma unroll
                     for (int r = 0; r < NR; r++) vec[((size_t)i * 64 + row) * ld + c0 + r] = y[r];
                 } else {
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         }  // have
         __syncthreads();
         stop = stop || s_stop;
-        if constexpr (CL > 1) {
+        if (CL > 1 && rank < CL - 1) {
             // the later ranks first: their hand-over then waits for no global
             // store (a fence waits for the stores issued before it). Every
             // later rank's barrier completes one phase per group (also when
@@ -474,6 +476,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     vec[((size_t)i * 64 + e / NR) * ld + c0 + (e % NR)] = slot[rank * NVP + pidx(e / NR, e % NR)];
             __syncthreads();
         }
+        if (CL > 1 && rank == CL - 1 && tid == 0 && stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
         if (tid == 0) {
             if (have && !stop) {
                 fence_acq_rel_gpu();  // the row written by all threads (ordered by the barrier) before the flag
@@ -574,7 +577,10 @@ template <typename T, int NR>
 int trisolve_chunk(const DevSolve& s, const T* tiles, T* vec, int ld, int c0, int nch, int& epoch, int grid,
                    cudaStream_t st) {
     int rc = 1;
-    if constexpr (NR == 8 || NR == 1) {
+    // clusters for full 8-column chunks: with one right-hand side the
+    // hand-over saves less than the group barrier costs (48^3: 22.1 against
+    // 20.0 ms)
+    if constexpr (NR == 8) {
         constexpr int CL = SOLVE_CLUSTER;
         // the kernel's resident clusters, queried once (every GPU this
         // library drives is the same model)

@@ -182,3 +182,28 @@ def test_batch_uniform_rhs_and_device_entry(sg, wl):
     assert all(q["rel_resid"] <= 1e-10 for q in stats)
     bs.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_clustered_substitution_matches_batch_path(sg, wl):
+    """A plain system's full 8-column chunks run the substitution in thread-
+    block clusters (rows handed over through distributed shared memory); the
+    same system inside a batch runs the unclustered kernel. FP64 results are
+    bit-identical (same products in the same order), with 16 right-hand sides
+    (two chunks of one launch) and a 40x40 grid (32 block rows)."""
+    big = wl.convdiff2d(40, 3.0, 0.5, nrhs=16, seed=7)
+    small = wl.convdiff2d(9, 2.0, 0.0, nrhs=1, seed=8)
+    ctx = sg.Context()
+    p = sg.Plan(big.n, big.rows, big.cols, big.vals)
+    alone = sg.System(ctx, p, precision=sg.FP64)
+    alone.factor(big.vals)
+    xa, sa = alone.solve(big.b)
+    alone.close()
+    plans = [p, sg.Plan(small.n, small.rows, small.cols, small.vals)]
+    bs = sg.System(ctx, sg.merge_plans(plans), precision=sg.FP64)
+    bs.factor(np.concatenate([big.vals, small.vals]))
+    xs, stats = bs.solve_batch([big.b, small.b[:1]])
+    bs.close()
+    assert sa["rel_resid"] <= 1e-12 and stats[0]["rel_resid"] <= 1e-12
+    np.testing.assert_array_equal(xs[0], xa)
+    ctx.close()

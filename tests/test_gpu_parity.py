@@ -176,7 +176,7 @@ def test_bench_config_fp64_vs_reference(sg, wl, ctx):
     sys_.close()
 
 
-def test_north_star_config_64cube(sg, wl, ctx):
+def test_laplacian_64cube_64rhs(sg, wl, ctx):
     """3D 7-point Laplacian 64^3 with 64 right-hand sides (the headline
     configuration, 7.1M unit ops): plain FP64 against the compiled
     reference's x for the first right-hand side (<= 1e-10; the reference
