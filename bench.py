@@ -432,14 +432,14 @@ def run_ours(args):
     hb = torch.from_numpy(work.b).pin_memory()
     hx = torch.empty_like(hb).pin_memory()
 
+    # one call per step: factor, then solve (a plain mixed system runs its
+    # first forward substitution while the factorisation runs)
     def step(sysm, host):
         if not host:
-            sysm.factor_device(V.data_ptr())
-            return sysm.solve_device(nrhs, b.data_ptr(), x.data_ptr())
+            return sysm.factor_solve_device(V.data_ptr(), nrhs, b.data_ptr(), x.data_ptr())
         st = sg.SolveStats()
-        sg._check(L.sog_factor(sysm._h, ctypes.c_void_p(hv.data_ptr())))
-        sg._check(L.sog_solve(sysm._h, nrhs, ctypes.c_void_p(hb.data_ptr()), ctypes.c_void_p(hx.data_ptr()),
-                              ctypes.byref(st)))
+        sg._check(L.sog_factor_solve(sysm._h, ctypes.c_void_p(hv.data_ptr()), nrhs, ctypes.c_void_p(hb.data_ptr()),
+                                     ctypes.c_void_p(hx.data_ptr()), ctypes.byref(st)))
         return st.as_dict()
 
     def timed(sysm, steps, warmup, host=False):
@@ -472,6 +472,12 @@ def run_ours(args):
                       pipeline_stages=args.stages)
     t_sys = time.perf_counter() - t_sys
     rm = timed(mixed, args.steps, args.warmup)
+    # device time of a whole solve (every pass on the system's stream), from
+    # separate factor and solve calls after the timed region: in the timed
+    # steps the first forward pass overlaps the factorisation
+    mixed.factor_device(V.data_ptr())
+    mixed.solve_device(nrhs, b.data_ptr(), x.data_ptr())
+    solve_ms_whole = mixed.last_times()[1]
     grid_mixed = mixed.task_info()["grid"]
     ex = mixed.executor_config()
     chosen = (["persistent, static order", "per level", "persistent, ready queue"][ex["executor"]]
@@ -514,12 +520,14 @@ def run_ours(args):
         tiles_read = (info.n_lleaf + info.n_uleaf - 2 * R) + 2 * R + 2 * R
         pass_bytes = tiles_read * 4096 * 4 + 3 * info.n_ext * 4 * nrhs
         passes = 1 + statistics.mean(rm["iters"])
-        s_ach = pass_bytes / (sm_ * 1e-3 / passes) / 1e9
+        s_ach = pass_bytes / (solve_ms_whole * 1e-3 / passes) / 1e9
         hbm_peak, hbm_src = (MEASURED.get("hbm_gbs"), "MEASURED_PEAKS.json hbm_gbs (measured copy)") \
             if MEASURED.get("hbm_gbs") else (6800.0, "fallback 6.8 TB/s")
         solve_roof = {"bound": "hbm", "kernel": "trisolve_kernel<float> (L and U passes)", "achieved": s_ach,
                       "peak": hbm_peak, "unit": "GB/s", "frac": s_ach / hbm_peak, "peak_source": hbm_src,
-                      "algorithmic_bytes_per_pass": pass_bytes, "passes_per_solve": passes}
+                      "algorithmic_bytes_per_pass": pass_bytes, "passes_per_solve": passes,
+                      "solve_ms": solve_ms_whole, "solve_ms_source": "separate factor and solve calls after "
+                                                                     "the timed steps"}
         fp64_roof = {"achieved": flops / (f64m * 1e-3) / 1e12, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                      "frac": flops / (f64m * 1e-3) / 1e12 / peaks["fp64_tflops"],
                      "peak_source": "cuBLAS DGEMM measured in this run", "avg_factor_ms": f64m}
@@ -553,7 +561,9 @@ def run_ours(args):
                                     "autotuned"][args.executor] + f" ({chosen})",
                        "factor_ctas": grid_mixed, "pipeline_stages": args.stages or "tuned",
                        "timed": "numeric factor + solve; ordering and planning (symbolic analysis) before timing, "
-                                "as in the reference arm"},
+                                "as in the reference arm",
+                       "step_call": "sog_factor_solve_device (a single system: the first forward substitution "
+                                    "overlaps the factorisation; solve_ms is the device time after the factor)"},
             "p50_ms": statistics.median(rm["lat"]), "p99_ms": float(np.percentile(rm["lat"], 99)),
             "factor_ms": fm, "solve_ms": sm_, "refine_steps": max(rm["iters"]),
             "factor_ms_steps": [round(v, 3) for v in rm["factor_ms"]],
@@ -570,7 +580,7 @@ def run_ours(args):
             "solve_roofline": solve_roof,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(work.nnz * 8 + work.b.size * 8),
                     "d2h_bytes_per_step": int(work.b.size * 8), "ms_per_step": re2e["ms"] / args.steps,
-                    "path": "sog_factor + sog_solve with pinned host buffers", "x_equals_device_path": e2e_match},
+                    "path": "sog_factor_solve with pinned host buffers", "x_equals_device_path": e2e_match},
             "cpu_baseline": cpu,
             "clocks": rm["clocks"],
             "gpu_launches": int(rm["launches"]),

@@ -229,6 +229,18 @@ int sog_system_set_stream(sog_system *sys, void *stream);
 int sog_solve(sog_system *sys, int32_t nrhs, const double *b, double *x, sog_solve_stats *stats);
 /* Same with device pointers. */
 int sog_solve_device(sog_system *sys, int32_t nrhs, const double *b_dev, double *x_dev, sog_solve_stats *stats);
+/* sog_factor then sog_solve in one call (host arrays; the device variant
+ * takes device pointers), with the same results and return codes: a pivot-gate
+ * failure (SOG_EPIVOT) still solves with the resident factors. A plain
+ * SOG_MIXED system factored by the static-order executor, with nrhs = 1 or a
+ * multiple of 8 up to 64, runs the first forward substitution while the
+ * factorisation runs, each block row starting once the factor tasks that
+ * produce its tiles have finished. The reference runs BlockPlanner::calculate
+ * and BlockPlanner::solve one after the other (main.cpp). */
+int sog_factor_solve(sog_system *sys, const double *V, int32_t nrhs, const double *b, double *x,
+                     sog_solve_stats *stats);
+int sog_factor_solve_device(sog_system *sys, const double *V_dev, int32_t nrhs, const double *b_dev, double *x_dev,
+                            sog_solve_stats *stats);
 /* Batch solve with a right-hand-side count per system (nrhs[k] >= 0; a
  * system with 0 right-hand sides is skipped): b / x = per system nrhs[k] x
  * n_k values, concatenated in system order. stats, if not NULL, receives one

@@ -92,7 +92,7 @@ EXPORTS = [
     "sog_plan_segments", "sog_solve_batch", "sog_solve_batch_device", "sog_ctx_trim", "sog_server_create",
     "sog_server_submit", "sog_server_wait", "sog_server_solve", "sog_server_release", "sog_server_counters",
     "sog_server_destroy", "sog_mtx_read", "sog_mtx_info", "sog_mtx_copy", "sog_mtx_destroy", "sog_system_pivots",
-    "sog_system_set_stream",
+    "sog_system_set_stream", "sog_factor_solve", "sog_factor_solve_device",
 ]
 
 _lib = None
@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         "sog_system_create": ([P, P, P, P], I32), "sog_system_bytes": ([P, P, P], I32),
         "sog_factor": ([P, P], I32), "sog_factor_device": ([P, P], I32), "sog_factor_tiles": ([P, P], I32),
         "sog_solve": ([P, I32, P, P, P], I32), "sog_solve_device": ([P, I32, P, P, P], I32),
+        "sog_factor_solve": ([P, P, I32, P, P, P], I32), "sog_factor_solve_device": ([P, P, I32, P, P, P], I32),
         "sog_solve_permuted": ([P, P, P], I32), "sog_system_export_factors": ([P, P, P], I32),
         "sog_system_last_times": ([P, P, P], I32), "sog_system_destroy": ([P], None),
         "sog_system_task_info": ([P, P], I32), "sog_system_executor": ([P, P, P, P], I32),
@@ -354,6 +355,32 @@ class System:
         if not (rc == SOG_OK or (allow_noconv and rc == SOG_ENOCONV)):
             _check(rc)
         return x, st.as_dict()
+
+    def factor_solve(self, vals, b, allow_epivot: bool = False, allow_noconv: bool = False):
+        """factor(vals) then solve(b) in one call (a plain mixed system
+        overlaps the first forward substitution with the factorisation):
+        x, the solve statistics and the factor's return code."""
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        if v.shape != (self.plan.nnz,):
+            raise ValueError(f"values must have shape ({self.plan.nnz},)")
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if b.ndim not in (1, 2) or b.shape[-1] != self.n:
+            raise ValueError(f"right-hand side must have shape (n,) or (k, n) with n = {self.n}")
+        if b.ndim == 2 and len(self.plan.segments()) > 1:
+            raise ValueError("several right-hand sides of a batch: use solve_batch")
+        k = 1 if b.ndim == 1 else b.shape[0]
+        x = np.empty_like(b)
+        st = SolveStats()
+        rc = lib().sog_factor_solve(self._h, _p(v), k, _p(b), _p(x), C.byref(st))
+        if not (rc == SOG_OK or (allow_epivot and rc == SOG_EPIVOT) or (allow_noconv and rc == SOG_ENOCONV)):
+            _check(rc)
+        return x, st.as_dict(), rc
+
+    def factor_solve_device(self, vals_ptr: int, nrhs: int, b_ptr: int, x_ptr: int) -> dict:
+        st = SolveStats()
+        _check(lib().sog_factor_solve_device(self._h, C.c_void_p(vals_ptr), nrhs, C.c_void_p(b_ptr),
+                                             C.c_void_p(x_ptr), C.byref(st)))
+        return st.as_dict()
 
     def solve_batch(self, bs, allow_noconv: bool = False):
         """Per-system right-hand sides of a batch system: bs[k] of shape (n_k,)

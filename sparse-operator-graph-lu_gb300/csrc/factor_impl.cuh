@@ -1065,9 +1065,10 @@ __device__ void release_item(const DevTasks& tk, int task) {
         if (last) fence_acq_rel_gpu();  // the other parts' writes, acquired above, released with ours
     }
     if (last) {
-        // completion flag for products started early (ordered after the
+        // completion flag (for products started early and for a forward
+        // substitution overlapping the factorisation; ordered after the
         // CTA's writes by the fence above), then the successors' counts
-        if (lane == 0 && tk.early) st_relaxed(tk.task_done + task, 1);
+        if (lane == 0) st_relaxed(tk.task_done + task, 1);
         for (int k = tk.succ_ptr[task] + lane; k < tk.succ_ptr[task + 1]; k += 32)
             red_release_add(&tk.dep[tk.succ[k]], -1);
     }

@@ -126,6 +126,12 @@ struct DevSolve {
     // resident, so a launch needs no co-residency of all its CTAs (systems on
     // other streams may hold part of the GPU)
     int32_t* claim;
+    // forward substitution overlapped with the factorisation (NULL = off):
+    // per block row the factor tasks producing the tiles it reads
+    // (fwait[fwait_ptr[i] .. fwait_ptr[i+1]]), and the factor's per-task
+    // completion flags; the row starts once all of them are set
+    const int32_t *fwait_ptr, *fwait;
+    const int32_t* task_done;
 };
 // Column chunks of 8 right-hand sides solved together in one launch pair
 constexpr int TRISOLVE_MAX_CHUNKS = 8;
@@ -139,6 +145,17 @@ int trisolve_launch(const DevSolve& s, const double* tiles, double* vec, int nrh
 int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int& epoch, int grid,
                     cudaStream_t st, int& launches);
 int trisolve_grid(bool fp64, int nrhs, int num_sms);
+// The lower (forward) pass alone, for nrhs = 1 or a multiple of 8 up to 64,
+// on grid CTAs, with s.fwait_ptr set: each block row waits for the factor
+// tasks that produce its tiles, so it runs while the factor kernel is still
+// running on other SMs. Uses epoch; the upper pass of the same solve uses
+// epoch + 1 (trisolve_upper_launch).
+int trisolve_lower_overlap_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
+                                  cudaStream_t st);
+// The upper (backward) pass alone, for the same nrhs as the lower pass
+// before it, with epoch + 1 of that pass.
+int trisolve_upper_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch1, int grid,
+                          cudaStream_t st);
 
 // CSR of the permuted, padded matrix for FP64 residuals
 struct DevCSR {

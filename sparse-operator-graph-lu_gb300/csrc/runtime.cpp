@@ -226,6 +226,12 @@ struct sog_system {
     uint64_t cbuf_bytes = 0;
     DevSolve ds_full{};
     std::vector<int32_t> cmap;  // block id -> compact slot while compacted
+    // factor + solve with the forward pass overlapping the factorisation
+    // (sog_factor_solve): per block row the factor tasks producing the tiles
+    // the forward pass reads, and a second stream with its events
+    int32_t *d_fwait_ptr = nullptr, *d_fwait = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_ready = nullptr, ev_lower = nullptr;
 };
 
 namespace {
@@ -410,11 +416,10 @@ int factor_grid(const sog_system* s, int stages) {
     return s->opt.max_ctas > 0 ? std::min(g, s->opt.max_ctas) : g;
 }
 
-int run_factor_once(sog_system* s) {
+// working state of the factor kernels, reset from the pristine copies
+int factor_reset(sog_system* s) {
     cudaStream_t st = s->stream;
     const TaskGraph& g = s->tg;
-    DevStatus fs = fresh_status();
-    // reset working state from pristine copies
     CK(cudaMemcpyAsync(s->dt.dep, s->d_ndep0, sizeof(int32_t) * g.ntasks, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->dt.parts_left, s->d_parts0, sizeof(int32_t) * g.ntasks, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(s->dt.queue, 0xff, sizeof(int32_t) * g.total_items, st));
@@ -424,8 +429,14 @@ int run_factor_once(sog_system* s) {
     CK(cudaMemcpyAsync(s->dt.status, s->d_status0, sizeof(DevStatus), cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->d_piv, s->d_piv0, sizeof(DevPivot) * s->segs.size(), cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(s->dt.task_done, 0, sizeof(int32_t) * g.ntasks, st));
-    (void)fs;
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(unsigned long long) * 4 * g.ntasks, st));
+    return SOG_OK;
+}
+
+int run_factor_once(sog_system* s) {
+    cudaStream_t st = s->stream;
+    const TaskGraph& g = s->tg;
+    if (int r = factor_reset(s)) return r;
     CK(cudaEventRecord(s->e0, st));
     int rc = 0;
     if (s->opt.executor == SOG_EXEC_LEVELS) {
@@ -644,6 +655,20 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
     return SOG_OK;
 }
 
+// the upper pass of a mixed solve whose lower pass ran overlapped with the
+// factorisation (epoch s->epoch; the upper pass takes s->epoch + 1)
+int trisolve_upper_only(sog_system* s, float* vec, int nrhs) {
+    sog_ctx* c = s->ctx;
+    const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));
+    int grid = std::min(s->R * nch, trisolve_grid(false, nrhs, c->num_sms));
+    if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
+    const int rc = trisolve_upper_launch(s->ds, (const float*)s->tiles, vec, nrhs, s->epoch + 1, grid, s->stream);
+    s->epoch += 2;
+    s->launches++;
+    if (rc) return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
+    return SOG_OK;
+}
+
 // Per-system norms of this chunk's residual (columns [c0, c0+nc)), folded
 // into the systems' statistics; rel[k] = worst relative residual of system k
 // over the chunk's columns it has (0 if none).
@@ -673,7 +698,9 @@ int read_norms(sog_system* s, int c0, int nc, std::vector<double>& rel) {
 // gathered into d_bext. Refinement (mixed) corrects only the systems that
 // have not converged yet: the others' corrections are masked to zero, which
 // leaves their iterates bit for bit unchanged.
-int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chunk_stats) {
+// lower_done: the mixed path's first lower pass (of b cast to FP32 in
+// d_v32) already ran, overlapped with the factorisation
+int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chunk_stats, bool lower_done = false) {
     cudaStream_t st = s->stream;
     const int64_t ne = (int64_t)s->n_ext * nc;
     const size_t ns = s->segs.size();
@@ -693,9 +720,13 @@ int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chu
             have_norms = true;
         }
     } else {
-        s->launches++;
-        cast_f64_to_f32_launch(s->d_bext, s->d_v32, ne, st);
-        if ((r = trisolve(s, s->d_v32, nc))) return r;
+        if (lower_done) {
+            if ((r = trisolve_upper_only(s, s->d_v32, nc))) return r;
+        } else {
+            s->launches++;
+            cast_f64_to_f32_launch(s->d_bext, s->d_v32, ne, st);
+            if ((r = trisolve(s, s->d_v32, nc))) return r;
+        }
         s->launches++;
         axpy_f32_to_f64_launch(s->d_v32, s->d_xext, ne, 1, st);
         if (s->csr.ptr) {
@@ -740,7 +771,7 @@ int solve_chunk(sog_system* s, int c0, int nc, std::vector<sog_solve_stats>& chu
 // system nrhs[k] x n_k, rhs-major, concatenated). Per-system statistics go to
 // s->seg_stats; agg (if not NULL) gets the worst over systems.
 int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, double* x_dev,
-                      sog_solve_stats* agg) {
+                      sog_solve_stats* agg, bool lower_done = false) {
     cudaStream_t st = s->stream;
     const size_t ns = s->segs.size();
     int maxr = 0;
@@ -775,9 +806,12 @@ int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, d
     CK(cudaEventRecord(s->e0, st));
     for (int c0 = 0; c0 < maxr; c0 += 64) {
         const int nc = std::min(64, maxr - c0);
-        s->launches++;
-        gather_seg_launch(b_dev, g, s->n_ext, c0, nc, s->d_bext, st);
-        r = solve_chunk(s, c0, nc, out);
+        const bool pre = lower_done && c0 == 0;  // gathered, cast and forward-solved already
+        if (!pre) {
+            s->launches++;
+            gather_seg_launch(b_dev, g, s->n_ext, c0, nc, s->d_bext, st);
+        }
+        r = solve_chunk(s, c0, nc, out, pre);
         if (r) return r;
         s->launches++;
         scatter_seg_launch(s->d_xext, g, s->n_ext, c0, nc, x_dev, s->d_cnt, st);
@@ -838,6 +872,111 @@ int solve_host(sog_system* s, const int32_t* nrhs, const double* b, double* x, s
     c->pool.release(db, bytes);
     c->pool.release(dx, bytes);
     return r;
+}
+
+// factor inputs from device values: input tiles, the CSR values of the
+// residual, max |a_ij| per system
+int factor_inputs(sog_system* s, const double* V_dev) {
+    if (int r = uncompact_tiles(s)) return r;
+    cudaStream_t st = s->stream;
+    const uint64_t eb = elem_bytes(s->opt);
+    CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
+    // input tile k (0-based, as the scatter map counts) is block id k+1
+    s->launches++;
+    scatter_values_launch(V_dev, s->d_vidx, s->d_sc_tile, s->d_sc_off, s->ntrip, s->d_pad_tile, s->d_pad_off, s->npad,
+                          s->fp64 ? (double*)s->tiles + 4096 : nullptr, s->fp64 ? nullptr : (float*)s->tiles + 4096,
+                          st);
+    s->launches++;
+    scatter_csr_launch(V_dev, s->d_vidx, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
+    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), st));
+    s->launches++;
+    csr_absmax_seg_launch(s->csr, seg_view(s), s->d_amax, st);
+    s->amax_global = false;
+    return SOG_OK;
+}
+
+// CTAs of the forward pass that overlaps the factorisation, and the SMs the
+// factor leaves it (the factor's persistent CTAs fill an SM each)
+constexpr int OVERLAP_SOLVE_CTAS = 16;
+constexpr int OVERLAP_SOLVE_SMS = 8;
+
+// Factor, then solve nrhs right-hand sides (device b, x): the same results as
+// sog_factor_device followed by sog_solve_device. A plain mixed system with
+// look-ahead products, factored by the static-order executor (tuned, not
+// compacted) and nrhs = 1 or a multiple of 8 up to 64, runs the first
+// forward pass on a second stream while the factor kernel runs: each block
+// row starts once the factor tasks producing its tiles have finished. The
+// factor then leaves OVERLAP_SOLVE_SMS SMs to that pass.
+int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const double* b_dev, double* x_dev,
+                      sog_solve_stats* stats) {
+    const bool overlap = !s->fp64 && s->segs.size() == 1 && !s->tune_pending && !s->poisoned &&
+                         s->opt.executor == SOG_EXEC_PERSISTENT && !s->opt.resident_compact && s->d_fwait_ptr &&
+                         s->csr.ptr && (nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) &&
+                         s->grid_factor > 2 * OVERLAP_SOLVE_SMS;
+    std::vector<int32_t> k(s->segs.size(), nrhs);
+    if (!overlap) {
+        int r = factor_inputs(s, V_dev);
+        if (!r) r = factor_checked(s);
+        if (r && r != SOG_EPIVOT) return r;
+        const int r2 = solve_device_impl(s, k.data(), b_dev, x_dev, stats);
+        return r ? r : r2;
+    }
+    cudaStream_t st = s->stream;
+    if (!s->stream2) {
+        CK(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&s->ev_ready, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->ev_lower, cudaEventDisableTiming));
+    }
+    int r = factor_inputs(s, V_dev);
+    if (r) return r;
+    // the forward pass's input: b gathered and cast to FP32 (one chunk)
+    s->h_nrhs[0] = nrhs;
+    s->h_voff[0] = 0;
+    if ((r = ensure_vectors(s, nrhs))) return r;
+    CK(cudaMemcpyAsync(s->d_seg_nrhs, s->h_nrhs, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->d_seg_voff, s->h_voff, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    const DevSegs g = seg_view(s);
+    s->launches += 2;
+    gather_seg_launch(b_dev, g, s->n_ext, 0, nrhs, s->d_bext, st);
+    cast_f64_to_f32_launch(s->d_bext, s->d_v32, (int64_t)s->n_ext * nrhs, st);
+    if ((r = factor_reset(s))) return r;
+    CK(cudaEventRecord(s->ev_ready, st));
+    // forward pass on the second stream, after the inputs and the reset
+    // completion flags
+    CK(cudaStreamWaitEvent(s->stream2, s->ev_ready, 0));
+    DevSolve dso = s->ds;
+    dso.fwait_ptr = s->d_fwait_ptr;
+    dso.fwait = s->d_fwait;
+    dso.task_done = s->dt.task_done;
+    const int grid2 = std::min(OVERLAP_SOLVE_CTAS, s->R * std::max(1, nrhs / 8));
+    if (trisolve_lower_overlap_launch(dso, (const float*)s->tiles, s->d_v32, nrhs, s->epoch, grid2, s->stream2))
+        return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
+    s->launches++;
+    CK(cudaEventRecord(s->ev_lower, s->stream2));
+    // the factor on the remaining SMs
+    CK(cudaEventRecord(s->e0, st));
+    const int fgrid = s->grid_factor - OVERLAP_SOLVE_SMS;
+    if (factor_ordered_launch(s->dt, (float*)s->tiles, fgrid, s->stages, st))
+        return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
+    s->launches++;
+    CK(cudaEventRecord(s->e1, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventElapsedTime(&s->t_factor, s->e0, s->e1));
+    r = check_status(s, true);
+    if (r) {
+        cudaStreamSynchronize(s->stream2);
+        return r;
+    }
+    s->factored = true;
+    const int pr = check_pivots(s);
+    if (pr && pr != SOG_EPIVOT) {
+        cudaStreamSynchronize(s->stream2);
+        return pr;
+    }
+    // the rest of the solve after the forward pass
+    CK(cudaStreamWaitEvent(st, s->ev_lower, 0));
+    const int r2 = solve_device_impl(s, k.data(), b_dev, x_dev, stats, true);
+    return pr ? pr : r2;
 }
 
 }  // namespace
@@ -1140,6 +1279,28 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
             task_seg[t] = b > 0 && b < storage2 ? bseg[b] : 0;
         }
     }
+    // forward pass overlapping the factorisation (a plain mixed system with
+    // look-ahead products): per block row the tasks producing its off-diagonal
+    // L leaves, its diagonal inverse and its look-ahead products
+    std::vector<int32_t> fw_ptr, fw;
+    if (!s->fp64 && ns == 1 && !lla.empty()) {
+        fw_ptr.assign(s->R + 1, 0);
+        std::vector<int32_t> row;
+        for (int i = 0; i < s->R; i++) {
+            row.clear();
+            auto add = [&](int32_t blk) {
+                if (blk > 0 && blk < (int32_t)g.producer.size() && g.producer[blk] >= 0) row.push_back(g.producer[blk]);
+            };
+            for (int32_t q = lptr[i]; q < lptr[i + 1]; q++) add(lid[q]);
+            add(ldinv[i]);
+            add(lla[i]);
+            if (!lla2.empty()) add(lla2[i]);
+            std::sort(row.begin(), row.end());
+            row.erase(std::unique(row.begin(), row.end()), row.end());
+            fw.insert(fw.end(), row.begin(), row.end());
+            fw_ptr[i + 1] = (int32_t)fw.size();
+        }
+    }
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),
              o_out2 = L.add<int32_t>(g.ntasks), o_a = L.add<int32_t>(g.ntasks), o_b = L.add<int32_t>(g.ntasks),
@@ -1164,6 +1325,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
              o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()), o_claim = L.add<int32_t>(2),
+             o_fwp = L.add<int32_t>(fw_ptr.size()), o_fw = L.add<int32_t>(fw.size()),
              o_lla2 = L.add<int32_t>(lla2.size()), o_ula2 = L.add<int32_t>(ula2.size()),
              o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
              o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
@@ -1269,6 +1431,10 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     ds.l_la2 = lla2.empty() ? nullptr : put(A, o_lla2, lla2, st);
     ds.u_la2 = ula2.empty() ? nullptr : put(A, o_ula2, ula2, st);
     ds.claim = reinterpret_cast<int32_t*>(A + o_claim);
+    if (!fw_ptr.empty()) {
+        s->d_fwait_ptr = put(A, o_fwp, fw_ptr, st);
+        s->d_fwait = fw.empty() ? reinterpret_cast<int32_t*>(A + o_fw) : put(A, o_fw, fw, st);
+    }
     if (cudaMallocHost(&s->h_red, sizeof(double) * RED * 64 * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_nrhs, sizeof(int32_t) * ns) != cudaSuccess ||
         cudaMallocHost(&s->h_active, sizeof(int32_t) * ns) != cudaSuccess ||
@@ -1321,6 +1487,12 @@ void sog_system_destroy(sog_system* s) {
     if (s->h_cnt) cudaFreeHost(s->h_cnt);
     if (s->e0) cudaEventDestroy(s->e0);
     if (s->e1) cudaEventDestroy(s->e1);
+    if (s->stream2) {
+        cudaStreamSynchronize(s->stream2);
+        cudaStreamDestroy(s->stream2);
+    }
+    if (s->ev_ready) cudaEventDestroy(s->ev_ready);
+    if (s->ev_lower) cudaEventDestroy(s->ev_lower);
     delete s;
 }
 
@@ -1336,24 +1508,50 @@ int sog_factor_device(sog_system* s, const double* V_dev) {
     if (!s) return fail(SOG_EINVAL, "NULL system");
     if (s->imported) return fail(SOG_ESTATE, "imported plan: use sog_factor_tiles");
     if (!V_dev && s->ntrip) return fail(SOG_EINVAL, "NULL values");
+    CK(cudaSetDevice(s->ctx->device));
+    if (int r = factor_inputs(s, V_dev)) return r;
+    return factor_checked(s);
+}
+
+int sog_factor_solve_device(sog_system* s, const double* V_dev, int32_t nrhs, const double* b_dev, double* x_dev,
+                            sog_solve_stats* stats) {
+    if (!s || nrhs <= 0 || !b_dev || !x_dev) return fail(SOG_EINVAL, "bad argument");
+    if (s->imported) return fail(SOG_ESTATE, "imported plan: use sog_factor_tiles");
+    if (!V_dev && s->ntrip) return fail(SOG_EINVAL, "NULL values");
+    CK(cudaSetDevice(s->ctx->device));
+    return factor_solve_impl(s, V_dev, nrhs, b_dev, x_dev, stats);
+}
+
+int sog_factor_solve(sog_system* s, const double* V, int32_t nrhs, const double* b, double* x,
+                     sog_solve_stats* stats) {
+    if (!s || nrhs <= 0 || !b || !x) return fail(SOG_EINVAL, "bad argument");
+    if (s->imported) return fail(SOG_ESTATE, "imported plan: use sog_factor_tiles");
+    if (!V && s->nval) return fail(SOG_EINVAL, "NULL values");
     sog_ctx* c = s->ctx;
     CK(cudaSetDevice(c->device));
-    if (int r = uncompact_tiles(s)) return r;
-    cudaStream_t st = s->stream;
-    const uint64_t eb = elem_bytes(s->opt);
-    CK(cudaMemsetAsync((char*)s->tiles + 4096 * eb, 0, (uint64_t)s->n_input * 4096 * eb, st));
-    // input tile k (0-based, as the scatter map counts) is block id k+1
-    s->launches++;
-    scatter_values_launch(V_dev, s->d_vidx, s->d_sc_tile, s->d_sc_off, s->ntrip, s->d_pad_tile, s->d_pad_off, s->npad,
-                          s->fp64 ? (double*)s->tiles + 4096 : nullptr, s->fp64 ? nullptr : (float*)s->tiles + 4096,
-                          st);
-    s->launches++;
-    scatter_csr_launch(V_dev, s->d_vidx, s->d_csr_pos, s->ntrip, s->d_csr_val, st);
-    CK(cudaMemsetAsync(s->d_amax, 0, sizeof(unsigned long long) * s->segs.size(), st));
-    s->launches++;
-    csr_absmax_seg_launch(s->csr, seg_view(s), s->d_amax, st);
-    s->amax_global = false;
-    return factor_checked(s);
+    if (s->nval) CK(cudaMemcpyAsync(s->d_V, V, sizeof(double) * s->nval, cudaMemcpyHostToDevice, s->stream));
+    const uint64_t bytes = sizeof(double) * (uint64_t)nrhs * (uint64_t)s->n;
+    double* db = static_cast<double*>(c->pool.alloc(bytes));
+    double* dx = static_cast<double*>(c->pool.alloc(bytes));
+    if (!db || !dx) {
+        c->pool.release(db, bytes);
+        c->pool.release(dx, bytes);
+        return fail(SOG_ENOMEM, "block pool exhausted (rhs)");
+    }
+    int r = SOG_OK;
+    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+        r = fail(SOG_ECUDA, "rhs upload failed");
+    if (!r) {
+        r = factor_solve_impl(s, s->d_V, nrhs, db, dx, stats);
+        if (!r || r == SOG_ENOCONV || r == SOG_ENAN || r == SOG_EPIVOT) {
+            if (cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+                cudaStreamSynchronize(s->stream) != cudaSuccess)
+                r = fail(SOG_ECUDA, "download failed");
+        }
+    }
+    c->pool.release(db, bytes);
+    c->pool.release(dx, bytes);
+    return r;
 }
 
 int sog_factor(sog_system* s, const double* V) {

@@ -63,6 +63,16 @@ __device__ __forceinline__ Vec16<T> ldg16(const T* p) {
     memcpy(&o, &r, 16);
     return o;
 }
+// the same through L2 only, for tiles a concurrently running factor kernel
+// has just written (FW: forward pass overlapping the factorisation)
+template <bool FW, typename T>
+__device__ __forceinline__ Vec16<T> ldt16(const T* p) {
+    if constexpr (!FW) return ldg16(p);
+    const int4 r = __ldcg(reinterpret_cast<const int4*>(p));
+    Vec16<T> o;
+    memcpy(&o, &r, 16);
+    return o;
+}
 
 // NR consecutive values of one row of vec, with 16-byte loads where the row
 // segment is 16-byte aligned (vec is written by other CTAs of the launch: L2
@@ -168,9 +178,14 @@ __device__ __forceinline__ bool mbar_test_cluster(const uint64_t* bar, uint32_t 
 // A staged row (ybuf, slot) keeps each block row's NR values together, with
 // 16 bytes of padding after every 16 rows: the four lanes of a row quad read
 // rows 16 apart without bank conflicts, 16 bytes at a time.
-template <typename T, int NR, int CL>
+//
+// FW (forward pass overlapping the factorisation, CL = 1): a row first waits
+// (warp 0, bounded) for the factor tasks that produce its tiles, then reads
+// them through L2 only, with no L1 prefetch.
+template <typename T, int NR, int CL, bool FW = false>
 __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
                                                       int cbase, int nch, int epoch, int lower) {
+    static_assert(!FW || CL == 1, "the overlapped forward pass runs unclustered");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NV = 64 * NR;
     constexpr int PADE = 16 / (int)sizeof(T);  // elements of 16 bytes
@@ -277,22 +292,49 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         bool stop = false;
         if (have) {
         if (s.trace && tid == 0) s.trace[4 * (size_t)i + (lower ? 0 : 2)] = globaltimer_ns();
+        if constexpr (FW) {
+            // the factor tasks producing this row's tiles (acquire by warp 0,
+            // passed to the CTA by the barrier)
+            if (warp == 0) {
+                for (int q = s.fwait_ptr[i] + lane; q < s.fwait_ptr[i + 1]; q += 32) {
+                    const int* f = s.task_done + s.fwait[q];
+                    if (ld_acquire(f) != 0) continue;
+                    const unsigned long long t0 = globaltimer_ns();
+                    while (ld_acquire(f) == 0) {
+                        // a factorisation that gave up never finishes the task
+                        if ((ld_acquire(&s.status->flags) & ST_TIMEOUT) ||
+                            globaltimer_ns() - t0 > s.wait_limit_ns) {
+                            atomicOr(&s.status->flags, ST_SOLVE_TIMEOUT);
+                            s_stop = 1;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                }
+            }
+            __syncthreads();
+            stop = *(volatile int*)&s_stop != 0;
+        }
         const T* Dm = tiles + (size_t)dinv[i] * 4096;
         const int la = lookahead ? lookahead[i] : 0, la2 = lookahead2 ? lookahead2[i] : 0;
         // warm L1 with this lane's slice of the diagonal inverse
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
+        if constexpr (!FW)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
         T pa[NR], pb[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
         // with look-ahead products the last blocks (the neighbouring rows i-1,
         // i-2; the lists run in readiness order) are left out
         const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0) - (la2 > 0 ? 1 : 0);
-        for (int q = ptr[i] + warp; q < q1; q += 8) {
+        for (int q = ptr[i] + warp; q < q1 && !stop; q += 8) {
             const int j = col[q];
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
             // warm L1 with the lane's two block rows (128 contiguous elements) while waiting
+            if constexpr (!FW) {
 #pragma unroll
-            for (int o = 0; o < 128; o += 128 / (int)sizeof(T)) asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
+                for (int o = 0; o < 128; o += 128 / (int)sizeof(T))
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(B + o));
+            }
             const int snd = rank_of(j);
             const T* ys = yw;
             if (snd >= 0) {
@@ -312,7 +354,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             }
 #pragma unroll 4
             for (int c = 0; c < 64; c += VW) {
-                const Vec16<T> b0 = ldg16(B + c), b1 = ldg16(B + 64 + c);
+                const Vec16<T> b0 = ldt16<FW>(B + c), b1 = ldt16<FW>(B + 64 + c);
 #pragma unroll
                 for (int v = 0; v < VW; v++)
 #pragma unroll
@@ -350,16 +392,16 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             if (la > 0) {  // the look-ahead slice, loaded before the wait
                 const T* M = tiles + (size_t)la * 4096 + row * 64 + cb;
 #pragma unroll
-                for (int c = 0; c < 16 / VW; c++) m[c] = ldg16(M + c * VW);
+                for (int c = 0; c < 16 / VW; c++) m[c] = ldt16<FW>(M + c * VW);
             }
-            if (la2 > 0)
+            if (!FW && la2 > 0)
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + (size_t)la2 * 4096 + row * 64 + cb));
             T y[NR];
 #pragma unroll
             for (int r = 0; r < NR; r++) y[r] = T(0);
 #pragma unroll
             for (int c = 0; c < 16; c += VW) {
-                const Vec16<T> d = ldg16(Dm + row * 64 + cb + c);
+                const Vec16<T> d = ldt16<FW>(Dm + row * 64 + cb + c);
 #pragma unroll
                 for (int v = 0; v < VW; v++)
 #pragma unroll
@@ -406,7 +448,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     Vec16<T> m2[16 / VW];
                     const T* M = tiles + (size_t)la2 * 4096 + row * 64 + cb;
 #pragma unroll
-                    for (int c = 0; c < 16 / VW; c++) m2[c] = ldg16(M + c * VW);
+                    for (int c = 0; c < 16 / VW; c++) m2[c] = ldt16<FW>(M + c * VW);
                     apply(m2, j2, snd2);
                 }
             }
@@ -841,6 +883,67 @@ int trisolve_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs,
                     cudaStream_t st, int& launches) {
     return trisolve_impl<float>(s, tiles, vec, nrhs, epoch, grid, st, launches);
 }
+int trisolve_lower_overlap_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
+                                  cudaStream_t st) {
+    if (!s.fwait_ptr || !(nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) || grid < 1) return -1;
+    cudaMemsetAsync(s.claim, 0, 8, st);
+    if (nrhs == 1) {
+        const size_t smem = trisolve_smem<float, 1, 1>();
+        auto kern = trisolve_kernel<float, 1, 1, true>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, 1, epoch, 1);
+    } else {
+        const size_t smem = trisolve_smem<float, 8, 1>();
+        auto kern = trisolve_kernel<float, 8, 1, true>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, nrhs / 8, epoch, 1);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int trisolve_upper_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch1, int grid,
+                          cudaStream_t st) {
+    if (!(nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) || grid < 1) return -1;
+    if (nrhs == 1) {
+        const size_t smem = trisolve_smem<float, 1, 1>();
+        auto kern = trisolve_kernel<float, 1, 1>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, 1, epoch1, 0);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
+    // clusters as in trisolve_chunk (the upper counter was zeroed with the lower one)
+    constexpr int CL = SOLVE_CLUSTER;
+    const int nch = nrhs / 8;
+    const int clusters = resident_clusters<float, 8, CL>();
+    const bool plain = s.order_l == nullptr && s.order_u == nullptr;
+    const size_t smem_cl = trisolve_smem<float, 8, CL>();
+    if (plain && clusters > 0 && grid >= CL) {
+        const int groups = (s.block_rows + CL - 1) / CL * nch;
+        const int ncl = std::max(1, std::min({clusters, groups, grid / CL}));
+        auto kern = trisolve_kernel<float, 8, CL>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cl);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = CL;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(ncl * CL);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = smem_cl;
+        cfg.stream = st;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, kern, s, tiles, vec, nrhs, 0, nch, epoch1, 0) != cudaSuccess) return -1;
+    } else {
+        const size_t smem = trisolve_smem<float, 8, 1>();
+        auto kern = trisolve_kernel<float, 8, 1>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, nch, epoch1, 0);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int trisolve_grid(bool fp64, int nrhs, int num_sms) {
     // the smallest occupancy over the chunk widths this nrhs uses
     int g = 1 << 30;

@@ -320,3 +320,31 @@ def test_resident_compaction(sg, wl, ctx, precision):
     np.testing.assert_array_equal(comp.solve(s.b)[0], full.solve(s.b)[0])
     full.close()
     comp.close()
+
+
+@pytest.mark.parametrize("nrhs", [1, 8, 64])
+@pytest.mark.parametrize("name", ["lap2d_128", "var3d_16", "cd_40"])
+def test_factor_solve_matches_factor_then_solve(sg, wl, ctx, name, nrhs):
+    """The combined call gives the results of factor then solve bit for bit:
+    on the mixed path its first forward substitution runs while the
+    factorisation runs (each block row waits for the factor tasks producing
+    its tiles); the FP64 path runs the two calls. Twice, to reuse the
+    second stream and the completion flags."""
+    s = golden_cases(wl)[name]()
+    b = rhs_of(s) if nrhs == 1 else np.random.default_rng(nrhs).standard_normal((nrhs, s.n))
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    for prec in (sg.MIXED, sg.FP64):
+        a = sg.System(ctx, p, precision=prec, max_refine=20, tol=1e-10)
+        a.factor(s.vals)
+        xa, sa = a.solve(b)
+        c = sg.System(ctx, p, precision=prec, max_refine=20, tol=1e-10)
+        for _ in range(2):
+            xc, sc, rc = c.factor_solve(s.vals, b)
+            assert rc == sg.SOG_OK
+            np.testing.assert_array_equal(xc, xa)
+            # the norms are sums of atomic adds: equal up to their order
+            assert sc["iterations"] == sa["iterations"]
+            assert sc["rel_resid"] == pytest.approx(sa["rel_resid"], rel=1e-12)
+            assert sc["min_pivot"] == sa["min_pivot"]
+        a.close()
+        c.close()
