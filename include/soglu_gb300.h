@@ -75,9 +75,9 @@ typedef struct {
     int32_t max_refine;  /* iterative-refinement steps allowed (SOG_MIXED) */
     double tol;          /* target ||b - A x||_2 / ||b||_2 (SOG_MIXED), e.g. 1e-10 */
     int32_t gemm_split;  /* 0 = auto; FP64 tile products split into 1 or 4 output quadrants */
-    int32_t solve_lookahead; /* 0 = on, -1 = off: the factor also forms Dinv_i * L_{i,i-1} (and the U
-                                counterpart) so each substitution row waits on its neighbour for one
-                                64x64 product only */
+    int32_t solve_lookahead; /* 0 = on, -1 = off: the factor also forms Dinv_i * L_{i,i-d} for d = 1..3
+                                (and the U counterparts) so each substitution row waits on each of its
+                                three nearest rows for one 64x64 product only */
     int32_t pipeline_stages; /* SOG_MIXED tensor-core operand stages: 2 (the next product stages while
                                 one computes; 128 KB of shared memory), 1 (64 KB), or 0 = 2, tuned with
                                 SOG_EXEC_AUTO */

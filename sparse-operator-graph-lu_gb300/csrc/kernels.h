@@ -99,6 +99,10 @@ void convert_tiles_launch(const double* src, float* dst, int64_t n, cudaStream_t
 void widen_tiles_launch(const float* src, double* dst, int64_t n, cudaStream_t s);
 
 // ---- solve (solve.cu) ----
+// Look-ahead distances of the substitution: the blocks of the SOLVE_LOOKAHEAD
+// neighbouring rows are applied as products with the diagonal inverse
+// folded in, each as soon as its row is published
+constexpr int SOLVE_LOOKAHEAD = 3;
 struct DevSolve {
     int32_t block_rows;
     // block-row CSR of off-diagonal L (j < i) and U (j > i) leaves; L sorted by
@@ -117,10 +121,11 @@ struct DevSolve {
     // dependencies must come at earlier positions. Batches interleave their
     // systems so that consecutive positions are independent rows.
     const int32_t *order_l, *order_u;
-    // optional look-ahead products per block row (block id of Dinv_i L_{i,i-1}
-    // / Dinv_i U_{i,i+1}, 0 = none; l_la2 / u_la2: Dinv_i L_{i,i-2} /
-    // Dinv_i U_{i,i+2}); NULL = none
-    const int32_t *l_la, *u_la, *l_la2, *u_la2;
+    // optional look-ahead products per block row: l_la[d-1][i] = block id of
+    // Dinv_i L_{i,i-d}, u_la[d-1][i] of Dinv_i U_{i,i+d} (d = 1 ..
+    // SOLVE_LOOKAHEAD; 0 = none); NULL = none at that distance
+    const int32_t* l_la[SOLVE_LOOKAHEAD];
+    const int32_t* u_la[SOLVE_LOOKAHEAD];
     // position claim counters of the lower and upper launch (zeroed before
     // each launch pair): CTAs claim positions in dealing order as they become
     // resident, so a launch needs no co-residency of all its CTAs (systems on

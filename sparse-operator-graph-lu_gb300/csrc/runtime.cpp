@@ -143,6 +143,10 @@ struct sog_ctx {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
 
+// id arrays of the substitution kept per system (six, then two per
+// look-ahead distance)
+constexpr int NSOL = 6 + 2 * SOLVE_LOOKAHEAD;
+
 struct sog_system {
     sog_ctx* ctx = nullptr;
     // every kernel and copy of this system: the context's stream unless the
@@ -220,7 +224,9 @@ struct sog_system {
     // resident compaction (sog_options.resident_compact): after a
     // factorisation only the tiles the substitution reads stay resident, in
     // their own allocation; the next factorisation allocates the full set again
-    std::vector<int32_t> sol_ids[10];  // host copies of l_id, u_id, l_diag, u_diag, l_dinv, u_dinv, l_la, u_la, l_la2, u_la2
+    // host copies of l_id, u_id, l_diag, u_diag, l_dinv, u_dinv, then per
+    // look-ahead distance d the pair l_la[d], u_la[d]
+    std::vector<int32_t> sol_ids[NSOL];
     bool compacted = false;
     char* cbuf = nullptr;  // compact tiles (slot 0 unused), then the remapped id arrays
     uint64_t cbuf_bytes = 0;
@@ -562,11 +568,11 @@ int compact_tiles(sog_system* s) {
     need.erase(std::unique(need.begin(), need.end()), need.end());
     std::vector<int32_t> cmap(s->storage, 0);
     for (size_t k = 0; k < need.size(); k++) cmap[need[k]] = (int32_t)k + 1;
-    std::vector<int32_t> remap[10];
+    std::vector<int32_t> remap[NSOL];
     Layout Lc;
     const uint64_t o_t = Lc.add<char>((need.size() + 1) * tile), o_need = Lc.add<int32_t>(need.size());
-    uint64_t o_ids[10];
-    for (int a = 0; a < 10; a++) {
+    uint64_t o_ids[NSOL];
+    for (int a = 0; a < NSOL; a++) {
         remap[a].resize(s->sol_ids[a].size());
         for (size_t k = 0; k < remap[a].size(); k++) remap[a][k] = s->sol_ids[a][k] > 0 ? cmap[s->sol_ids[a][k]] : 0;
         o_ids[a] = Lc.add<int32_t>(remap[a].size());
@@ -577,8 +583,8 @@ int compact_tiles(sog_system* s) {
     int32_t* d_need = put(buf, o_need, need, st);
     s->launches++;
     gather_tiles_launch(s->tiles, buf + o_t, d_need, (int64_t)need.size(), tile, st);
-    const int32_t* d_ids[10];
-    for (int a = 0; a < 10; a++) d_ids[a] = remap[a].empty() ? nullptr : put(buf, o_ids[a], remap[a], st);
+    const int32_t* d_ids[NSOL];
+    for (int a = 0; a < NSOL; a++) d_ids[a] = remap[a].empty() ? nullptr : put(buf, o_ids[a], remap[a], st);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         const std::string m = cudaGetErrorString(cudaGetLastError());
         c->pool.release(buf, Lc.off);
@@ -592,10 +598,10 @@ int compact_tiles(sog_system* s) {
     s->ds.u_diag = d_ids[3];
     s->ds.l_dinv = d_ids[4];
     s->ds.u_dinv = d_ids[5];
-    s->ds.l_la = d_ids[6];
-    s->ds.u_la = d_ids[7];
-    s->ds.l_la2 = d_ids[8];
-    s->ds.u_la2 = d_ids[9];
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++) {
+        s->ds.l_la[d] = d_ids[6 + 2 * d];
+        s->ds.u_la[d] = d_ids[7 + 2 * d];
+    }
     s->tiles = buf + o_t;
     s->cbuf = buf;
     s->cbuf_bytes = Lc.off;
@@ -1058,7 +1064,7 @@ int sog_system_bytes(const sog_plan* plan, const sog_options* opt, uint64_t* byt
     // + the transposed L leaves of an LL^T plan
     bool any_sym = p.symmetric;
     for (const Segment& sg : p.segs) any_sym = any_sym || sg.symmetric;
-    uint64_t tiles = ((uint64_t)p.storage_count + 6ull * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
+    uint64_t tiles = ((uint64_t)p.storage_count + (2ull + 2 * SOLVE_LOOKAHEAD) * p.cfg.block_rows + (any_sym ? p.L.size() : 0)) * 4096 *
                      elem_bytes(o);
     uint64_t ops = (uint64_t)p.ops.size();
     uint64_t aux = ops * 40 + (uint64_t)p.scatter_tile.size() * 22 + (uint64_t)p.cfg.n_ext() * 64 + (1 << 20);
@@ -1134,19 +1140,20 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     }
     std::vector<int32_t> ldinv, udinv;
     add_diag_inverses(ops2, storage2, s->R, s->L, s->U, ldinv, udinv);
-    std::vector<int32_t> lla, ula, lla2, ula2;
-    if (o.solve_lookahead >= 0) {
-        add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla, ula);
-        add_lookahead2_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, lla2, ula2);
-    }
+    // look-ahead products by distance: lla[d] / ula[d] at distance d + 1
+    std::vector<int32_t> lla[SOLVE_LOOKAHEAD], ula[SOLVE_LOOKAHEAD];
+    if (o.solve_lookahead >= 0)
+        for (int d = 0; d < SOLVE_LOOKAHEAD; d++)
+            add_lookahead_products(ops2, storage2, s->R, s->L, s->U, ldinv, udinv, d + 1, lla[d], ula[d]);
     s->storage = storage2;
     std::vector<int32_t> outputs;
     for (const Leaf& lf : s->L) outputs.push_back(lf.id);
     for (const Leaf& lf : s->U) outputs.push_back(lf.id);
     for (int32_t id : ldinv) if (id > 0) outputs.push_back(id);
     for (int32_t id : udinv) if (id > 0) outputs.push_back(id);
-    for (auto* v : {&lla, &ula, &lla2, &ula2})
-        for (int32_t id : *v) if (id > 0) outputs.push_back(id);
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++)
+        for (auto* v : {&lla[d], &ula[d]})
+            for (int32_t id : *v) if (id > 0) outputs.push_back(id);
     try {
         s->tg = build_tasks(ops2, storage2, p.n_input, outputs, gemm_parts, true, !s->fp64);
         if (!s->fp64) order_pairs_by_ready(s->tg, false);
@@ -1159,9 +1166,13 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // value lives in its source's tile
     for (Leaf& lf : s->L) lf.id = g.alias[lf.id];
     for (Leaf& lf : s->U) lf.id = g.alias[lf.id];
-    for (auto* v : {&ldinv, &udinv, &lla, &ula, &lla2, &ula2})
+    for (auto* v : {&ldinv, &udinv})
         for (int32_t& id : *v)
             if (id > 0) id = g.alias[id];
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++)
+        for (auto* v : {&lla[d], &ula[d]})
+            for (int32_t& id : *v)
+                if (id > 0) id = g.alias[id];
     // solve structure
     std::vector<int32_t> lptr(s->R + 1, 0), uptr(s->R + 1, 0), ldiag(s->R, 0), udiag(s->R, 0);
     std::vector<Leaf> loff, uoff;
@@ -1190,10 +1201,10 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->sol_ids[3] = udiag;
     s->sol_ids[4] = ldinv;
     s->sol_ids[5] = udinv;
-    s->sol_ids[6] = lla;
-    s->sol_ids[7] = ula;
-    s->sol_ids[8] = lla2;
-    s->sol_ids[9] = ula2;
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++) {
+        s->sol_ids[6 + 2 * d] = lla[d];
+        s->sol_ids[7 + 2 * d] = ula[d];
+    }
     std::vector<int32_t> order = static_order(g, s->fp64);
     // mixed path: the ordered executor starts a product before its last
     // producer finished (item bit 3), waiting per operand pair; every pair
@@ -1283,7 +1294,7 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // look-ahead products): per block row the tasks producing its off-diagonal
     // L leaves, its diagonal inverse and its look-ahead products
     std::vector<int32_t> fw_ptr, fw;
-    if (!s->fp64 && ns == 1 && !lla.empty()) {
+    if (!s->fp64 && ns == 1 && !lla[0].empty()) {
         fw_ptr.assign(s->R + 1, 0);
         std::vector<int32_t> row;
         for (int i = 0; i < s->R; i++) {
@@ -1293,8 +1304,8 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
             };
             for (int32_t q = lptr[i]; q < lptr[i + 1]; q++) add(lid[q]);
             add(ldinv[i]);
-            add(lla[i]);
-            if (!lla2.empty()) add(lla2[i]);
+            for (int d = 0; d < SOLVE_LOOKAHEAD; d++)
+                if (!lla[d].empty()) add(lla[d][i]);
             std::sort(row.begin(), row.end());
             row.erase(std::unique(row.begin(), row.end()), row.end());
             fw.insert(fw.end(), row.begin(), row.end());
@@ -1324,14 +1335,17 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
              o_pdo = L.add<int16_t>(p.pad_off.size()), o_n2o = L.add<int32_t>(n2o.size()),
              o_sbr = L.add<int32_t>(seg_brow.size()), o_sn = L.add<int32_t>(seg_n.size()),
              o_ordl = L.add<int32_t>(ord_l.size()), o_ordu = L.add<int32_t>(ord_u.size()),
-             o_lla = L.add<int32_t>(lla.size()), o_ula = L.add<int32_t>(ula.size()), o_claim = L.add<int32_t>(2),
-             o_fwp = L.add<int32_t>(fw_ptr.size()), o_fw = L.add<int32_t>(fw.size()),
-             o_lla2 = L.add<int32_t>(lla2.size()), o_ula2 = L.add<int32_t>(ula2.size()),
+             o_claim = L.add<int32_t>(2), o_fwp = L.add<int32_t>(fw_ptr.size()), o_fw = L.add<int32_t>(fw.size()),
              o_order = L.add<int32_t>(order.size()), o_pwa = L.add<int32_t>(pair_wa.size()),
              o_pwb = L.add<int32_t>(pair_wb.size()), o_initw = L.add<int32_t>(init_w.size()),
              o_done = L.add<int32_t>(g.ntasks), o_piv = L.add<DevPivot>(ns), o_piv0 = L.add<DevPivot>(ns),
              o_amax = L.add<unsigned long long>(ns), o_tseg = L.add<int32_t>(task_seg.size()),
              o_V = L.add<double>(s->nval), o_vidx = L.add<int32_t>(p.mirror_src.size());
+    uint64_t o_lla[SOLVE_LOOKAHEAD], o_ula[SOLVE_LOOKAHEAD];
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++) {
+        o_lla[d] = L.add<int32_t>(lla[d].size());
+        o_ula[d] = L.add<int32_t>(ula[d].size());
+    }
     s->tiles_bytes = (uint64_t)s->storage * 4096 * elem_bytes(o);
     s->tiles = c->pool.alloc(s->tiles_bytes);
     if (!s->tiles) {
@@ -1426,10 +1440,10 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     s->d_seg_n = put(A, o_sn, seg_n, st);
     ds.order_l = ord_l.empty() ? nullptr : put(A, o_ordl, ord_l, st);
     ds.order_u = ord_u.empty() ? nullptr : put(A, o_ordu, ord_u, st);
-    ds.l_la = lla.empty() ? nullptr : put(A, o_lla, lla, st);
-    ds.u_la = ula.empty() ? nullptr : put(A, o_ula, ula, st);
-    ds.l_la2 = lla2.empty() ? nullptr : put(A, o_lla2, lla2, st);
-    ds.u_la2 = ula2.empty() ? nullptr : put(A, o_ula2, ula2, st);
+    for (int d = 0; d < SOLVE_LOOKAHEAD; d++) {
+        ds.l_la[d] = lla[d].empty() ? nullptr : put(A, o_lla[d], lla[d], st);
+        ds.u_la[d] = ula[d].empty() ? nullptr : put(A, o_ula[d], ula[d], st);
+    }
     ds.claim = reinterpret_cast<int32_t*>(A + o_claim);
     if (!fw_ptr.empty()) {
         s->d_fwait_ptr = put(A, o_fwp, fw_ptr, st);

@@ -112,6 +112,7 @@ struct sog_server {
     std::deque<SolveJob*> jobs;
     std::vector<std::shared_ptr<Batch>> dead;  // batches whose requests are all released
     int freeing = 0;  // batches taken from dead that the scheduler is destroying right now
+    uint64_t mem_gen = 0;  // counts the returns of pool memory (released batches destroyed)
     std::vector<std::thread> planners;
     std::thread sched;
     std::vector<Lane> lanes;
@@ -193,6 +194,11 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
         for (Request* r : group) plans.push_back(r->plan);
         rc = sog_plan_merge(plans.data(), (int32_t)plans.size(), &bt->plan);
     }
+    uint64_t gen0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        gen0 = mem_gen;
+    }
     if (!rc) rc = sog_system_create(ctx, bt->plan, &opt, &bt->sys);
     if (rc == SOG_ENOMEM) {  // chunks left empty by released batches go back to the device first
         sog_ctx_trim(ctx);
@@ -228,10 +234,11 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
         }
         // memory still held by resident requests, by released batches the
         // scheduler has not freed yet, or by other lanes' batches: wait for it
-        // instead of failing
+        // instead of failing; memory returned since the attempt: retry at once
         bool others = false;
         for (size_t k = 0; k < lanes.size(); k++) others = others || ((int)k != lane && lanes[k].busy);
-        if (any_resident() || !dead.empty() || freeing > 0 || others) {
+        const bool returned = mem_gen != gen0;
+        if (returned || any_resident() || !dead.empty() || freeing > 0 || others) {
             if (single) {
                 group[0]->plan = bt->plan;
                 bt->plan = nullptr;
@@ -239,7 +246,7 @@ int sog_server::run_batch(std::vector<Request*>& group, int lane) {
             group[0]->state = R_PLANNED;
             planned.push_front(group[0]);
             group.clear();
-            mem_blocked = true;
+            mem_blocked = !returned;
             return 2;
         }
     }
@@ -371,6 +378,7 @@ void sog_server::scheduler_loop() {
             to_free.clear();  // destroys systems (on the context's stream)
             std::lock_guard<std::mutex> lk(mu);
             freeing = 0;
+            mem_gen++;
             mem_blocked = false;  // memory returned: a blocked request may fit now
         }
         if (job) {

@@ -74,26 +74,6 @@ __device__ __forceinline__ Vec16<T> ldt16(const T* p) {
     return o;
 }
 
-// NR consecutive values of one row of vec, with 16-byte loads where the row
-// segment is 16-byte aligned (vec is written by other CTAs of the launch: L2
-// loads)
-template <typename T, int NR>
-__device__ __forceinline__ void load_row(const T* p, bool vec16, T (&o)[NR]) {
-    constexpr int PER = 16 / (int)sizeof(T);
-    if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
-        if (vec16) {
-#pragma unroll
-            for (int q = 0; q < NR / PER; q++) {
-                const int4 r = __ldcg(reinterpret_cast<const int4*>(p) + q);
-                memcpy(&o[q * PER], &r, 16);
-            }
-            return;
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < NR; r++) o[r] = __ldcg(p + r);
-}
-
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -206,8 +186,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     const int* col = lower ? s.l_col : s.u_col;
     const int* ids = lower ? s.l_id : s.u_id;
     const int* dinv = lower ? s.l_dinv : s.u_dinv;
-    const int* lookahead = lower ? s.l_la : s.u_la;
-    const int* lookahead2 = lower ? s.l_la2 : s.u_la2;
+    const int32_t* const* lookahead = lower ? s.l_la : s.u_la;
     const int dir = lower ? -1 : 1;  // the rows a row waits on lie on this side
     const int* order = lower ? s.order_l : s.order_u;
     int* claim = s.claim + (lower ? 0 : 1);
@@ -230,6 +209,27 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
     }
     __syncthreads();
     T* yw = ybuf + warp * NVP;
+    // row j's NR-column slice [c0, c0+NR) of vec into this warp's buffer yw
+    // (staged layout); vec is written by other CTAs of the launch: L2 loads
+    auto stage_row = [&](int j, int c0, bool vec16) {
+        const T* vj = vec + (size_t)j * 64 * ld + c0;
+        __syncwarp();  // the warp's earlier reads of yw are done
+        if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
+            if (vec16) {
+                constexpr int Q = NR * (int)sizeof(T) / 16;  // 16-byte pieces per block row
+#pragma unroll
+                for (int e = lane; e < 64 * Q; e += 32) {
+                    const int row = e / Q, h = e - row * Q;
+                    const int4 w4 = __ldcg(reinterpret_cast<const int4*>(vj + (size_t)row * ld) + h);
+                    *reinterpret_cast<int4*>(yw + pidx(row, h * PADE)) = w4;
+                }
+                __syncwarp();
+                return;
+            }
+        }
+        for (int e = lane; e < NV; e += 32) yw[pidx(e / NR, e % NR)] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
+        __syncwarp();
+    };
     // bounded wait of lane 0 for row j's flag; the warp's later reads of row j
     // are ordered after lane 0's acquire by the __syncwarp that follows
     const int* fl = nullptr;  // this position's chunk of the flags
@@ -278,6 +278,8 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             }
         }
         const int kg = k / nch, ch = k - kg * nch, c0 = cbase + ch * NR;
+        // this chunk's rows of vec in 16-byte pieces
+        const bool vec16 = ((size_t)ld * sizeof(T)) % 16 == 0 && ((size_t)c0 * sizeof(T)) % 16 == 0;
         const int kk = kg * CL + rank, kk0 = kg * CL;
         const bool have = kk < R;  // CL > 1: the last group may be short
         const int i = !have ? 0 : (order ? order[kk] : (lower ? kk : R - 1 - kk));
@@ -316,16 +318,31 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
             stop = *(volatile int*)&s_stop != 0;
         }
         const T* Dm = tiles + (size_t)dinv[i] * 4096;
-        const int la = lookahead ? lookahead[i] : 0, la2 = lookahead2 ? lookahead2[i] : 0;
+        // this thread's values of b_i (row i of vec is written only by this
+        // CTA, at its end): loaded now, used after the products
+        constexpr int NB = (NV + NT - 1) / NT;
+        T bv[NB];
+#pragma unroll
+        for (int k = 0; k < NB; k++) {
+            const int e = tid + k * NT;
+            bv[k] = e < NV ? __ldcg(vec + ((size_t)i * 64 + e / NR) * ld + c0 + (e % NR)) : T(0);
+        }
+        // look-ahead products of this row by distance (la[d-1]: row i + d*dir)
+        int la[SOLVE_LOOKAHEAD], nla = 0;
+#pragma unroll
+        for (int d = 0; d < SOLVE_LOOKAHEAD; d++) {
+            la[d] = lookahead[d] ? lookahead[d][i] : 0;
+            nla += la[d] > 0;
+        }
         // warm L1 with this lane's slice of the diagonal inverse
         if constexpr (!FW)
             asm volatile("prefetch.global.L1 [%0];" ::"l"(Dm + (warp * 8 + (lane >> 2)) * 64 + (lane & 3) * 16));
         T pa[NR], pb[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) pa[r] = pb[r] = T(0);
-        // with look-ahead products the last blocks (the neighbouring rows i-1,
-        // i-2; the lists run in readiness order) are left out
-        const int q1 = ptr[i + 1] - (la > 0 ? 1 : 0) - (la2 > 0 ? 1 : 0);
+        // with look-ahead products the last blocks (the neighbouring rows; the
+        // lists run in readiness order) are left out
+        const int q1 = ptr[i + 1] - nla;
         for (int q = ptr[i] + warp; q < q1 && !stop; q += 8) {
             const int j = col[q];
             const T* B = tiles + (size_t)ids[q] * 4096 + (2 * lane) * 64;
@@ -348,9 +365,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     stop = true;
                     break;
                 }
-                const T* vj = vec + (size_t)j * 64 * ld + c0;
-                for (int e = lane; e < NV; e += 32) yw[pidx(e / NR, e % NR)] = __ldcg(vj + (size_t)(e / NR) * ld + (e % NR));
-                __syncwarp();
+                stage_row(j, c0, vec16);
             }
 #pragma unroll 4
             for (int c = 0; c < 64; c += VW) {
@@ -375,11 +390,15 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         __syncthreads();
         stop = stop || s_stop;
         if (!stop) {
-        for (int e = tid; e < NV; e += NT) {
-            T v = __ldcg(vec + ((size_t)i * 64 + e / NR) * ld + c0 + (e % NR));
 #pragma unroll
-            for (int w = 0; w < 8; w++) v -= part[w * NV + e];
-            acc[e] = v;
+        for (int k = 0; k < NB; k++) {
+            const int e = tid + k * NT;
+            if (e < NV) {
+                T v = bv[k];
+#pragma unroll
+                for (int w = 0; w < 8; w++) v -= part[w * NV + e];
+                acc[e] = v;
+            }
         }
         }
         __syncthreads();
@@ -387,15 +406,18 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         // per row, each lane 16 columns; partial sums reduced over the four lanes
         if (!stop) {
             const int row = warp * 8 + (lane >> 2), cb = (lane & 3) * 16;
-            const bool vec16 = ((size_t)ld * sizeof(T)) % 16 == 0 && ((size_t)c0 * sizeof(T)) % 16 == 0;
             Vec16<T> m[16 / VW];
-            if (la > 0) {  // the look-ahead slice, loaded before the wait
-                const T* M = tiles + (size_t)la * 4096 + row * 64 + cb;
+            if (la[0] > 0) {  // the nearest row's look-ahead slice, loaded before the wait
+                const T* M = tiles + (size_t)la[0] * 4096 + row * 64 + cb;
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++) m[c] = ldt16<FW>(M + c * VW);
             }
-            if (!FW && la2 > 0)
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + (size_t)la2 * 4096 + row * 64 + cb));
+            if constexpr (!FW) {
+#pragma unroll
+                for (int d = 1; d < SOLVE_LOOKAHEAD; d++)
+                    if (la[d] > 0)
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + (size_t)la[d] * 4096 + row * 64 + cb));
+            }
             T y[NR];
 #pragma unroll
             for (int r = 0; r < NR; r++) y[r] = T(0);
@@ -408,51 +430,59 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                     for (int r = 0; r < NR; r++) y[r] += d.v[v] * acc[(cb + c + v) * NR + r];
             }
             // y -= M y_j over this lane's 16 columns (all warps: a 64x64 product
-            // split over the CTA instead of one warp's block product); row j
-            // from global memory or, within a cluster group, from its slot
+            // split over the CTA instead of one warp's block product). Row j
+            // comes from this CTA's shared memory: within a cluster group from
+            // the sender's slot, otherwise staged from global memory into the
+            // warp's buffer first (independent 16-byte L2 loads, one round
+            // trip, instead of loads interleaved with the products)
             auto apply = [&](const Vec16<T>* mm, int j, int snd) {
-                const T* vj = vec + ((size_t)j * 64 + cb) * ld + c0;
-                const T* sj = slot + (snd >= 0 ? snd : 0) * NVP;
+                const T* sj;
+                if (CL > 1 && snd >= 0) {
+                    sj = slot + snd * NVP;
+                } else {
+                    stage_row(j, c0, vec16);
+                    sj = yw;
+                }
 #pragma unroll
                 for (int c = 0; c < 16 / VW; c++)
 #pragma unroll
                     for (int v = 0; v < VW; v++) {
                         T yj[NR];
-                        if (CL > 1 && snd >= 0) {
-                            const T* q = sj + pidx(cb + c * VW + v, 0);
-                            if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
+                        const T* q = sj + pidx(cb + c * VW + v, 0);
+                        if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
 #pragma unroll
-                                for (int h = 0; h < NR * (int)sizeof(T) / 16; h++) {
-                                    const int4 w4 = reinterpret_cast<const int4*>(q)[h];
-                                    memcpy(&yj[h * PADE], &w4, 16);
-                                }
-                            } else {
-#pragma unroll
-                                for (int r = 0; r < NR; r++) yj[r] = q[r];
+                            for (int h = 0; h < NR * (int)sizeof(T) / 16; h++) {
+                                const int4 w4 = reinterpret_cast<const int4*>(q)[h];
+                                memcpy(&yj[h * PADE], &w4, 16);
                             }
                         } else {
-                            load_row<T, NR>(vj + (size_t)(c * VW + v) * ld, vec16, yj);
+#pragma unroll
+                            for (int r = 0; r < NR; r++) yj[r] = q[r];
                         }
 #pragma unroll
                         for (int r = 0; r < NR; r++) y[r] -= mm[c].v[v] * yj[r];
                     }
             };
             auto wait_any = [&](int j, int snd) { return snd >= 0 ? wait_rank(snd) : wait_row(j); };
-            // row i-2 first (M2 = Dinv_i B_{i,i-2}), then row i-1 (M1); a wait
-            // that runs out sets s_stop: the CTA publishes nothing
+            // the farthest look-ahead row first (Md = Dinv_i B_{i,i+d*dir}),
+            // the nearest last; a wait that runs out sets s_stop: the CTA
+            // publishes nothing
             bool ok = true;
-            if (la2 > 0) {
-                const int j2 = i + 2 * dir, snd2 = rank_of(j2);
-                ok = wait_any(j2, snd2);
-                if (ok) {
-                    Vec16<T> m2[16 / VW];
-                    const T* M = tiles + (size_t)la2 * 4096 + row * 64 + cb;
 #pragma unroll
-                    for (int c = 0; c < 16 / VW; c++) m2[c] = ldt16<FW>(M + c * VW);
-                    apply(m2, j2, snd2);
+            for (int d = SOLVE_LOOKAHEAD - 1; d >= 1; d--) {
+                if (ok && la[d] > 0) {
+                    const int jd = i + (d + 1) * dir, sndd = rank_of(jd);
+                    ok = wait_any(jd, sndd);
+                    if (ok) {
+                        Vec16<T> md[16 / VW];
+                        const T* M = tiles + (size_t)la[d] * 4096 + row * 64 + cb;
+#pragma unroll
+                        for (int c = 0; c < 16 / VW; c++) md[c] = ldt16<FW>(M + c * VW);
+                        apply(md, jd, sndd);
+                    }
                 }
             }
-            if (ok && la > 0) {
+            if (ok && la[0] > 0) {
                 const int j1 = i + dir, snd1 = rank_of(j1);
                 if (wait_any(j1, snd1)) apply(m, j1, snd1);
             }

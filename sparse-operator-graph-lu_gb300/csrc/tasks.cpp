@@ -492,43 +492,23 @@ void order_pairs_by_ready(TaskGraph& g, bool fp64) {
 
 void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                            const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula) {
+                            const std::vector<int32_t>& uinv, int dist, std::vector<int32_t>& lla,
+                            std::vector<int32_t>& ula) {
     lla.assign(block_rows, 0);
     ula.assign(block_rows, 0);
     int32_t seq = ops.last_seq();
     const int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
     for (const Leaf& lf : L)
-        if (lf.bj == lf.bi - 1 && linv[lf.bi] > 0) {
+        if (lf.bj == lf.bi - dist && linv[lf.bi] > 0) {
             const int32_t id = storage_count++;
             ops.extra.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             lla[lf.bi] = id;
         }
     for (const Leaf& lf : U)
-        if (lf.bj == lf.bi + 1 && uinv[lf.bi] > 0) {
+        if (lf.bj == lf.bi + dist && uinv[lf.bi] > 0) {
             const int32_t id = storage_count++;
             ops.extra.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
             ula[lf.bi] = id;
-        }
-}
-
-void add_lookahead2_products(OpSeq& ops, int32_t& storage_count, int block_rows,
-                             const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2) {
-    lla2.assign(block_rows, 0);
-    ula2.assign(block_rows, 0);
-    int32_t seq = ops.last_seq();
-    const int32_t stage = ops.size() == 0 ? 1 : ops.last_stage() + 1;
-    for (const Leaf& lf : L)
-        if (lf.bj == lf.bi - 2 && linv[lf.bi] > 0) {
-            const int32_t id = storage_count++;
-            ops.extra.push_back({OP_MUL, linv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
-            lla2[lf.bi] = id;
-        }
-    for (const Leaf& lf : U)
-        if (lf.bj == lf.bi + 2 && uinv[lf.bi] > 0) {
-            const int32_t id = storage_count++;
-            ops.extra.push_back({OP_MUL, uinv[lf.bi], lf.id, id, 0, stage, ++seq, 0});
-            ula2[lf.bi] = id;
         }
 }
 

@@ -112,20 +112,16 @@ std::vector<int32_t> static_order(const TaskGraph& g, bool fp64);
 // accumulates the ready pairs first and the late one last.
 void order_pairs_by_ready(TaskGraph& g, bool fp64);
 
-// Look-ahead products for the substitution: for every block row i with an L
-// block at (i, i-1), lla[i] = id of a new block Linv_ii * L_{i,i-1}; for every
-// U block at (i, i+1), ula[i] = id of Uinv_ii * U_{i,i+1} (0 = none). The
-// substitution then forms y_i = Linv_ii (b_i - sum_{j<i-1} L_ij y_j) - lla_i
-// y_{i-1}: everything but one 64x64 product is done before row i-1 is ready.
+// Look-ahead products for the substitution at distance dist: for every block
+// row i with an L block at (i, i-dist), lla[i] = id of a new block Linv_ii *
+// L_{i,i-dist}; for every U block at (i, i+dist), ula[i] = id of Uinv_ii *
+// U_{i,i+dist} (0 = none). With distances 1..d the substitution forms y_i =
+// Linv_ii (b_i - sum_{j<i-d} L_ij y_j) - sum_k lla_k[i] y_{i-k}: each of the
+// d nearest rows costs one 64x64 product once it is published, and the rest
+// is done before.
 void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, const std::vector<Leaf>& L,
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                            const std::vector<int32_t>& uinv, std::vector<int32_t>& lla, std::vector<int32_t>& ula);
-// The same at distance 2: lla2[i] = Linv_ii * L_{i,i-2}, ula2[i] = Uinv_ii *
-// U_{i,i+2} (0 = none), so the block of row i-2 is applied by the whole
-// substitution CTA as soon as that row is published, and row i waits only on
-// its two neighbours' products.
-void add_lookahead2_products(OpSeq& ops, int32_t& storage_count, int block_rows,
-                             const std::vector<Leaf>& L, const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
-                             const std::vector<int32_t>& uinv, std::vector<int32_t>& lla2, std::vector<int32_t>& ula2);
+                            const std::vector<int32_t>& uinv, int dist, std::vector<int32_t>& lla,
+                            std::vector<int32_t>& ula);
 
 }  // namespace sog
