@@ -258,7 +258,9 @@ int sog_solve_permuted(sog_system *sys, const double *b_ext, double *x_ext);
  * plan has L leaves only). */
 int sog_system_export_factors(sog_system *sys, double *ltiles, double *utiles);
 /* Device time of the last factor / solve in milliseconds (CUDA events on the
- * context's stream). */
+ * context's stream; after sog_factor_solve the solve's time runs from the end
+ * of the factor kernel, including any wait for the overlapped forward
+ * substitution). */
 int sog_system_last_times(const sog_system *sys, double *factor_ms, double *solve_ms);
 void sog_system_destroy(sog_system *sys);
 /* Build the device task graph of a plan on the host only (no device):

@@ -157,6 +157,11 @@ int trisolve_grid(bool fp64, int nrhs, int num_sms);
 // epoch + 1 (trisolve_upper_launch).
 int trisolve_lower_overlap_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
                                   cudaStream_t st);
+// After the factor kernel has finished: the same lower pass on grid more
+// CTAs, without the factor waits, sharing the overlapped launch's claim
+// counter and flags, so it takes over every position not yet claimed.
+int trisolve_lower_join_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
+                               cudaStream_t st);
 // The upper (backward) pass alone, for the same nrhs as the lower pass
 // before it, with epoch + 1 of that pass.
 int trisolve_upper_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch1, int grid,

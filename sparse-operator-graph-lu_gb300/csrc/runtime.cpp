@@ -809,7 +809,9 @@ int solve_device_impl(sog_system* s, const int32_t* nrhs, const double* b_dev, d
     CK(cudaMemcpyAsync(s->d_seg_voff, s->h_voff, sizeof(int64_t) * ns, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->d_cnt, 0, sizeof(unsigned long long) * ns, st));
     const DevSegs g = seg_view(s);
-    CK(cudaEventRecord(s->e0, st));
+    // solve time from here (lower_done: from the factorisation's end, set by
+    // the caller, so that waiting for the overlapped forward pass counts)
+    if (!lower_done) CK(cudaEventRecord(s->e0, st));
     for (int c0 = 0; c0 < maxr; c0 += 64) {
         const int nc = std::min(64, maxr - c0);
         const bool pre = lower_done && c0 == 0;  // gathered, cast and forward-solved already
@@ -902,9 +904,11 @@ int factor_inputs(sog_system* s, const double* V_dev) {
 }
 
 // CTAs of the forward pass that overlaps the factorisation, and the SMs the
-// factor leaves it (the factor's persistent CTAs fill an SM each)
-constexpr int OVERLAP_SOLVE_CTAS = 16;
-constexpr int OVERLAP_SOLVE_SMS = 8;
+// factor leaves it (the factor's persistent CTAs fill an SM each); once the
+// factor has finished, a launch on the whole GPU takes over the positions
+// that pass has not reached
+constexpr int OVERLAP_SOLVE_CTAS = 8;
+constexpr int OVERLAP_SOLVE_SMS = 4;
 
 // Factor, then solve nrhs right-hand sides (device b, x): the same results as
 // sog_factor_device followed by sog_solve_device. A plain mixed system with
@@ -974,12 +978,23 @@ int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const do
         return r;
     }
     s->factored = true;
+    // the forward pass's positions not yet claimed, on the whole GPU
+    {
+        const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));
+        int grid = std::min(s->R * nch, trisolve_grid(false, nrhs, s->ctx->num_sms));
+        if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
+        if (trisolve_lower_join_launch(s->ds, (const float*)s->tiles, s->d_v32, nrhs, s->epoch, grid, st))
+            return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
+        s->launches++;
+    }
     const int pr = check_pivots(s);
     if (pr && pr != SOG_EPIVOT) {
         cudaStreamSynchronize(s->stream2);
         return pr;
     }
-    // the rest of the solve after the forward pass
+    // the rest of the solve after the forward pass; the solve time counts
+    // from the factor kernel's end (its event becomes the solve's start)
+    std::swap(s->e0, s->e1);
     CK(cudaStreamWaitEvent(st, s->ev_lower, 0));
     const int r2 = solve_device_impl(s, k.data(), b_dev, x_dev, stats, true);
     return pr ? pr : r2;

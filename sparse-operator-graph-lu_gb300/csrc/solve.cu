@@ -931,6 +931,25 @@ int trisolve_lower_overlap_launch(const DevSolve& s, const float* tiles, float* 
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+int trisolve_lower_join_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch, int grid,
+                               cudaStream_t st) {
+    if (!(nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) || grid < 1) return -1;
+    // the overlapped pass's kernel without its factor waits, on the same
+    // claim counter (not zeroed again) and flags
+    if (nrhs == 1) {
+        const size_t smem = trisolve_smem<float, 1, 1>();
+        auto kern = trisolve_kernel<float, 1, 1>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, 1, epoch, 1);
+    } else {
+        const size_t smem = trisolve_smem<float, 8, 1>();
+        auto kern = trisolve_kernel<float, 8, 1>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, NT, smem, st>>>(s, tiles, vec, nrhs, 0, nrhs / 8, epoch, 1);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int trisolve_upper_launch(const DevSolve& s, const float* tiles, float* vec, int nrhs, int epoch1, int grid,
                           cudaStream_t st) {
     if (!(nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) || grid < 1) return -1;
