@@ -1310,22 +1310,9 @@ int sog_system_create(sog_ctx* c, const sog_plan* plan, const sog_options* opt, 
     // L leaves, its diagonal inverse and its look-ahead products
     std::vector<int32_t> fw_ptr, fw;
     if (!s->fp64 && ns == 1 && !lla[0].empty()) {
-        fw_ptr.assign(s->R + 1, 0);
-        std::vector<int32_t> row;
-        for (int i = 0; i < s->R; i++) {
-            row.clear();
-            auto add = [&](int32_t blk) {
-                if (blk > 0 && blk < (int32_t)g.producer.size() && g.producer[blk] >= 0) row.push_back(g.producer[blk]);
-            };
-            for (int32_t q = lptr[i]; q < lptr[i + 1]; q++) add(lid[q]);
-            add(ldinv[i]);
-            for (int d = 0; d < SOLVE_LOOKAHEAD; d++)
-                if (!lla[d].empty()) add(lla[d][i]);
-            std::sort(row.begin(), row.end());
-            row.erase(std::unique(row.begin(), row.end()), row.end());
-            fw.insert(fw.end(), row.begin(), row.end());
-            fw_ptr[i + 1] = (int32_t)fw.size();
-        }
+        std::vector<const std::vector<int32_t>*> las;
+        for (int d = 0; d < SOLVE_LOOKAHEAD; d++) las.push_back(&lla[d]);
+        forward_wait_lists(g, s->R, lptr, lid, ldinv, las, fw_ptr, fw);
     }
     Layout L;
     uint64_t o_kind = L.add<uint8_t>(g.ntasks), o_parts = L.add<uint8_t>(g.ntasks), o_out = L.add<int32_t>(g.ntasks),

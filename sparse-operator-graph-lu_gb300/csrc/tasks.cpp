@@ -512,4 +512,27 @@ void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, 
         }
 }
 
+void forward_wait_lists(const TaskGraph& g, int block_rows, const std::vector<int32_t>& lptr,
+                        const std::vector<int32_t>& lid, const std::vector<int32_t>& linv,
+                        const std::vector<const std::vector<int32_t>*>& la, std::vector<int32_t>& ptr,
+                        std::vector<int32_t>& list) {
+    ptr.assign(block_rows + 1, 0);
+    list.clear();
+    std::vector<int32_t> row;
+    auto add = [&](int32_t blk) {
+        if (blk > 0 && blk < (int32_t)g.producer.size() && g.producer[blk] >= 0) row.push_back(g.producer[blk]);
+    };
+    for (int i = 0; i < block_rows; i++) {
+        row.clear();
+        for (int32_t q = lptr[i]; q < lptr[i + 1]; q++) add(lid[q]);
+        add(linv[i]);
+        for (const std::vector<int32_t>* v : la)
+            if (!v->empty()) add((*v)[i]);
+        std::sort(row.begin(), row.end());
+        row.erase(std::unique(row.begin(), row.end()), row.end());
+        list.insert(list.end(), row.begin(), row.end());
+        ptr[i + 1] = (int32_t)list.size();
+    }
+}
+
 }  // namespace sog

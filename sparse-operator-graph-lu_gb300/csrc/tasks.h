@@ -123,5 +123,15 @@ void add_lookahead_products(OpSeq& ops, int32_t& storage_count, int block_rows, 
                             const std::vector<Leaf>& U, const std::vector<int32_t>& linv,
                             const std::vector<int32_t>& uinv, int dist, std::vector<int32_t>& lla,
                             std::vector<int32_t>& ula);
+// The forward substitution overlapping the factorisation: per block row i
+// the tasks producing the tiles it reads (its off-diagonal L leaves
+// lid[lptr[i] .. lptr[i+1]), its diagonal inverse linv[i] and its look-ahead
+// products la[d][i]), sorted and unique, as list[ptr[i] .. ptr[i+1]). Block
+// ids are the graph's (aliased) ids; tiles no task writes (input blocks) need
+// no wait.
+void forward_wait_lists(const TaskGraph& g, int block_rows, const std::vector<int32_t>& lptr,
+                        const std::vector<int32_t>& lid, const std::vector<int32_t>& linv,
+                        const std::vector<const std::vector<int32_t>*>& la, std::vector<int32_t>& ptr,
+                        std::vector<int32_t>& list);
 
 }  // namespace sog

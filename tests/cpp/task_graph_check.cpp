@@ -11,7 +11,11 @@
 //    task writes the same L, U, L^-1 and U^-1 blocks as the LU task it
 //    absorbed, whose input block it produces and nothing else reads;
 //  - reordering pairs by readiness permutes each product's pairs only;
-//  - the static claim order lists every item once, predecessors first.
+//  - the static claim order lists every item once, predecessors first;
+//  - look-ahead products Dinv_i * L_{i,i-d} (d = 1..3, and the U
+//    counterparts) exist exactly for the leaves at that distance, and the
+//    forward-wait list of each block row names, sorted and once, the task
+//    that writes each non-input tile the row reads, and no other task.
 // Prints "ok" and exits 0, or prints the first violation and exits 1.
 #include <algorithm>
 #include <cstdio>
@@ -101,6 +105,105 @@ static std::vector<std::pair<int32_t, int32_t>> pairs_of(const TaskGraph& g, int
     return v;
 }
 
+// blocks a task writes
+static std::vector<int32_t> writes_of(const TaskGraph& g, int32_t t) {
+    std::vector<int32_t> w = {g.out[t]};
+    const uint8_t k = g.kind[t];
+    if (k == K_LU || k == K_LLT || k == K_GEMM_LU || k == K_GEMM_LLT) {
+        w.push_back(g.out2[t]);
+        w.push_back(g.b[t]);
+        w.push_back(g.c[t]);
+    }
+    if (k == K_GEMM_LU || k == K_GEMM_LLT) w.push_back(g.out3[t]);
+    return w;
+}
+
+// look-ahead products and the forward substitution's wait lists (mixed graph)
+static void check_lookahead(const char* name, const Plan& p) {
+    constexpr int D = 3;
+    OpSeq ops(p.ops.data(), (int64_t)p.ops.size());
+    int32_t storage = p.storage_count;
+    const int R = p.cfg.block_rows;
+    std::vector<int32_t> linv, uinv, outputs;
+    add_diag_inverses(ops, storage, R, p.L, p.U, linv, uinv);
+    std::vector<int32_t> lla[D], ula[D];
+    for (int d = 0; d < D; d++) {
+        const size_t before = ops.extra.size();
+        add_lookahead_products(ops, storage, R, p.L, p.U, linv, uinv, d + 1, lla[d], ula[d]);
+        std::map<int32_t, Op> made;  // result block -> op
+        for (size_t k = before; k < ops.extra.size(); k++) made[ops.extra[k].res] = ops.extra[k];
+        std::vector<int32_t> lwant(R, 0), uwant(R, 0);
+        for (const Leaf& lf : p.L)
+            if (lf.bj == lf.bi - (d + 1)) lwant[lf.bi] = lf.id;
+        for (const Leaf& lf : p.U)
+            if (lf.bj == lf.bi + (d + 1)) uwant[lf.bi] = lf.id;
+        for (int i = 0; i < R; i++) {
+            CHECK((lla[d][i] > 0) == (lwant[i] > 0), "%s: row %d L look-ahead at %d", name, i, d + 1);
+            CHECK((ula[d][i] > 0) == (uwant[i] > 0), "%s: row %d U look-ahead at %d", name, i, d + 1);
+            if (lla[d][i] > 0) {
+                const Op& o = made.at(lla[d][i]);
+                CHECK(o.op == OP_MUL && o.src == linv[i] && o.src2 == lwant[i], "%s: L product of row %d", name, i);
+            }
+            if (ula[d][i] > 0) {
+                const Op& o = made.at(ula[d][i]);
+                CHECK(o.op == OP_MUL && o.src == uinv[i] && o.src2 == uwant[i], "%s: U product of row %d", name, i);
+            }
+        }
+        CHECK(made.size() == (size_t)(std::count_if(lwant.begin(), lwant.end(), [](int32_t v) { return v > 0; }) +
+                                      std::count_if(uwant.begin(), uwant.end(), [](int32_t v) { return v > 0; })),
+              "%s: extra look-ahead products at %d", name, d + 1);
+    }
+    for (const Leaf& lf : p.L) outputs.push_back(lf.id);
+    for (const Leaf& lf : p.U) outputs.push_back(lf.id);
+    for (int32_t id : linv) outputs.push_back(id);
+    for (int32_t id : uinv) outputs.push_back(id);
+    for (int d = 0; d < D; d++)
+        for (auto* v : {&lla[d], &ula[d]})
+            for (int32_t id : *v)
+                if (id > 0) outputs.push_back(id);
+    const TaskGraph g = build_tasks(ops, storage, p.n_input, outputs, 1, true, true);
+    // the substitution's view: aliased ids, off-diagonal L leaves by (row, column)
+    std::vector<Leaf> loff;
+    for (Leaf lf : p.L) {
+        lf.id = g.alias[lf.id];
+        if (lf.bj < lf.bi) loff.push_back(lf);
+    }
+    std::sort(loff.begin(), loff.end(), [](const Leaf& a, const Leaf& b) { return a.bi != b.bi ? a.bi < b.bi : a.bj < b.bj; });
+    std::vector<int32_t> lptr(R + 1, 0), lid;
+    for (const Leaf& lf : loff) { lptr[lf.bi + 1]++; lid.push_back(lf.id); }
+    for (int i = 0; i < R; i++) lptr[i + 1] += lptr[i];
+    for (int32_t& id : linv) if (id > 0) id = g.alias[id];
+    std::vector<const std::vector<int32_t>*> las;
+    for (int d = 0; d < D; d++) {
+        for (int32_t& id : lla[d]) if (id > 0) id = g.alias[id];
+        las.push_back(&lla[d]);
+    }
+    std::vector<int32_t> fptr, fw;
+    forward_wait_lists(g, R, lptr, lid, linv, las, fptr, fw);
+    CHECK((int)fptr.size() == R + 1 && fptr[R] == (int32_t)fw.size(), "%s: wait list offsets", name);
+    for (int i = 0; i < R; i++) {
+        std::vector<int32_t> tiles(lid.begin() + lptr[i], lid.begin() + lptr[i + 1]);
+        tiles.push_back(linv[i]);
+        for (int d = 0; d < D; d++) tiles.push_back(lla[d][i]);
+        std::vector<int32_t> want;  // writers of the row's non-input tiles, from the tasks' own outputs
+        for (int32_t b : tiles) {
+            if (b <= p.n_input) continue;
+            int32_t writer = -1;
+            for (int32_t t = 0; t < g.ntasks && writer < 0; t++) {
+                const std::vector<int32_t> w = writes_of(g, t);
+                if (std::find(w.begin(), w.end(), b) != w.end()) writer = t;
+            }
+            CHECK(writer >= 0, "%s: row %d reads block %d that no task writes", name, i, b);
+            want.push_back(writer);
+        }
+        std::sort(want.begin(), want.end());
+        want.erase(std::unique(want.begin(), want.end()), want.end());
+        const std::vector<int32_t> got(fw.begin() + fptr[i], fw.begin() + fptr[i + 1]);
+        CHECK(got == want, "%s: row %d waits on %zu tasks, its tiles have %zu writers", name, i, got.size(),
+              want.size());
+    }
+}
+
 static void check_system(const char* name, int n, const std::vector<int32_t>& I, const std::vector<int32_t>& J,
                          const std::vector<double>& V) {
     sog_plan* plan = nullptr;
@@ -154,6 +257,7 @@ static void check_system(const char* name, int n, const std::vector<int32_t>& I,
     check_order(plain, true, (nm + " plain").c_str());
     check_order(fp64, true, (nm + " fp64").c_str());
     check_order(mixed, false, (nm + " mixed").c_str());
+    check_lookahead(name, p);
     sog_plan_destroy(plan);
 }
 
