@@ -130,6 +130,11 @@ __device__ __forceinline__ bool mbar_test_cluster(const uint64_t* bar, uint32_t 
     return done != 0;
 }
 
+// A row solved by a cluster rank goes through distributed shared memory to
+// the next SOLVE_FANOUT ranks of its group; farther ranks, which need it
+// several hops later, read it from global memory like rows of earlier groups
+constexpr int SOLVE_FANOUT = 7;
+
 // One launch per triangle and per chunk of NR right-hand-side columns
 // [c0, c0+NR) of vec (n_ext x ld, row-major). For block row i the warps split
 // its off-diagonal blocks: each warp waits (bounded) only for the row its
@@ -145,8 +150,8 @@ __device__ __forceinline__ bool mbar_test_cluster(const uint64_t* bar, uint32_t 
 // CL > 1 (a plain system, no dealing order): the CTAs of a thread-block
 // cluster take CL consecutive rows of one column chunk together (cluster rank
 // r: the r-th row in dealing order). A solved row is also stored straight into
-// the shared memory of every later rank of the cluster, with one mbarrier
-// arrival per receiving rank, so the hand-over between neighbouring rows of a
+// the shared memory of the next SOLVE_FANOUT ranks of the cluster, with one
+// mbarrier arrival per receiving rank, so the hand-over between neighbouring rows of a
 // group is a distributed-shared-memory store and an mbarrier wait instead of
 // an L2 round trip behind a GPU-scope fence and a polled flag; rows of earlier
 // groups come through the global flags as before. The ranks finish a group
@@ -166,6 +171,7 @@ template <typename T, int NR, int CL, bool FW = false>
 __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __restrict__ tiles, T* vec, int ld,
                                                       int cbase, int nch, int epoch, int lower) {
     static_assert(!FW || CL == 1, "the overlapped forward pass runs unclustered");
+    constexpr int FAN = CL - 1 < SOLVE_FANOUT ? CL - 1 : SOLVE_FANOUT;  // hand-over reach in ranks
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NV = 64 * NR;
     constexpr int PADE = 16 / (int)sizeof(T);  // elements of 16 bytes
@@ -288,7 +294,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
         auto rank_of = [&](int j) -> int {
             if constexpr (CL == 1) return -1;
             const int d = lower ? j - kk0 : (R - 1 - kk0) - j;
-            return d >= 0 && d < rank ? d : -1;
+            return d >= 0 && d < rank && rank - d <= FAN ? d : -1;
         };
         fl = s.flags + (size_t)ch * R;
         bool stop = false;
@@ -505,7 +511,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
 #pragma unroll
                     for (int r = 0; r < NR; r++) own[r] = y[r];
                     const uint32_t src = smem_addr(own);
-                    for (int dst = rank + 1; dst < CL; dst++) {
+                    for (int dst = rank + 1; dst < CL && dst <= rank + FAN; dst++) {
                         const uint32_t a = map_rank(src, (uint32_t)dst);
                         if constexpr ((NR * (int)sizeof(T)) % 16 == 0) {
 #pragma unroll
@@ -539,7 +545,7 @@ __global__ void __launch_bounds__(NT) trisolve_kernel(DevSolve s, const T* __res
                 if (lane == 0) asm volatile("fence.acq_rel.cluster;" ::: "memory");
                 __syncwarp();
                 const int dst = rank + 1 + lane;
-                if (dst < CL) mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
+                if (dst < CL && dst <= rank + FAN) mbar_arrive_remote(map_rank(smem_addr(&s_bar[rank]), (uint32_t)dst));
                 if (lane == 0 && stop) st_cluster_u32(map_rank(smem_addr(&s_cstop), 0), 1u);
             }
             __syncthreads();
@@ -971,6 +977,7 @@ int trisolve_upper_launch(const DevSolve& s, const float* tiles, float* vec, int
         const int ncl = std::max(1, std::min({clusters, groups, grid / CL}));
         auto kern = trisolve_kernel<float, 8, CL>;
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cl);
+        if (CL > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
