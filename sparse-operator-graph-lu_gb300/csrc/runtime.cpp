@@ -962,21 +962,29 @@ int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const do
     if (trisolve_lower_overlap_launch(dso, (const float*)s->tiles, s->d_v32, nrhs, s->epoch, grid2, s->stream2))
         return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     s->launches++;
+    // from here on every return waits for the forward pass on the second
+    // stream (its waits are bounded; a factorisation that cannot run is
+    // marked as given up below, which ends them at once)
+    struct Join {
+        cudaStream_t s2;
+        ~Join() { cudaStreamSynchronize(s2); }
+    } join{s->stream2};
     CK(cudaEventRecord(s->ev_lower, s->stream2));
     // the factor on the remaining SMs
     CK(cudaEventRecord(s->e0, st));
     const int fgrid = s->grid_factor - OVERLAP_SOLVE_SMS;
-    if (factor_ordered_launch(s->dt, (float*)s->tiles, fgrid, s->stages, st))
-        return fail(SOG_ECUDA, std::string("factor launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (factor_ordered_launch(s->dt, (float*)s->tiles, fgrid, s->stages, st)) {
+        const std::string m = cudaGetErrorString(cudaGetLastError());
+        static const int32_t gave_up = ST_TIMEOUT;
+        cudaMemcpy(&s->dt.status->flags, &gave_up, sizeof(gave_up), cudaMemcpyHostToDevice);
+        return fail(SOG_ECUDA, "factor launch: " + m);
+    }
     s->launches++;
     CK(cudaEventRecord(s->e1, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaEventElapsedTime(&s->t_factor, s->e0, s->e1));
     r = check_status(s, true);
-    if (r) {
-        cudaStreamSynchronize(s->stream2);
-        return r;
-    }
+    if (r) return r;
     s->factored = true;
     // the forward pass's positions not yet claimed, on the whole GPU
     {
@@ -988,10 +996,7 @@ int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const do
         s->launches++;
     }
     const int pr = check_pivots(s);
-    if (pr && pr != SOG_EPIVOT) {
-        cudaStreamSynchronize(s->stream2);
-        return pr;
-    }
+    if (pr && pr != SOG_EPIVOT) return pr;
     // the rest of the solve after the forward pass; the solve time counts
     // from the factor kernel's end (its event becomes the solve's start)
     std::swap(s->e0, s->e1);
