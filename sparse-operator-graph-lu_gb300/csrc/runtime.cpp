@@ -211,6 +211,9 @@ struct sog_system {
     unsigned long long* h_cnt = nullptr;
     std::vector<sog_solve_stats> seg_stats;
     int epoch = 2;
+    // epoch of the forward pass that overlapped the last factorisation (its
+    // backward pass takes fw_epoch + 1); reserved before that pass starts
+    int fw_epoch = 0;
     bool factored = false;
     float t_factor = 0, t_solve = 0;
     int grid_factor = 0;
@@ -662,14 +665,13 @@ int trisolve(sog_system* s, void* vec, int nrhs) {
 }
 
 // the upper pass of a mixed solve whose lower pass ran overlapped with the
-// factorisation (epoch s->epoch; the upper pass takes s->epoch + 1)
+// factorisation (epoch s->fw_epoch; the upper pass takes s->fw_epoch + 1)
 int trisolve_upper_only(sog_system* s, float* vec, int nrhs) {
     sog_ctx* c = s->ctx;
     const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));
     int grid = std::min(s->R * nch, trisolve_grid(false, nrhs, c->num_sms));
     if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
-    const int rc = trisolve_upper_launch(s->ds, (const float*)s->tiles, vec, nrhs, s->epoch + 1, grid, s->stream);
-    s->epoch += 2;
+    const int rc = trisolve_upper_launch(s->ds, (const float*)s->tiles, vec, nrhs, s->fw_epoch + 1, grid, s->stream);
     s->launches++;
     if (rc) return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     return SOG_OK;
@@ -919,7 +921,7 @@ constexpr int OVERLAP_SOLVE_SMS = 4;
 // factor then leaves OVERLAP_SOLVE_SMS SMs to that pass.
 int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const double* b_dev, double* x_dev,
                       sog_solve_stats* stats) {
-    const bool overlap = !s->fp64 && s->segs.size() == 1 && !s->tune_pending && !s->poisoned &&
+    const bool overlap = !s->fp64 && s->segs.size() == 1 && !s->tune_pending &&
                          s->opt.executor == SOG_EXEC_PERSISTENT && !s->opt.resident_compact && s->d_fwait_ptr &&
                          s->csr.ptr && (nrhs == 1 || (nrhs % 8 == 0 && nrhs <= 8 * TRISOLVE_MAX_CHUNKS)) &&
                          s->grid_factor > 2 * OVERLAP_SOLVE_SMS;
@@ -954,12 +956,16 @@ int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const do
     // forward pass on the second stream, after the inputs and the reset
     // completion flags
     CK(cudaStreamWaitEvent(s->stream2, s->ev_ready, 0));
+    // this solve's two epochs, reserved now: flags a pass that is cut short
+    // leaves behind never match a later pass
+    s->fw_epoch = s->epoch;
+    s->epoch += 2;
     DevSolve dso = s->ds;
     dso.fwait_ptr = s->d_fwait_ptr;
     dso.fwait = s->d_fwait;
     dso.task_done = s->dt.task_done;
     const int grid2 = std::min(OVERLAP_SOLVE_CTAS, s->R * std::max(1, nrhs / 8));
-    if (trisolve_lower_overlap_launch(dso, (const float*)s->tiles, s->d_v32, nrhs, s->epoch, grid2, s->stream2))
+    if (trisolve_lower_overlap_launch(dso, (const float*)s->tiles, s->d_v32, nrhs, s->fw_epoch, grid2, s->stream2))
         return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
     s->launches++;
     // from here on every return waits for the forward pass on the second
@@ -991,7 +997,7 @@ int factor_solve_impl(sog_system* s, const double* V_dev, int32_t nrhs, const do
         const int nch = std::max(1, std::min(nrhs / 8, TRISOLVE_MAX_CHUNKS));
         int grid = std::min(s->R * nch, trisolve_grid(false, nrhs, s->ctx->num_sms));
         if (s->opt.max_ctas > 0) grid = std::min(grid, s->opt.max_ctas);
-        if (trisolve_lower_join_launch(s->ds, (const float*)s->tiles, s->d_v32, nrhs, s->epoch, grid, st))
+        if (trisolve_lower_join_launch(s->ds, (const float*)s->tiles, s->d_v32, nrhs, s->fw_epoch, grid, st))
             return fail(SOG_ECUDA, std::string("solve launch: ") + cudaGetErrorString(cudaGetLastError()));
         s->launches++;
     }

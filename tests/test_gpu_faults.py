@@ -30,6 +30,39 @@ def test_poisoned_dependency_times_out_then_recovers(sg, wl, executor):
     ctx.close()
 
 
+def test_poisoned_factor_solve_times_out_then_recovers(sg, wl):
+    """The combined call with a factor task that never becomes ready: the
+    factor kernel's bounded wait runs out and the forward pass overlapping it
+    stops on the factorisation's status; the call returns SOG_ETIMEOUT. The
+    next combined call on the same system (with the flags the cut-short pass
+    left behind) gives the results of factor then solve bit for bit."""
+    import time
+    ctx = sg.Context()
+    s = wl.lap2d(128)
+    p = sg.Plan(s.n, s.rows, s.cols, s.vals)
+    ref = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10)
+    ref.factor(s.vals)
+    xr, _ = ref.solve(s.b)
+    sys_ = sg.System(ctx, p, precision=sg.MIXED, max_refine=20, tol=1e-10)
+    x0, _, _ = sys_.factor_solve(s.vals, s.b)
+    np.testing.assert_array_equal(x0, xr)
+    sys_.set_wait_limit(200.0)
+    ntasks = sys_.task_info()["tasks"]
+    assert sg.lib().sog_debug_poison_task(sys_._h, ntasks // 2) == 0
+    t0 = time.perf_counter()
+    with pytest.raises(sg.SOGError) as e:
+        sys_.factor_solve(s.vals, s.b)
+    assert e.value.code == sg.SOG_ETIMEOUT
+    assert time.perf_counter() - t0 < 10.0
+    assert sg.lib().sog_debug_unpoison(sys_._h) == 0
+    x, st, rc = sys_.factor_solve(s.vals, s.b)
+    assert rc == sg.SOG_OK
+    np.testing.assert_array_equal(x, xr)
+    sys_.close()
+    ref.close()
+    ctx.close()
+
+
 def test_solve_before_factor_is_state_error(sg, wl):
     ctx = sg.Context()
     s = wl.lap2d(16)
