@@ -141,20 +141,22 @@ constexpr int SOLVE_FANOUT = 7;
 // block multiplies, stages that row's NR-column slice in shared memory and
 // accumulates block * slice in registers (lane l: rows 2l, 2l+1). The warp
 // partials and b_i are combined and multiplied by the precomputed inverse of
-// the diagonal block. With a look-ahead product M = Dinv_i * B_{i,j} for the
-// neighbouring row j (i-1 for L, i+1 for U), block B_{i,j} is left out of the
-// sum and y_i = Dinv_i (b_i - sum) - M y_j is finished after row j is
-// published: the row's critical path is one 64x64 product. The row is then
-// published with a release store.
+// the diagonal block. With look-ahead products M_d = Dinv_i * B_{i,j_d} for
+// the SOLVE_LOOKAHEAD nearest rows j_d = i -+ d (d = 1, 2, ...), those blocks
+// are left out of the sum and y_i = Dinv_i (b_i - sum) - sum_d M_d y_{j_d}
+// is finished as the rows j_d are published, the farthest first: after the
+// nearest row arrives the critical path is one 64x64 product. A row from
+// global memory is staged in the warp's shared buffer before its product.
+// The row is then published with a release store.
 //
 // CL > 1 (a plain system, no dealing order): the CTAs of a thread-block
 // cluster take CL consecutive rows of one column chunk together (cluster rank
 // r: the r-th row in dealing order). A solved row is also stored straight into
 // the shared memory of the next SOLVE_FANOUT ranks of the cluster, with one
-// mbarrier arrival per receiving rank, so the hand-over between neighbouring rows of a
-// group is a distributed-shared-memory store and an mbarrier wait instead of
-// an L2 round trip behind a GPU-scope fence and a polled flag; rows of earlier
-// groups come through the global flags as before. The ranks finish a group
+// mbarrier arrival per receiving rank, so the hand-over between neighbouring
+// rows of a group is a distributed-shared-memory store and an mbarrier wait
+// instead of an L2 round trip behind a GPU-scope fence and a polled flag;
+// rows of earlier groups come through the global flags as before. The ranks finish a group
 // with a cluster barrier (their receive slots are then free), after which
 // rank 0's claim of the next group is read by all. Results are bit-identical
 // to CL = 1: the same products in the same order, only the source of the
