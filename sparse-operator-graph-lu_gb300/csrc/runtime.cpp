@@ -1776,7 +1776,8 @@ int sog_system_trace_enable(sog_system* s, int32_t on) {
 }
 
 int sog_system_trace_get(sog_system* s, uint64_t* task_trace, uint64_t* row_trace, int32_t* task_kind) {
-    if (!s || !s->trace) return fail(SOG_ESTATE, "trace not enabled");
+    if (!s) return fail(SOG_EINVAL, "NULL system");
+    if (!s->trace) return fail(SOG_ESTATE, "trace not enabled");
     CK(cudaSetDevice(s->ctx->device));
     CK(cudaStreamSynchronize(s->stream));
     if (task_trace)

@@ -106,3 +106,39 @@ def test_mtx_reader_triplets_parallel_and_cache(sg, wl, tmp_path):
     assert third[1].size == s.nnz + 1 and third[3][-1] == -0.5
     with pytest.raises(sg.SOGError):
         sg.read_mtx(str(tmp_path / "missing.mtx"))
+
+
+# entry points whose first argument is an opaque handle (plan, context,
+# system, server) or an array of them
+HANDLE_ENTRIES = [
+    "sog_plan_get_info", "sog_plan_export", "sog_plan_input_tiles", "sog_plan_segments", "sog_plan_task_graph_info",
+    "sog_ctx_pool_usage", "sog_ctx_stream", "sog_ctx_trim", "sog_system_create", "sog_system_bytes",
+    "sog_factor", "sog_factor_device", "sog_factor_tiles", "sog_solve", "sog_solve_device", "sog_factor_solve",
+    "sog_factor_solve_device", "sog_solve_permuted", "sog_solve_batch", "sog_solve_batch_device",
+    "sog_system_export_factors", "sog_system_last_times", "sog_system_task_info", "sog_system_executor",
+    "sog_system_pivots", "sog_system_set_stream", "sog_system_set_wait_limit", "sog_debug_poison_task",
+    "sog_debug_unpoison", "sog_debug_fp64_fragment_skip", "sog_system_trace_enable", "sog_system_trace_get",
+    "sog_system_task_graph", "sog_plan_merge", "sog_server_create", "sog_server_submit", "sog_server_wait",
+    "sog_server_solve", "sog_server_release", "sog_server_counters", "sog_mtx_info", "sog_mtx_copy",
+]
+
+
+def test_null_handles_are_rejected(sg):
+    """Every entry point that takes a handle answers a NULL handle (and NULL
+    outputs) with SOG_EINVAL, without touching the device; the destructors
+    accept NULL."""
+    L = sg.lib()
+    for name in HANDLE_ENTRIES:
+        f = getattr(L, name)
+        args = []
+        for t in f.argtypes:
+            if t is ctypes.c_void_p or t is ctypes.c_char_p:
+                args.append(None)
+            elif t is ctypes.c_double:
+                args.append(1.0)
+            else:
+                args.append(1)
+        assert f(*args) == sg.SOG_EINVAL, name
+    for name in ("sog_plan_destroy", "sog_ctx_destroy", "sog_system_destroy", "sog_server_destroy",
+                 "sog_mtx_destroy"):
+        getattr(L, name)(None)
